@@ -1,0 +1,362 @@
+"""Benchmark of the PulsarSr search hot path on GB300.
+
+Workload (default): the GBT L-band-shaped observation -- 96 x 1 MHz
+channels, 4-bit, 72 us, 531000 samples, seeded synthetic data with a
+4.6214 ms pulsar at DM 62.4, a 28.76 Hz zero-DM tone and 5 bursts -- searched
+over the default DM plan 0-500 (2000 trials, step 0.25006), RFI masking on,
+15-2000 Hz, threshold 8, 32 candidates per trial.
+
+A step is one whole search of the observation: unpack -> RFI mask -> for
+every trial DM dedisperse -> real FFT + power -> normalise -> harmonic sums
+-> per-trial candidate list.  metric: DM-trial*samples per second
+(trials x discovery samples / step time).
+
+  value : device-resident (packed payload already in HBM), CUDA events on the
+          session stream, L2 flushed (512 MB memset) before every step.
+  e2e   : through the public API with host buffers: payload H2D from pinned
+          memory, run, sync, candidate lists D2H, host wall clock.
+  --impl reference : the CPU restatement of the reference's path (the Rust
+          reference cannot be built here) timed on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import glob
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "search DM-trial*samples/s (GBT-shaped 2000-trial search)"
+UNIT = "DM-trial*samples/s"
+
+
+# ------------------------------------------------------------ cudart
+def cudart():
+    for p in ["libcudart.so"] + sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        try:
+            return C.CDLL(p)
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+class Events:
+    def __init__(self, rt):
+        self.rt = rt
+
+    def new(self):
+        e = C.c_void_p()
+        assert self.rt.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def record(self, e, stream):
+        assert self.rt.cudaEventRecord(e, C.c_void_p(stream)) == 0
+
+    def ms(self, a, b):
+        assert self.rt.cudaEventSynchronize(b) == 0
+        v = C.c_float()
+        assert self.rt.cudaEventElapsedTime(C.byref(v), a, b) == 0
+        return v.value
+
+
+# ------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows = []
+        self.proc = None
+        self.idx = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[0]) for r in self.rows if len(r) >= 8 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 8 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 8 for i in range(4)
+                          if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ workload
+def workload(name: str):
+    from pulsarsr_gb300 import dedisperse, synth
+    obs = synth.config_c2(2) if name == "c2" else synth.config_c1(1)
+    raw = obs.to_bytes()
+    freqs = obs.frequencies()
+    step = dedisperse.dm_step(freqs, obs.tsamp)
+    dm_max = 500.0 if name == "c2" else 120.0
+    trials = dedisperse.plan(0.0, dm_max, step if name == "c2" else 2.0)
+    md = int(dedisperse.delays(freqs, obs.tsamp, dm_max).max())
+    length = obs.nsamples - md
+    discovery = (length - md) // 2
+    return obs, raw, trials, discovery
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(stage, obs, trials, discovery, N):
+    """Algorithmic HBM bytes of one whole search, per stage."""
+    nt, nch, ns = len(trials), obs.nchans, obs.nsamples
+    M = N // 2
+    if stage == "dedisperse":      # samples read once + f32 series written
+        return nch * ns + 4 * nt * discovery
+    if stage == "fft":             # series read, complex work written+read, power written
+        return nt * (4 * discovery + 8 * M + 8 * M + 4 * (M + 1))
+    if stage == "spectrum":        # power read (scales) + power read (harmonics)
+        return nt * (2 * 4 * (M + 1))
+    if stage == "rfi":             # samples read (stats, medians) + written (fill)
+        return 3 * nch * ns
+    if stage == "unpack":          # packed payload read + u8 samples written
+        return (ns * nch * obs.nbits) // 8 + ns * nch
+    return 0
+
+
+def run_ours(args):
+    from pulsarsr_gb300 import fbank, search, session
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # plumbing only: barrier + max over ranks
+        dist.init_process_group("gloo")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rt = cudart()
+    rt.cudaSetDevice(C.c_int(local))
+    obs, raw, trials, discovery = workload(args.config)
+    hdr = fbank.parse_header(raw)
+    payload = np.frombuffer(raw, dtype=np.uint8)[hdr.data_offset:].copy()
+    # pinned host payload for the e2e leg
+    assert rt.cudaHostRegister(C.c_void_p(payload.ctypes.data), C.c_size_t(payload.nbytes),
+                               C.c_uint(0)) == 0
+    cfg = search.Config(min_hz=15.0, max_hz=2000.0, threshold=8.0, max_candidates=32)
+    block = max(int(0.1 / obs.tsamp), 32)
+    s = session.SearchSession(hdr, obs.nsamples, trials, discovery, cfg, block, 8.0)
+    s.load(payload)
+    flush = C.c_void_p()
+    FLUSH = 512 << 20
+    assert rt.cudaMalloc(C.byref(flush), C.c_size_t(FLUSH)) == 0
+    ev = Events(rt)
+    stream = s.stream
+    for _ in range(args.warmup):
+        s.run()
+        s.sync()
+    # ---- device-resident timing
+    if dist:
+        dist.barrier()
+    rt.cudaDeviceSynchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        rt.cudaMemsetAsync(flush, C.c_int(0), C.c_size_t(FLUSH), C.c_void_p(stream))
+        a, b = ev.new(), ev.new()
+        ev.record(a, stream)
+        s.run()
+        ev.record(b, stream)
+        s.sync()
+        times.append(ev.ms(a, b))
+    rt.cudaDeviceSynchronize()
+    clk = clocks.stop()
+    ms = statistics.mean(times)
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    units = len(trials) * discovery
+    value = world * units / (ms / 1e3)
+    counts, cands = s.candidates()
+    # ---- end to end through the public API with host buffers
+    e2e = []
+    for _ in range(max(args.steps // 2, 2)):
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        s.load(payload)
+        s.run()
+        s.sync()
+        c2, k2 = s.candidates()
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e)
+    d2h = counts.nbytes + len(trials) * 32 * 40
+    # ---- per-stage profile (separate runs; events per stage launch)
+    s.set_profiling(True)
+    s.stage_times(reset=True)
+    for _ in range(2):
+        rt.cudaMemsetAsync(flush, C.c_int(0), C.c_size_t(FLUSH), C.c_void_p(stream))
+        s.run()
+        s.sync()
+    st = s.stage_times()
+    s.set_profiling(False)
+    N = 2 * (1 << (discovery - 1).bit_length())
+    best = max(("dedisperse", "fft", "spectrum", "rfi"), key=lambda k: st[k][0])
+    peak, src = peaks()
+    stages = {}
+    for k in ("unpack", "rfi", "dedisperse", "fft", "spectrum"):
+        tot_ms, nl = st[k]
+        if nl == 0:
+            continue
+        per_launch_ms = tot_ms / nl
+        b = stage_bytes(k, obs, trials, discovery, N) * (2 / nl) if k in (
+            "dedisperse", "fft", "spectrum") else stage_bytes(k, obs, trials, discovery, N)
+        gbs = b / (per_launch_ms / 1e3) / 1e9
+        stages[k] = {"ms_per_search": round(tot_ms / 2, 4), "launches_per_search": nl // 2,
+                     "ms_per_launch": round(per_launch_ms, 5), "gbs": round(gbs, 1)}
+    nchunks = st["dedisperse"][1] // 2
+    fft_kernels = 2 if N // 2 > 4096 else 1
+    launches = 1 + 8 + nchunks * (2 + fft_kernels + 3)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    tot_ms, nl = st[best]
+    per_launch_ms = tot_ms / nl
+    algo = stage_bytes(best, obs, trials, discovery, N) * (2 / nl)
+    achieved = algo / (per_launch_ms / 1e3) / 1e9
+    cpu = cpu_baseline(obs, raw, trials, discovery, args) if not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/f32",
+        "data": "synthetic (seeded numpy generator, GBT L-band tutorial shape)",
+        "config": {"workload": f"{'GBT-shaped' if args.config == 'c2' else 'config-1'} search: "
+                               f"{obs.nchans} ch x {obs.nbits}-bit x {obs.nsamples} samples, "
+                               f"tsamp {obs.tsamp * 1e6:.0f} us, {len(trials)} DM trials, "
+                               f"discovery {discovery}, rFFT {N}, RFI on",
+                   "trials": len(trials), "discovery_samples": discovery,
+                   "l2": "flushed (512 MB memset) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(world * units / e2e_s, 1), "unit": UNIT,
+                "h2d_bytes_per_step": int(payload.nbytes), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": best, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": None, "peak_source": src},
+        "stages": stages,
+        "clocks": clk,
+        "candidates": int(counts.sum()),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(obs, raw, trials, discovery, args, sample_trials=None):
+    """The oracle (CPU restatement of the reference path) on a bounded sample:
+    decode + RFI once, then `sample_trials` trial DMs spread over the plan on
+    all host threads; the full-plan time is extrapolated per trial."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    nsample = sample_trials or max(2 * threads, 32)
+    t0 = time.perf_counter()
+    h, d = O.decode(raw)
+    block = max(int(0.1 / obs.tsamp), 32)
+    md, _ = O.rfi_mask(d, block, 8.0)
+    t_pre = time.perf_counter() - t0
+    pick = np.linspace(0, len(trials) - 1, nsample).astype(int)
+    t1 = time.perf_counter()
+    O.search_trials(md, obs.frequencies(), obs.tsamp, trials[pick], discovery, threads=threads,
+                    min_hz=15.0, max_hz=2000.0, threshold=8.0, max_candidates=32)
+    t_tr = time.perf_counter() - t1
+    full = t_pre + t_tr * len(trials) / nsample
+    value = len(trials) * discovery / full
+    return {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"decode+RFI once ({t_pre:.2f}s) + {nsample} of {len(trials)} trials "
+                      f"({t_tr:.2f}s on {threads} threads), extrapolated to the full plan "
+                      f"({full:.1f}s)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    obs, raw, trials, discovery = workload(args.config)
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_baseline(obs, raw, trials, discovery, args)
+        if i >= args.warmup:
+            vals.append(info["value"])
+    v = statistics.mean(vals)
+    info = dict(info)
+    info["value"] = round(v, 1)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": UNIT,
+            "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32/f64 (CPU)", "data": "synthetic",
+            "config": {"workload": "same observation and DM plan as the GPU arm",
+                       "trials": len(trials), "discovery_samples": discovery},
+            "cpu_baseline": info,
+            "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "PulsarSr is Rust; cargo/rustc are absent, so the timed CPU path is the "
+                    "C++ restatement of its search path (oracle/), validated against the "
+                    "reference's saved reports"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        from pulsarsr_gb300 import build
+        build.build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,216 @@
+/*
+ * libpsr - GB300 (sm_103a) implementation of the PulsarSr search path.
+ *
+ * A C ABI (plain pointers and sizes) whose functions mirror the reference's
+ * crate functions one to one, so a Rust `extern "C"` block (or ctypes, cgo,
+ * JNI ...) can bind them in place of the crate calls.  Each declaration cites
+ * the reference function it replaces (paths inside the PulsarSr project).
+ *
+ * Conventions
+ *   - Every function returns a status (PSR_OK == 0).  On failure the calling
+ *     thread's message is available from psr_last_error(); for the error kinds
+ *     that the reference reports through Display it carries the same text
+ *     ("invalid or unsupported filterbank: ...", "invalid dedispersion
+ *     input: ...").  Cases where the reference panics (assert!) return
+ *     PSR_EINVAL.
+ *   - Host buffers are allocated by the caller, with explicit capacities.
+ *     Opaque handles (psr_fb, psr_session) are freed by their psr_*_free.
+ *   - Arrays follow the reference layout: filterbank data is channel-major,
+ *     data[channel * nsamples + time], as in fbank::Filterbank.
+ *   - Handles are not shared between threads; each owns one CUDA stream.
+ *     Functions are reentrant.  Everything runs on the current CUDA device.
+ */
+#ifndef PSR_H
+#define PSR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PSR_OK = 0,
+  PSR_EIO = 1,          /* fbank::Error::Io */
+  PSR_EFORMAT = 2,      /* fbank::Error::Format */
+  PSR_EDEDISPERSE = 3,  /* dedisperse::Error */
+  PSR_EINVAL = 4,       /* a reference assert! / invalid argument */
+  PSR_ECUDA = 5,        /* CUDA runtime failure (message names the call) */
+  PSR_ETIMEOUT = 6,     /* a bounded device wait gave up */
+  PSR_ECAPACITY = 7     /* a caller buffer is too small (size reported) */
+};
+
+/* fbank::Header (fbank/src/lib.rs:29-38); keyword map omitted. */
+typedef struct {
+  int64_t nchans;
+  int64_t nbits;
+  double tsamp;
+  double fch1;
+  double foff;
+  int64_t data_offset;
+} psr_header;
+
+/* search::Candidate (search/src/lib.rs:6-13). */
+typedef struct {
+  double frequency_hz;
+  double period_s;
+  double dm;
+  uint64_t harmonics;
+  double score;
+} psr_candidate;
+
+/* search::Config (search/src/lib.rs:14-32); birdies are (center, half width)
+ * pairs, 2*nbirdies doubles. */
+typedef struct {
+  double min_hz;
+  double max_hz;
+  double threshold;
+  uint64_t max_candidates;
+  const double *birdies;
+  uint64_t nbirdies;
+} psr_search_config;
+
+/* fold::Profile scalars (fold/src/lib.rs:3-11); bins/counts are arrays. */
+typedef struct {
+  double period_s;
+  double snr;
+  double reduced_chi_square;
+} psr_profile_stats;
+
+/* confirmation::Measurement (search/src/confirmation.rs:52-59). */
+typedef struct {
+  double snr;
+  uint64_t on_samples;
+  uint64_t off_samples;
+  double mean_difference;
+  double standard_error;
+} psr_measurement;
+
+/* Library version string ("pulsarsr-gb300 <semver> sm_103a"). */
+const char *psr_version(void);
+/* Copy the calling thread's last error message (NUL-terminated, truncated
+ * to len).  Returns the full message length. */
+uint64_t psr_last_error(char *buf, uint64_t len);
+
+/* ------------------------------------------------------------- fbank */
+/* fbank::parse_header (fbank/src/lib.rs:72-147), host. */
+int psr_parse_header(const uint8_t *bytes, uint64_t len, psr_header *out);
+
+/* Device-resident filterbank: the decoded samples live in HBM, channel-major,
+ * stored in their integer width (u8 for nbits <= 8, u16, or f32). */
+typedef struct psr_fb psr_fb;
+/* fbank::decode (fbank/src/lib.rs:149-196): header parsed on the host, the
+ * packed payload copied once to the device and unpacked there. */
+int psr_fb_decode(const uint8_t *bytes, uint64_t len, int64_t limit /* <0: none */,
+                  psr_fb **out);
+int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples);
+/* Filterbank.data as f32, channel-major (nchans * nsamples values). */
+int psr_fb_download(const psr_fb *fb, float *out);
+void psr_fb_free(psr_fb *fb);
+
+/* --------------------------------------------------------------- rfi */
+/* rfi::median (rfi/src/lib.rs:4-12): upper median, exact, on the device. */
+int psr_median(const float *values, uint64_t n, float *out);
+/* rfi::mask (rfi/src/lib.rs:31-96) applied in place to the device samples.
+ * channels has room for nchans entries; blocks for blocks_cap entries. */
+int psr_rfi_mask(psr_fb *fb, uint64_t block_samples, float threshold,
+                 uint64_t *channels, uint64_t *nchannels_bad, uint64_t *blocks,
+                 uint64_t blocks_cap, uint64_t *nblocks_bad,
+                 double *masked_fraction);
+
+/* -------------------------------------------------------- dedisperse */
+/* dedisperse::delays (dedisperse/src/lib.rs:9-34), host FP64, bit-exact. */
+int psr_delays(const double *freqs, uint64_t nchans, double tsamp, double dm,
+               uint64_t *out);
+/* dedisperse::dm_step (dedisperse/src/lib.rs:35-44). */
+int psr_dm_step(const double *freqs, uint64_t nchans, double tsamp, double *out);
+/* dedisperse::plan (dedisperse/src/lib.rs:45-60); *n receives the trial
+ * count even when cap is too small (then PSR_ECAPACITY). */
+int psr_plan(double dm_min, double dm_max, double step, double *out,
+             uint64_t cap, uint64_t *n);
+/* dedisperse::apply (dedisperse/src/lib.rs:61-90) on a device filterbank.
+ * length < 0 means the longest valid output.  out holds *n_out floats. */
+int psr_dedisperse(const psr_fb *fb, const uint64_t *delays, int64_t length,
+                   float *out, uint64_t cap, uint64_t *n_out);
+/* Many trials at once: out is [ntrials][length] (the CLI loop,
+ * cli/src/main.rs:462-469, without the periodicity step). */
+int psr_dedisperse_trials(const psr_fb *fb, const double *trials,
+                          uint64_t ntrials, uint64_t length, float *out);
+
+/* ------------------------------------------------------------ search */
+/* The raw power spectrum of search::periodicity (search/src/lib.rs:35-44):
+ * mean removal, zero padding to N = 2*next_pow2(len), real FFT, |X|^2.
+ * out holds N/2 + 1 floats. */
+int psr_raw_power(const float *series, uint64_t len, float *out);
+/* search::periodicity (search/src/lib.rs:33-145) on one host series. */
+int psr_periodicity(const float *series, uint64_t len, double tsamp, double dm,
+                    const psr_search_config *cfg, psr_candidate *out,
+                    uint64_t cap, uint64_t *n);
+/* The psr search trial loop (cli/src/main.rs:462-473): for every trial DM,
+ * delays -> apply(discovery) -> periodicity, candidates concatenated in trial
+ * order.  counts[i] gets trial i's count; *n_total the total. */
+int psr_search_trials(const psr_fb *fb, const double *trials, uint64_t ntrials,
+                      uint64_t discovery, const psr_search_config *cfg,
+                      uint64_t *counts, psr_candidate *out, uint64_t cap,
+                      uint64_t *n_total);
+/* search::sift (search/src/lib.rs:147-176), host. */
+int psr_sift(const psr_candidate *in, uint64_t n, double resolution_hz,
+             uint64_t limit, int reject_dm_zero, psr_candidate *out,
+             uint64_t *n_out);
+
+/* -------------------------------------------------------------- fold */
+/* fold::profile_at (fold/src/lib.rs:16-80); values/counts hold bins entries. */
+int psr_profile_at(const float *series, uint64_t n, double tsamp, double period,
+                   uint64_t bins, uint64_t sample_offset,
+                   psr_profile_stats *stats, float *values, uint64_t *counts);
+/* fold::refine (fold/src/lib.rs:81-97): all steps+1 folds in one launch. */
+int psr_refine(const float *series, uint64_t n, double tsamp, double frequency,
+               double span_hz, uint64_t steps, uint64_t bins,
+               psr_profile_stats *stats, float *values, uint64_t *counts);
+/* confirmation::measure (search/src/confirmation.rs:107-141). */
+int psr_measure(const float *x, uint64_t n, uint64_t offset, double tsamp,
+                double period, uint64_t start_bin, uint64_t width_bins,
+                uint64_t bins, psr_measurement *out);
+
+/* ----------------------------------------------------------- session */
+/* A whole search of one observation shape kept resident on the device:
+ * packed payload -> unpack -> RFI mask -> trial loop -> per-trial candidate
+ * lists.  Buffers are allocated once at creation, so run() allocates
+ * nothing; this is the call a survey pipeline repeats per observation.
+ * rfi_block_samples == 0 disables masking (psr search --no-rfi). */
+typedef struct psr_session psr_session;
+int psr_session_create(const psr_header *header, uint64_t nsamples,
+                       const double *trials, uint64_t ntrials,
+                       uint64_t discovery, const psr_search_config *cfg,
+                       uint64_t rfi_block_samples, float rfi_threshold,
+                       psr_session **out);
+/* Copy a packed payload (the bytes after the header) from host memory. */
+int psr_session_load(psr_session *s, const uint8_t *payload, uint64_t nbytes);
+/* Enqueue unpack + mask + search on the session stream (asynchronous). */
+int psr_session_run(psr_session *s);
+/* Wait for the session stream; reports device-side errors. */
+int psr_session_sync(psr_session *s);
+/* Results of the last run (after sync). */
+int psr_session_candidates(psr_session *s, uint64_t *counts, psr_candidate *out,
+                           uint64_t cap, uint64_t *n_total);
+int psr_session_mask(psr_session *s, uint64_t *channels, uint64_t *nchannels_bad,
+                     uint64_t *blocks, uint64_t blocks_cap, uint64_t *nblocks_bad,
+                     double *masked_fraction);
+/* Diagnostics with no counterpart in the reference (which only times whole
+ * runs, cli/src/main.rs:415): when enabled, run() records CUDA events around
+ * every stage on the session stream.  stage_times() fills ms[5] and
+ * launches[5] for (unpack, rfi, dedisperse, fft, spectrum), summed over the
+ * runs since the last reset. */
+int psr_session_set_profiling(psr_session *s, int enable);
+int psr_session_stage_times(psr_session *s, double *ms, uint64_t *launches, int reset);
+/* Device copy of the packed payload buffer (for device-resident timing). */
+void *psr_session_payload_device(psr_session *s);
+/* The session's CUDA stream (cudaStream_t), for event timing. */
+void *psr_session_stream(psr_session *s);
+void psr_session_free(psr_session *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PSR_H */

@@ -1,0 +1,910 @@
+// C ABI of libpsr: host-side logic that stays on the host in the reference's
+// own terms (header parsing, FP64 delay tables, DM plans, sifting) and the
+// entry points that drive the device kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "psr_internal.h"
+#include "search.h"
+
+namespace psr {
+
+namespace {
+thread_local std::string g_error;
+const double K_DM = 4148.808;  // dedisperse/src/lib.rs:3
+}  // namespace
+
+void set_error(const std::string &msg) { g_error = msg; }
+const std::string &last_error() { return g_error; }
+
+// ------------------------------------------------------- fbank header
+namespace {
+bool rd_string(const uint8_t *b, uint64_t len, uint64_t &pos, std::string &out, int &code) {
+  if (pos + 4 > len) {
+    set_error("failed to fill whole buffer");
+    code = PSR_EIO;
+    return false;
+  }
+  int32_t n;
+  std::memcpy(&n, b + pos, 4);
+  pos += 4;
+  if (n < 1 || n > 4096) {
+    set_error("invalid or unsupported filterbank: bad string length " + std::to_string(n));
+    code = PSR_EFORMAT;
+    return false;
+  }
+  if (pos + (uint64_t)n > len) {
+    set_error("failed to fill whole buffer");
+    code = PSR_EIO;
+    return false;
+  }
+  out.assign(reinterpret_cast<const char *>(b + pos), (size_t)n);
+  pos += (uint64_t)n;
+  return true;
+}
+}  // namespace
+
+// fbank::parse_header (fbank/src/lib.rs:72-147): strict keyword table.
+int parse_header(const uint8_t *b, uint64_t len, psr_header &h) {
+  static const char *kInts[] = {"machine_id", "telescope_id", "data_type", "barycentric",
+                                "pulsarcentric", "nbits", "nsamples", "nchans", "nifs",
+                                "nbeams", "ibeam", "signed"};
+  static const char *kFloats[] = {"az_start", "za_start", "src_raj", "src_dej", "tstart",
+                                  "tsamp", "fch1", "foff", "refdm", "period"};
+  struct V {
+    int kind;
+    int32_t i;
+    double f;
+  };
+  uint64_t pos = 0;
+  int code = PSR_OK;
+  std::string s;
+  if (!rd_string(b, len, pos, s, code)) return code;
+  if (s != "HEADER_START") {
+    set_error("invalid or unsupported filterbank: missing HEADER_START");
+    return PSR_EFORMAT;
+  }
+  std::map<std::string, V> f;
+  for (;;) {
+    std::string key;
+    if (!rd_string(b, len, pos, key, code)) return code;
+    if (key == "HEADER_END") break;
+    V v{};
+    if (key == "rawdatafile" || key == "source_name") {
+      std::string t;
+      if (!rd_string(b, len, pos, t, code)) return code;
+      v.kind = 2;
+    } else if (std::any_of(std::begin(kInts), std::end(kInts),
+                           [&](const char *k) { return key == k; })) {
+      if (pos + 4 > len) {
+        set_error("failed to fill whole buffer");
+        return PSR_EIO;
+      }
+      v.kind = 0;
+      std::memcpy(&v.i, b + pos, 4);
+      pos += 4;
+    } else if (std::any_of(std::begin(kFloats), std::end(kFloats),
+                           [&](const char *k) { return key == k; })) {
+      if (pos + 8 > len) {
+        set_error("failed to fill whole buffer");
+        return PSR_EIO;
+      }
+      v.kind = 1;
+      std::memcpy(&v.f, b + pos, 8);
+      pos += 8;
+    } else {
+      set_error("invalid or unsupported filterbank: unknown keyword " + key +
+                "; cannot infer its type safely");
+      return PSR_EFORMAT;
+    }
+    if (!f.emplace(key, v).second) {
+      set_error("invalid or unsupported filterbank: duplicate " + key);
+      return PSR_EFORMAT;
+    }
+  }
+  auto geti = [&](const char *k, int32_t &out) {
+    auto it = f.find(k);
+    if (it == f.end() || it->second.kind != 0) {
+      set_error(std::string("invalid or unsupported filterbank: missing integer ") + k);
+      return false;
+    }
+    out = it->second.i;
+    return true;
+  };
+  auto getf = [&](const char *k, double &out) {
+    auto it = f.find(k);
+    if (it == f.end() || it->second.kind != 1 || !std::isfinite(it->second.f)) {
+      set_error(std::string("invalid or unsupported filterbank: missing/invalid float ") + k);
+      return false;
+    }
+    out = it->second.f;
+    return true;
+  };
+  int32_t nchans, nbits;
+  double tsamp, fch1, foff;
+  if (!geti("nchans", nchans) || !geti("nbits", nbits) || !getf("tsamp", tsamp) ||
+      !getf("fch1", fch1) || !getf("foff", foff))
+    return PSR_EFORMAT;
+  if (nchans <= 0 || tsamp <= 0.0 ||
+      !(nbits == 1 || nbits == 2 || nbits == 4 || nbits == 8 || nbits == 16 || nbits == 32)) {
+    set_error("invalid or unsupported filterbank: invalid nchans/tsamp/nbits");
+    return PSR_EFORMAT;
+  }
+  auto bad_int = [&](const char *k, int32_t want) {
+    auto it = f.find(k);
+    return it != f.end() && !(it->second.kind == 0 && it->second.i == want);
+  };
+  if (bad_int("nifs", 1)) {
+    set_error("invalid or unsupported filterbank: only nifs=1 supported");
+    return PSR_EFORMAT;
+  }
+  if (bad_int("signed", 0)) {
+    set_error("invalid or unsupported filterbank: signed integer samples unsupported");
+    return PSR_EFORMAT;
+  }
+  if (bad_int("data_type", 1)) {
+    set_error("invalid or unsupported filterbank: only filterbank data_type=1 supported");
+    return PSR_EFORMAT;
+  }
+  for (int32_t c = 0; c < nchans; ++c) {
+    const double fr = fch1 + (double)c * foff;
+    if (!std::isfinite(fr) || fr <= 0.0) {
+      set_error("invalid or unsupported filterbank: nonpositive frequency");
+      return PSR_EFORMAT;
+    }
+  }
+  h.nchans = nchans;
+  h.nbits = nbits;
+  h.tsamp = tsamp;
+  h.fch1 = fch1;
+  h.foff = foff;
+  h.data_offset = (int64_t)pos;
+  return PSR_OK;
+}
+
+// dedisperse::delays (dedisperse/src/lib.rs:9-34); powi(-2) is 1/(f*f).
+bool host_delays(const double *f, size_t n, double tsamp, double dm, std::vector<uint64_t> &out) {
+  bool bad = n == 0 || !std::isfinite(tsamp) || tsamp <= 0.0 || !std::isfinite(dm) || dm < 0.0;
+  for (size_t i = 0; i < n && !bad; ++i) bad = !std::isfinite(f[i]) || f[i] <= 0.0;
+  if (bad) {
+    set_error(
+        "invalid dedispersion input: positive frequencies/tsamp and nonnegative DM required");
+    return false;
+  }
+  double ref = 0.0;
+  for (size_t i = 0; i < n; ++i) ref = std::fmax(ref, f[i]);
+  const double rinv = 1.0 / (ref * ref);
+  out.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    const double s = std::round(K_DM * dm * (1.0 / (f[i] * f[i]) - rinv) / tsamp);
+    if (s > 18446744073709551615.0) {
+      set_error("invalid dedispersion input: delay overflow");
+      return false;
+    }
+    out[i] = s > 0.0 ? (uint64_t)s : 0;
+  }
+  return true;
+}
+
+namespace {
+
+struct Stream {
+  cudaStream_t s = nullptr;
+  Stream() { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); }
+  ~Stream() {
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+// Decode the header and stage the payload on the device (fbank/src/lib.rs:149-170).
+int obs_from_bytes(const uint8_t *bytes, uint64_t len, int64_t limit, DeviceObs &o,
+                   cudaStream_t st) {
+  PSR_TRY(parse_header(bytes, len, o.h));
+  const uint64_t plen = len - (uint64_t)o.h.data_offset;
+  const uint64_t bpf = (uint64_t)o.h.nchans * (uint64_t)o.h.nbits;
+  const uint64_t bits = plen * 8;
+  if (bits % bpf != 0) {
+    set_error("invalid or unsupported filterbank: truncated frame or packed padding unsupported");
+    return PSR_EFORMAT;
+  }
+  const uint64_t total = bits / bpf;
+  const uint64_t ns = limit < 0 ? total : std::min<uint64_t>((uint64_t)limit, total);
+  if (ns < 2) {
+    set_error("invalid or unsupported filterbank: need at least two samples");
+    return PSR_EFORMAT;
+  }
+  o.ns = ns;
+  o.nch = (uint64_t)o.h.nchans;
+  o.kind = kind_for_bits(o.h.nbits);
+  o.payload_bytes = (ns * bpf + 7) / 8;
+  PSR_TRY(o.payload.ensure(o.payload_bytes + 16));
+  PSR_CUDA(cudaMemcpyAsync(o.payload.p, bytes + o.h.data_offset, o.payload_bytes,
+                           cudaMemcpyHostToDevice, st));
+  PSR_TRY(o.alloc());
+  return PSR_OK;
+}
+
+int unpack_checked(DeviceObs &o, DevBuf &errbuf, cudaStream_t st) {
+  PSR_TRY(errbuf.ensure(8));
+  PSR_CUDA(cudaMemsetAsync(errbuf.p, 0xff, 8, st));
+  PSR_TRY(launch_unpack(o, errbuf.as<unsigned long long>(), st));
+  unsigned long long e = 0;
+  PSR_CUDA(cudaMemcpyAsync(&e, errbuf.p, 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  if (e != ~0ull) {
+    set_error("invalid or unsupported filterbank: nonfinite sample at " +
+              std::to_string(e / o.nch) + "/" + std::to_string(e % o.nch));
+    return PSR_EFORMAT;
+  }
+  return PSR_OK;
+}
+
+bool valid_config(const psr_search_config *c) {
+  return c && c->max_candidates >= 1 && c->max_candidates <= 64 && !std::isnan(c->min_hz) &&
+         !std::isnan(c->max_hz) && !std::isnan(c->threshold) && (c->nbirdies == 0 || c->birdies);
+}
+
+SpecConfig to_spec(const psr_search_config *c, double tsamp) {
+  SpecConfig s;
+  s.tsamp = tsamp;
+  s.min_hz = c->min_hz;
+  s.max_hz = c->max_hz;
+  s.threshold = c->threshold;
+  s.max_candidates = c->max_candidates;
+  s.birdies.assign(c->birdies, c->birdies + 2 * c->nbirdies);
+  return s;
+}
+
+// A filterbank made from a host f32 array (channel-major), for the entry
+// points that take host series or arrays.
+int obs_from_f32(const float *data, uint64_t nch, uint64_t ns, double tsamp, DeviceObs &o,
+                 cudaStream_t st) {
+  o.h = psr_header{(int64_t)nch, 32, tsamp, 1.0, 0.0, 0};
+  o.ns = ns;
+  o.nch = nch;
+  o.kind = SAMPLE_F32;
+  PSR_TRY(o.alloc());
+  PSR_CUDA(cudaMemcpy2DAsync(o.samples.p, o.ld * 4, data, ns * 4, ns * 4, nch,
+                             cudaMemcpyHostToDevice, st));
+  return PSR_OK;
+}
+
+}  // namespace
+}  // namespace psr
+
+using namespace psr;
+
+struct psr_fb {
+  DeviceObs o;
+  Stream stream;
+};
+
+struct psr_session {
+  DeviceObs o;
+  Stream stream;
+  RfiWork rfi;
+  RfiResult rfi_res;
+  uint64_t rfi_block = 0;
+  float rfi_threshold = 8.0f;
+  SearchEngine eng;
+  DevBuf errbuf;
+  bool have_run = false;
+  // unpack / rfi timing (the engine times its own stages)
+  std::vector<cudaEvent_t> ev[2][2];
+  double pre_ms[2] = {0, 0};
+  uint64_t pre_launches[2] = {0, 0};
+  int mark(int stage, int which) {
+    if (!eng.profile) return PSR_OK;
+    cudaEvent_t e;
+    PSR_CUDA(cudaEventCreate(&e));
+    PSR_CUDA(cudaEventRecord(e, stream.s));
+    ev[stage][which].push_back(e);
+    if (which) pre_launches[stage] += 1;
+    return PSR_OK;
+  }
+  int harvest() {
+    for (int st = 0; st < 2; ++st) {
+      for (size_t i = 0; i < ev[st][0].size() && i < ev[st][1].size(); ++i) {
+        float ms = 0.0f;
+        PSR_CUDA(cudaEventElapsedTime(&ms, ev[st][0][i], ev[st][1][i]));
+        pre_ms[st] += ms;
+      }
+      for (int w = 0; w < 2; ++w) {
+        for (cudaEvent_t e : ev[st][w]) cudaEventDestroy(e);
+        ev[st][w].clear();
+      }
+    }
+    return PSR_OK;
+  }
+  ~psr_session() {
+    for (int st = 0; st < 2; ++st)
+      for (int w = 0; w < 2; ++w)
+        for (cudaEvent_t e : ev[st][w]) cudaEventDestroy(e);
+  }
+};
+
+namespace psr {
+template <class T>
+__global__ void k_to_f32(const T *s, uint64_t ld, uint64_t ns, uint64_t nch, float *out) {
+  const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= ns * nch) return;
+  const uint64_t c = id / ns, t = id % ns;
+  out[id] = (float)s[c * ld + t];
+}
+
+}  // namespace psr
+
+extern "C" {
+
+const char *psr_version(void) { return "pulsarsr-gb300 0.1.0 sm_103a"; }
+
+uint64_t psr_last_error(char *buf, uint64_t len) {
+  const std::string &e = last_error();
+  if (buf && len) {
+    const uint64_t n = std::min<uint64_t>(len - 1, e.size());
+    std::memcpy(buf, e.data(), n);
+    buf[n] = 0;
+  }
+  return e.size();
+}
+
+int psr_parse_header(const uint8_t *bytes, uint64_t len, psr_header *out) {
+  if (!bytes || !out) {
+    set_error("parse_header: null argument");
+    return PSR_EINVAL;
+  }
+  return parse_header(bytes, len, *out);
+}
+
+int psr_fb_decode(const uint8_t *bytes, uint64_t len, int64_t limit, psr_fb **out) {
+  if (!bytes || !out) {
+    set_error("decode: null argument");
+    return PSR_EINVAL;
+  }
+  std::unique_ptr<psr_fb> fb(new psr_fb());
+  PSR_TRY(obs_from_bytes(bytes, len, limit, fb->o, fb->stream.s));
+  DevBuf e;
+  PSR_TRY(unpack_checked(fb->o, e, fb->stream.s));
+  *out = fb.release();
+  return PSR_OK;
+}
+
+int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples) {
+  if (!fb) {
+    set_error("fb_info: null handle");
+    return PSR_EINVAL;
+  }
+  if (header) *header = fb->o.h;
+  if (nsamples) *nsamples = fb->o.ns;
+  return PSR_OK;
+}
+
+int psr_fb_download(const psr_fb *fb, float *out) {
+  if (!fb || !out) {
+    set_error("fb_download: null argument");
+    return PSR_EINVAL;
+  }
+  const DeviceObs &o = fb->o;
+  cudaStream_t st = fb->stream.s;
+  DevBuf tmp;
+  PSR_TRY(tmp.ensure(o.ns * o.nch * 4));
+  const unsigned g = (unsigned)((o.ns * o.nch + 255) / 256);
+  switch (o.kind) {
+    case SAMPLE_U8: k_to_f32<uint8_t><<<g, 256, 0, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns, o.nch, tmp.as<float>()); break;
+    case SAMPLE_U16: k_to_f32<uint16_t><<<g, 256, 0, st>>>(o.samples.as<uint16_t>(), o.ld, o.ns, o.nch, tmp.as<float>()); break;
+    default: k_to_f32<float><<<g, 256, 0, st>>>(o.samples.as<float>(), o.ld, o.ns, o.nch, tmp.as<float>());
+  }
+  PSR_CUDA(cudaGetLastError());
+  PSR_CUDA(cudaMemcpyAsync(out, tmp.p, o.ns * o.nch * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  return PSR_OK;
+}
+
+void psr_fb_free(psr_fb *fb) { delete fb; }
+
+int psr_median(const float *values, uint64_t n, float *out) {
+  if (!out || (n && !values)) {
+    set_error("median: null argument");
+    return PSR_EINVAL;
+  }
+  Stream s;
+  DevBuf v, r;
+  PSR_TRY(v.ensure(std::max<uint64_t>(n, 1) * 4));
+  PSR_TRY(r.ensure(4));
+  if (n) PSR_CUDA(cudaMemcpyAsync(v.p, values, n * 4, cudaMemcpyHostToDevice, s.s));
+  PSR_TRY(launch_median_f32(v.as<float>(), n, r.as<float>(), nullptr, s.s));
+  PSR_CUDA(cudaMemcpyAsync(out, r.p, 4, cudaMemcpyDeviceToHost, s.s));
+  PSR_CUDA(cudaStreamSynchronize(s.s));
+  return PSR_OK;
+}
+
+int psr_rfi_mask(psr_fb *fb, uint64_t block_samples, float threshold, uint64_t *channels,
+                 uint64_t *nchannels_bad, uint64_t *blocks, uint64_t blocks_cap,
+                 uint64_t *nblocks_bad, double *masked_fraction) {
+  if (!fb || !nchannels_bad || !nblocks_bad || !masked_fraction) {
+    set_error("rfi::mask: null argument");
+    return PSR_EINVAL;
+  }
+  RfiWork w;
+  RfiResult res;
+  PSR_TRY(rfi_enqueue(fb->o, block_samples, threshold, w, fb->stream.s));
+  PSR_TRY(rfi_collect(fb->o, block_samples, w, fb->stream.s, res));
+  *nchannels_bad = res.channels.size();
+  if (channels) std::copy(res.channels.begin(), res.channels.end(), channels);
+  *nblocks_bad = res.blocks.size();
+  if (blocks)
+    for (uint64_t i = 0; i < res.blocks.size() && i < blocks_cap; ++i) blocks[i] = res.blocks[i];
+  *masked_fraction = res.masked_fraction;
+  if (res.blocks.size() > blocks_cap && blocks) {
+    set_error("rfi::mask: blocks buffer too small");
+    return PSR_ECAPACITY;
+  }
+  return PSR_OK;
+}
+
+int psr_delays(const double *freqs, uint64_t nchans, double tsamp, double dm, uint64_t *out) {
+  std::vector<uint64_t> d;
+  if (!host_delays(freqs, nchans, tsamp, dm, d)) return PSR_EDEDISPERSE;
+  std::copy(d.begin(), d.end(), out);
+  return PSR_OK;
+}
+
+int psr_dm_step(const double *f, uint64_t n, double tsamp, double *out) {
+  std::vector<uint64_t> tmp;
+  if (!host_delays(f, n, tsamp, 0.0, tmp)) return PSR_EDEDISPERSE;
+  double lo = INFINITY, hi = 0.0;
+  for (uint64_t i = 0; i < n; ++i) {
+    lo = std::fmin(lo, f[i]);
+    hi = std::fmax(hi, f[i]);
+  }
+  const double span = K_DM * (1.0 / (lo * lo) - 1.0 / (hi * hi));
+  if (span <= 0.0) {
+    set_error("invalid dedispersion input: DM planning requires finite bandwidth");
+    return PSR_EDEDISPERSE;
+  }
+  *out = tsamp / span;
+  return PSR_OK;
+}
+
+int psr_plan(double mn, double mx, double step, double *out, uint64_t cap, uint64_t *n) {
+  if (!std::isfinite(mn) || !std::isfinite(mx) || !std::isfinite(step) || mn < 0.0 || mx < mn ||
+      step <= 0.0) {
+    set_error("invalid dedispersion input: invalid DM bounds/step");
+    return PSR_EDEDISPERSE;
+  }
+  const uint64_t cnt = (uint64_t)std::floor((mx - mn) / step) + 1;
+  if (cnt > 100000) {
+    set_error("invalid dedispersion input: more than 100000 DM trials");
+    return PSR_EDEDISPERSE;
+  }
+  *n = cnt;
+  if (out && cap < cnt) {
+    set_error("plan: output buffer too small");
+    return PSR_ECAPACITY;
+  }
+  if (out)
+    for (uint64_t i = 0; i < cnt; ++i) out[i] = mn + (double)i * step;
+  return PSR_OK;
+}
+
+namespace {
+uint64_t series_ld_(uint64_t n) { return series_ld(n); }
+
+// Dedisperse with explicit per-channel delays (one trial) on a device obs.
+int dedisperse_delays(const DeviceObs &o, const uint64_t *d, int64_t length, float *out,
+                      uint64_t cap, uint64_t *n_out, cudaStream_t st) {
+  uint64_t maxd = 0;
+  for (uint64_t c = 0; c < o.nch; ++c) maxd = std::max(maxd, d[c]);
+  if (maxd > o.ns) {
+    set_error("invalid dedispersion input: delay exceeds observation");
+    return PSR_EDEDISPERSE;
+  }
+  const uint64_t avail = o.ns - maxd;
+  const uint64_t n = length < 0 ? avail : (uint64_t)length;
+  if (n < 2 || n > avail) {
+    set_error("invalid dedispersion input: invalid output length");
+    return PSR_EDEDISPERSE;
+  }
+  *n_out = n;
+  if (!out) return PSR_OK;
+  if (cap < n) {
+    set_error("dedisperse: output buffer too small");
+    return PSR_ECAPACITY;
+  }
+  std::vector<uint32_t> tab(o.nch);
+  for (uint64_t c = 0; c < o.nch; ++c) tab[c] = (uint32_t)d[c];
+  uint64_t spread = 0;
+  DevBuf dd, ser, parts, sums, err;
+  PSR_TRY(dd.ensure(o.nch * 4));
+  PSR_CUDA(cudaMemcpyAsync(dd.p, tab.data(), o.nch * 4, cudaMemcpyHostToDevice, st));
+  const uint64_t ldo = series_ld_(n);
+  PSR_TRY(ser.ensure(ldo * 4 + 256));
+  PSR_TRY(parts.ensure(((n + 1023) / 1024 + 8) * 8));
+  PSR_TRY(sums.ensure(8));
+  PSR_TRY(err.ensure(8));
+  PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
+  PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), 1, n, ser.as<float>(), ldo,
+                               parts.as<double>(), sums.as<double>(), spread, err.as<unsigned>(),
+                               st));
+  PSR_CUDA(cudaMemcpyAsync(out, ser.p, n * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  return PSR_OK;
+}
+}  // namespace
+
+int psr_dedisperse(const psr_fb *fb, const uint64_t *delays, int64_t length, float *out,
+                   uint64_t cap, uint64_t *n_out) {
+  if (!fb || !delays || !n_out) {
+    set_error("invalid dedispersion input: array shape mismatch");
+    return PSR_EDEDISPERSE;
+  }
+  return dedisperse_delays(fb->o, delays, length, out, cap, n_out, fb->stream.s);
+}
+
+int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntrials,
+                          uint64_t length, float *out) {
+  if (!fb || !trials || !out || ntrials == 0) {
+    set_error("dedisperse_trials: null argument or empty plan");
+    return PSR_EINVAL;
+  }
+  const DeviceObs &o = fb->o;
+  cudaStream_t st = fb->stream.s;
+  std::vector<uint32_t> tab;
+  uint64_t spread = 0, maxd = 0;
+  PSR_TRY(make_delay_table(o, trials, ntrials, tab, spread, maxd));
+  if (length < 2 || length > o.ns - maxd) {
+    set_error("invalid dedispersion input: invalid output length");
+    return PSR_EDEDISPERSE;
+  }
+  const uint64_t ldo = series_ld(length);
+  DevBuf dd, ser, parts, sums, err;
+  PSR_TRY(dd.ensure(tab.size() * 4));
+  PSR_CUDA(cudaMemcpyAsync(dd.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st));
+  PSR_TRY(ser.ensure(ntrials * ldo * 4 + 256));
+  PSR_TRY(parts.ensure(ntrials * dedisperse_part_count(o, length) * 8 + 8));
+  PSR_TRY(sums.ensure(ntrials * 8));
+  PSR_TRY(err.ensure(8));
+  PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
+  PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), ntrials, length, ser.as<float>(), ldo,
+                               parts.as<double>(), sums.as<double>(), spread,
+                               err.as<unsigned>(), st));
+  PSR_CUDA(cudaMemcpy2DAsync(out, length * 4, ser.p, ldo * 4, length * 4, ntrials,
+                             cudaMemcpyDeviceToHost, st));
+  unsigned e = 0;
+  PSR_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  if (e) {
+    set_error("dedispersion: a bounded wait for a staged tile gave up");
+    return PSR_ETIMEOUT;
+  }
+  return PSR_OK;
+}
+
+int psr_raw_power(const float *series, uint64_t len, float *out) {
+  if (!series || !out || len < 2) {
+    set_error("periodicity: series of at least two samples required");
+    return PSR_EINVAL;
+  }
+  Stream s;
+  FftPlan p;
+  PSR_TRY(p.init(len, s.s));
+  const uint64_t ldo = series_ld_(len);
+  DevBuf ser, sums, work, power, psum;
+  PSR_TRY(ser.ensure(ldo * 4 + 256));
+  PSR_TRY(sums.ensure(8));
+  PSR_TRY(work.ensure(p.M * 8 + 16));
+  PSR_TRY(power.ensure((p.M + 1 + 64) * 4));
+  PSR_TRY(psum.ensure(p.pass2_ctas() * 8 + 8));
+  PSR_CUDA(cudaMemcpyAsync(ser.p, series, len * 4, cudaMemcpyHostToDevice, s.s));
+  // Mean of the series (f64 sequential in the reference; exact for the
+  // integer-valued and bounded-range series the search produces).
+  double sum = -0.0;
+  for (uint64_t i = 0; i < len; ++i) sum += (double)series[i];
+  PSR_CUDA(cudaMemcpyAsync(sums.p, &sum, 8, cudaMemcpyHostToDevice, s.s));
+  PSR_TRY(launch_raw_power_ex(p, ser.as<float>(), ldo, sums.as<double>(), 1, work.as<float2>(),
+                              power.as<float>(), ((p.M + 1 + 63) / 64) * 64, psum.as<double>(),
+                              s.s));
+  PSR_CUDA(cudaMemcpyAsync(out, power.p, (p.M + 1) * 4, cudaMemcpyDeviceToHost, s.s));
+  PSR_CUDA(cudaStreamSynchronize(s.s));
+  return PSR_OK;
+}
+
+int psr_periodicity(const float *series, uint64_t len, double tsamp, double dm,
+                    const psr_search_config *cfg, psr_candidate *out, uint64_t cap,
+                    uint64_t *n) {
+  if (!series || len < 2 || !std::isfinite(tsamp) || tsamp <= 0.0 || !valid_config(cfg) || !n) {
+    set_error("periodicity: series.len() >= 2, finite positive tsamp and a valid config "
+              "are required");
+    return PSR_EINVAL;
+  }
+  // A one-channel f32 filterbank with zero delay reproduces the series.
+  Stream s;
+  DeviceObs o;
+  PSR_TRY(obs_from_f32(series, 1, len, tsamp, o, s.s));
+  SearchEngine e;
+  e.chunk = 1;
+  PSR_TRY(e.prepare(o, &dm, 1, len, to_spec(cfg, tsamp), s.s));
+  // The engine computes delays from the DM; with one channel they are zero.
+  // The mean is the reference's sequential f64 sum (search/src/lib.rs:36).
+  double sum = -0.0;
+  for (uint64_t i = 0; i < len; ++i) sum += (double)series[i];
+  e.host_sums.assign(1, sum);
+  PSR_TRY(e.enqueue(o, s.s));
+  PSR_TRY(e.finish(o, s.s));
+  uint64_t counts = 0;
+  return e.collect(s.s, &counts, out, cap, n);
+}
+
+int psr_search_trials(const psr_fb *fb, const double *trials, uint64_t ntrials,
+                      uint64_t discovery, const psr_search_config *cfg, uint64_t *counts,
+                      psr_candidate *out, uint64_t cap, uint64_t *n_total) {
+  if (!fb || !trials || !valid_config(cfg) || !n_total) {
+    set_error("search: null argument or invalid config");
+    return PSR_EINVAL;
+  }
+  cudaStream_t st = fb->stream.s;
+  SearchEngine e;
+  PSR_TRY(e.prepare(fb->o, trials, ntrials, discovery, to_spec(cfg, fb->o.h.tsamp), st));
+  PSR_TRY(e.enqueue(fb->o, st));
+  PSR_TRY(e.finish(fb->o, st));
+  return e.collect(st, counts, out, cap, n_total);
+}
+
+// search::sift (search/src/lib.rs:147-176).
+int psr_sift(const psr_candidate *in, uint64_t n, double res, uint64_t limit,
+             int reject_dm_zero, psr_candidate *out, uint64_t *n_out) {
+  std::vector<psr_candidate> c(in, in + n);
+  auto key = [](double x) {
+    int64_t i;
+    std::memcpy(&i, &x, 8);
+    return i ^ (int64_t)((uint64_t)(i >> 63) >> 1);
+  };
+  std::stable_sort(c.begin(), c.end(), [&](const psr_candidate &a, const psr_candidate &b) {
+    return key(a.score) > key(b.score);
+  });
+  std::vector<psr_candidate> kept;
+  std::vector<double> rejected;
+  for (const psr_candidate &x : c) {
+    auto related = [&](double f) {
+      for (int h = 1; h <= 16; ++h)
+        if (std::fabs(x.frequency_hz - f * h) <= res || std::fabs(f - x.frequency_hz * h) <= res)
+          return true;
+      return false;
+    };
+    bool skip = std::any_of(kept.begin(), kept.end(),
+                            [&](const psr_candidate &k) { return related(k.frequency_hz); }) ||
+                std::any_of(rejected.begin(), rejected.end(), related);
+    if (skip) continue;
+    if (reject_dm_zero && x.dm <= 0.0) {
+      rejected.push_back(x.frequency_hz);
+      continue;
+    }
+    kept.push_back(x);
+    if (kept.size() >= limit) break;
+  }
+  *n_out = kept.size();
+  if (out) std::copy(kept.begin(), kept.end(), out);
+  return PSR_OK;
+}
+
+int psr_profile_at(const float *series, uint64_t n, double tsamp, double period, uint64_t bins,
+                   uint64_t sample_offset, psr_profile_stats *stats, float *values,
+                   uint64_t *counts) {
+  if (!series || !stats || bins < 4 || !std::isfinite(period) || period <= 0.0 ||
+      !std::isfinite(tsamp) || tsamp <= 0.0 || n == 0) {
+    set_error("profile_at: bins >= 4, finite positive period/tsamp required");
+    return PSR_EINVAL;
+  }
+  Stream s;
+  DevBuf x;
+  PSR_TRY(x.ensure(n * 4));
+  PSR_CUDA(cudaMemcpyAsync(x.p, series, n * 4, cudaMemcpyHostToDevice, s.s));
+  return fold_profiles(x.as<float>(), n, tsamp, &period, 1, bins, sample_offset, stats, values,
+                       counts, s.s);
+}
+
+int psr_refine(const float *series, uint64_t n, double tsamp, double frequency, double span_hz,
+               uint64_t steps, uint64_t bins, psr_profile_stats *stats, float *values,
+               uint64_t *counts) {
+  if (!series || !stats || steps == 0 || !(frequency > span_hz) || !(span_hz >= 0.0) ||
+      bins < 4 || n == 0) {
+    set_error("refine: steps > 0 and frequency > span_hz >= 0 required");
+    return PSR_EINVAL;
+  }
+  std::vector<double> periods(steps + 1);
+  for (uint64_t i = 0; i <= steps; ++i) {
+    const double f = frequency - span_hz + 2.0 * span_hz * (double)i / (double)steps;
+    periods[i] = 1.0 / f;
+  }
+  Stream s;
+  DevBuf x;
+  PSR_TRY(x.ensure(n * 4));
+  PSR_CUDA(cudaMemcpyAsync(x.p, series, n * 4, cudaMemcpyHostToDevice, s.s));
+  std::vector<psr_profile_stats> st(steps + 1);
+  std::vector<float> vals((steps + 1) * bins);
+  std::vector<uint64_t> cnts((steps + 1) * bins);
+  PSR_TRY(fold_profiles(x.as<float>(), n, tsamp, periods.data(), steps + 1, bins, 0, st.data(),
+                        vals.data(), cnts.data(), s.s));
+  // max_by keeps the last maximum (fold/src/lib.rs:93-95).
+  uint64_t best = 0;
+  auto key = [](double v) {
+    int64_t i;
+    std::memcpy(&i, &v, 8);
+    return i ^ (int64_t)((uint64_t)(i >> 63) >> 1);
+  };
+  for (uint64_t i = 1; i <= steps; ++i)
+    if (key(st[i].reduced_chi_square) >= key(st[best].reduced_chi_square)) best = i;
+  *stats = st[best];
+  if (values) std::copy(vals.begin() + best * bins, vals.begin() + (best + 1) * bins, values);
+  if (counts) std::copy(cnts.begin() + best * bins, cnts.begin() + (best + 1) * bins, counts);
+  return PSR_OK;
+}
+
+int psr_measure(const float *x, uint64_t n, uint64_t offset, double tsamp, double period,
+                uint64_t start_bin, uint64_t width_bins, uint64_t bins, psr_measurement *out) {
+  if (!x || !out || bins == 0 || width_bins == 0 || width_bins > bins || start_bin >= bins ||
+      !(period > 0.0) || !(tsamp > 0.0) || n == 0) {
+    set_error("measure: a valid window, positive period/tsamp and samples are required");
+    return PSR_EINVAL;
+  }
+  Stream s;
+  DevBuf d;
+  PSR_TRY(d.ensure(n * 4));
+  PSR_CUDA(cudaMemcpyAsync(d.p, x, n * 4, cudaMemcpyHostToDevice, s.s));
+  return measure_device(d.as<float>(), n, offset, tsamp, period, start_bin, width_bins, bins,
+                        out, s.s);
+}
+
+// ------------------------------------------------------------ session
+int psr_session_create(const psr_header *header, uint64_t nsamples, const double *trials,
+                       uint64_t ntrials, uint64_t discovery, const psr_search_config *cfg,
+                       uint64_t rfi_block_samples, float rfi_threshold, psr_session **out) {
+  if (!header || !trials || !valid_config(cfg) || !out || nsamples < 2 || header->nchans <= 0) {
+    set_error("session: invalid arguments");
+    return PSR_EINVAL;
+  }
+  std::unique_ptr<psr_session> s(new psr_session());
+  DeviceObs &o = s->o;
+  o.h = *header;
+  o.ns = nsamples;
+  o.nch = (uint64_t)header->nchans;
+  o.kind = kind_for_bits(header->nbits);
+  o.payload_bytes = (nsamples * o.nch * (uint64_t)header->nbits + 7) / 8;
+  PSR_TRY(o.payload.ensure(o.payload_bytes + 16));
+  PSR_TRY(o.alloc());
+  s->rfi_block = rfi_block_samples;
+  s->rfi_threshold = rfi_threshold;
+  PSR_TRY(s->eng.prepare(o, trials, ntrials, discovery, to_spec(cfg, header->tsamp),
+                         s->stream.s));
+  PSR_TRY(s->errbuf.ensure(8));
+  PSR_CUDA(cudaStreamSynchronize(s->stream.s));
+  *out = s.release();
+  return PSR_OK;
+}
+
+int psr_session_load(psr_session *s, const uint8_t *payload, uint64_t nbytes) {
+  if (!s || !payload || nbytes < s->o.payload_bytes) {
+    set_error("session_load: payload smaller than the session's observation");
+    return PSR_EINVAL;
+  }
+  PSR_CUDA(cudaMemcpyAsync(s->o.payload.p, payload, s->o.payload_bytes, cudaMemcpyHostToDevice,
+                           s->stream.s));
+  return PSR_OK;
+}
+
+int psr_session_run(psr_session *s) {
+  if (!s) {
+    set_error("session_run: null handle");
+    return PSR_EINVAL;
+  }
+  cudaStream_t st = s->stream.s;
+  PSR_CUDA(cudaMemsetAsync(s->errbuf.p, 0xff, 8, st));
+  PSR_TRY(s->mark(0, 0));
+  PSR_TRY(launch_unpack(s->o, s->errbuf.as<unsigned long long>(), st));
+  PSR_TRY(s->mark(0, 1));
+  if (s->rfi_block) {
+    PSR_TRY(s->mark(1, 0));
+    PSR_TRY(rfi_enqueue(s->o, s->rfi_block, s->rfi_threshold, s->rfi, st));
+    PSR_TRY(s->mark(1, 1));
+  }
+  PSR_TRY(s->eng.enqueue(s->o, st));
+  s->have_run = true;
+  return PSR_OK;
+}
+
+int psr_session_sync(psr_session *s) {
+  if (!s || !s->have_run) {
+    set_error("session_sync: nothing has been run");
+    return PSR_EINVAL;
+  }
+  cudaStream_t st = s->stream.s;
+  unsigned long long e = 0;
+  PSR_CUDA(cudaMemcpyAsync(&e, s->errbuf.p, 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  if (e != ~0ull) {
+    set_error("invalid or unsupported filterbank: nonfinite sample at " +
+              std::to_string(e / s->o.nch) + "/" + std::to_string(e % s->o.nch));
+    return PSR_EFORMAT;
+  }
+  PSR_TRY(s->harvest());
+  return s->eng.finish(s->o, st);
+}
+
+int psr_session_set_profiling(psr_session *s, int enable) {
+  if (!s) {
+    set_error("session_set_profiling: null handle");
+    return PSR_EINVAL;
+  }
+  s->eng.profile = enable != 0;
+  return PSR_OK;
+}
+
+int psr_session_stage_times(psr_session *s, double *ms, uint64_t *launches, int reset) {
+  if (!s) {
+    set_error("session_stage_times: null handle");
+    return PSR_EINVAL;
+  }
+  const double v[5] = {s->pre_ms[0], s->pre_ms[1], s->eng.stage_ms[0], s->eng.stage_ms[1],
+                       s->eng.stage_ms[2]};
+  const uint64_t l[5] = {s->pre_launches[0], s->pre_launches[1], s->eng.stage_launches[0],
+                         s->eng.stage_launches[1], s->eng.stage_launches[2]};
+  for (int i = 0; i < 5; ++i) {
+    if (ms) ms[i] = v[i];
+    if (launches) launches[i] = l[i];
+  }
+  if (reset) {
+    s->pre_ms[0] = s->pre_ms[1] = 0.0;
+    s->pre_launches[0] = s->pre_launches[1] = 0;
+    for (int i = 0; i < 3; ++i) {
+      s->eng.stage_ms[i] = 0.0;
+      s->eng.stage_launches[i] = 0;
+    }
+  }
+  return PSR_OK;
+}
+
+int psr_session_candidates(psr_session *s, uint64_t *counts, psr_candidate *out, uint64_t cap,
+                           uint64_t *n_total) {
+  if (!s || !n_total) {
+    set_error("session_candidates: null argument");
+    return PSR_EINVAL;
+  }
+  return s->eng.collect(s->stream.s, counts, out, cap, n_total);
+}
+
+int psr_session_mask(psr_session *s, uint64_t *channels, uint64_t *nchannels_bad,
+                     uint64_t *blocks, uint64_t blocks_cap, uint64_t *nblocks_bad,
+                     double *masked_fraction) {
+  if (!s || !nchannels_bad || !nblocks_bad || !masked_fraction) {
+    set_error("session_mask: null argument");
+    return PSR_EINVAL;
+  }
+  if (!s->rfi_block) {
+    *nchannels_bad = 0;
+    *nblocks_bad = 0;
+    *masked_fraction = 0.0;
+    return PSR_OK;
+  }
+  RfiResult res;
+  PSR_TRY(rfi_collect(s->o, s->rfi_block, s->rfi, s->stream.s, res));
+  *nchannels_bad = res.channels.size();
+  if (channels) std::copy(res.channels.begin(), res.channels.end(), channels);
+  *nblocks_bad = res.blocks.size();
+  if (blocks)
+    for (uint64_t i = 0; i < res.blocks.size() && i < blocks_cap; ++i) blocks[i] = res.blocks[i];
+  *masked_fraction = res.masked_fraction;
+  return PSR_OK;
+}
+
+void *psr_session_payload_device(psr_session *s) { return s ? s->o.payload.p : nullptr; }
+void *psr_session_stream(psr_session *s) { return s ? (void *)s->stream.s : nullptr; }
+void psr_session_free(psr_session *s) { delete s; }
+
+}  // extern "C"

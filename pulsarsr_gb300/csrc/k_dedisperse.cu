@@ -1,0 +1,381 @@
+// K3 incoherent dedispersion (dedisperse::apply, dedisperse/src/lib.rs:61-90,
+// run for many trials as in the CLI loop cli/src/main.rs:462-469).
+//
+// out[trial][t] = sum_c data[c][t + delay[trial][c]],  t in [0, n).
+//
+// Integer samples (u8): every partial sum is an integer below 2^16, so the
+// reference's channel-ordered f32 sum is exact and any summation order gives
+// the bit-identical value.  The fast kernel stages a tile of every channel
+// row into shared memory with TMA bulk copies (cp.async.bulk + mbarrier,
+// double buffered), and each thread accumulates 16 consecutive samples for a
+// block of trials in packed 2 x u16 lanes.  Consecutive trials whose delay
+// for a channel is unchanged reuse the unpacked lanes (warp-uniform test).
+//
+// Everything else (f32 samples, or integer sums that could exceed 2^16) uses
+// a kernel that adds channels in reference order in f32.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "psr_internal.h"
+
+namespace psr {
+namespace {
+
+constexpr int DD_NT = 256;              // threads per CTA
+constexpr int DD_TPT = 16;              // samples per thread
+constexpr int DD_TT = DD_NT * DD_TPT;   // samples per tile (4096)
+constexpr int DD_DB = 8;                // trials per CTA
+constexpr int DD_MAXCC = 32;            // rows per stage (one issuing lane each)
+constexpr long long DD_SPIN_LIMIT = 1ll << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false (and the error word set) if the phase never completes.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity,
+                                                  unsigned *err) {
+  for (long long i = 0; i < DD_SPIN_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicOr(err, 1u);
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+struct StageInfo {
+  long long base[DD_MAXCC];  // absolute sample index of the staged row start
+};
+
+// Issue the TMA copies of rows [c0, c0+cc) for trials [d0, d0+DB) of tile t0.
+// Run by warp 0: lane i stages row c0+i.
+__device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns,
+                            uint64_t nch, const uint32_t *__restrict__ delays,
+                            uint64_t ntrials, uint64_t d0, uint64_t t0, uint64_t c0, int cc,
+                            uint8_t *buf, int rowcap, StageInfo *info, uint64_t *bar) {
+  const int lane = threadIdx.x & 31;
+  unsigned bytes = 0;
+  if (lane < cc && c0 + lane < nch) {
+    const uint64_t c = c0 + lane;
+    uint32_t dmin = 0xffffffffu, dmax = 0;
+    for (int d = 0; d < DD_DB; ++d) {
+      uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
+      uint32_t v = delays[tr * nch + c];
+      dmin = min(dmin, v);
+      dmax = max(dmax, v);
+    }
+    long long a = (long long)((t0 + dmin) & ~(uint64_t)15);
+    long long rowend = (long long)((ns + 15) & ~(uint64_t)15);
+    long long b = (long long)((t0 + dmax + DD_TT + 15) & ~(uint64_t)15);
+    if (b > rowend) b = rowend;
+    if (b > a + rowcap) b = a + rowcap;
+    info->base[lane] = a;
+    if (b > a) {
+      bytes = (unsigned)(b - a);
+      mbar_expect_tx(bar, bytes);
+    }
+    __syncwarp(__activemask());
+    if (bytes) bulk_g2s(buf + (size_t)lane * rowcap, s + c * ld + a, bytes, bar);
+  }
+  __syncwarp();
+  if (lane == 0) mbar_arrive(bar);
+}
+
+__global__ void __launch_bounds__(DD_NT)
+    k_dedisp_u8(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
+                const uint32_t *__restrict__ delays, uint64_t ntrials, uint64_t n,
+                float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
+                uint64_t ntiles, int cc, int rowcap, unsigned *err) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  uint8_t *bufs[2] = {smem, smem + (size_t)cc * rowcap};
+  __shared__ uint64_t bars[2];
+  __shared__ StageInfo info[2];
+  __shared__ unsigned long long wsum[DD_NT / 32][DD_DB];
+
+  const uint64_t t0 = (uint64_t)blockIdx.x * DD_TT;
+  const uint64_t d0 = (uint64_t)blockIdx.y * DD_DB;
+  const int tl = threadIdx.x;
+  const int nchunks = (int)((nch + cc - 1) / cc);
+
+  if (tl == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tl < 32) {
+    issue_stage(s, ld, ns, nch, delays, ntrials, d0, t0, 0, cc, bufs[0], rowcap, &info[0],
+                &bars[0]);
+    if (nchunks > 1)
+      issue_stage(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)cc, cc, bufs[1], rowcap,
+                  &info[1], &bars[1]);
+  }
+
+  uint32_t acc[DD_DB][8];
+#pragma unroll
+  for (int d = 0; d < DD_DB; ++d)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[d][i] = 0;
+
+  bool alive = true;
+  for (int k = 0; k < nchunks; ++k) {
+    const int b = k & 1;
+    if (!mbar_wait_bounded(&bars[b], (unsigned)((k >> 1) & 1), err)) {
+      alive = false;
+      break;
+    }
+    const uint64_t c0 = (uint64_t)k * cc;
+    const int rows = (int)min((uint64_t)cc, (uint64_t)(nch - c0));
+    const uint8_t *buf = bufs[b];
+    for (int r = 0; r < rows; ++r) {
+      const uint64_t c = c0 + r;
+      const long long base = info[b].base[r];
+      const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
+      long long prev = -1;
+      uint32_t p[8];
+#pragma unroll
+      for (int d = 0; d < DD_DB; ++d) {
+        uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
+        long long off = (long long)t0 + (long long)__ldg(&delays[tr * nch + c]) - base;
+        if (off != prev) {  // uniform across the CTA
+          prev = off;
+          const int q = tl + (int)(off >> 4);
+          const int o = (int)(off & 15);
+          uint4 lo = row16[q], hi = row16[q + 1];
+          uint32_t w0 = lo.x, w1 = lo.y, w2 = lo.z, w3 = lo.w, w4 = hi.x, w5 = hi.y, w6 = hi.z,
+                   w7 = hi.w;
+          if (o & 8) {
+            w0 = w2; w1 = w3; w2 = w4; w3 = w5; w4 = w6; w5 = w7;
+          }
+          if (o & 4) {
+            w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5;
+          }
+          const unsigned sh = (unsigned)(o & 3) * 8u;
+          uint32_t x0 = __funnelshift_r(w0, w1, sh), x1 = __funnelshift_r(w1, w2, sh);
+          uint32_t x2 = __funnelshift_r(w2, w3, sh), x3 = __funnelshift_r(w3, w4, sh);
+          p[0] = __byte_perm(x0, 0, 0x4140);
+          p[1] = __byte_perm(x0, 0, 0x4342);
+          p[2] = __byte_perm(x1, 0, 0x4140);
+          p[3] = __byte_perm(x1, 0, 0x4342);
+          p[4] = __byte_perm(x2, 0, 0x4140);
+          p[5] = __byte_perm(x2, 0, 0x4342);
+          p[6] = __byte_perm(x3, 0, 0x4140);
+          p[7] = __byte_perm(x3, 0, 0x4342);
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[d][i] += p[i];
+      }
+    }
+    __syncthreads();  // every thread is done reading buffer b
+    if (tl < 32 && k + 2 < nchunks) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue_stage(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc, cc,
+                  bufs[b], rowcap, &info[b], &bars[b]);
+    }
+  }
+  if (!alive) {
+    // Drain the other buffer's copy (bounded) before leaving.
+    if (tl == 0) mbar_wait_bounded(&bars[0], 0, err), mbar_wait_bounded(&bars[1], 0, err);
+    return;
+  }
+
+  const uint64_t tb = t0 + (uint64_t)tl * DD_TPT;
+#pragma unroll
+  for (int d = 0; d < DD_DB; ++d) {
+    const uint64_t tr = d0 + d;
+    float v[16];
+    unsigned long long local = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      uint32_t lo = acc[d][i] & 0xffffu, hi = acc[d][i] >> 16;
+      bool in0 = tb + 2 * i < n, in1 = tb + 2 * i + 1 < n;
+      v[2 * i] = (float)lo;
+      v[2 * i + 1] = (float)hi;
+      local += (in0 ? lo : 0u) + (in1 ? hi : 0u);
+    }
+    if (tr < ntrials) {
+      float *dst = out + tr * ldo + tb;
+      if (tb + 16 <= n) {
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          d4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+      } else {
+        for (int i = 0; i < 16; ++i)
+          if (tb + i < n) dst[i] = v[i];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((tl & 31) == 0) wsum[tl >> 5][d] = local;
+  }
+  __syncthreads();
+  if (tl < DD_DB && d0 + tl < ntrials) {
+    unsigned long long t = 0;
+    for (int w = 0; w < DD_NT / 32; ++w) t += wsum[w][tl];
+    part[(d0 + tl) * ntiles + blockIdx.x] = (double)t;
+  }
+}
+
+// Reference-order f32 accumulation (one output per thread per trial).
+constexpr int DG_TPT = 4;
+constexpr int DG_NT = 256;
+constexpr int DG_TT = DG_NT * DG_TPT;
+constexpr int DG_DB = 4;
+
+template <class T>
+__global__ void __launch_bounds__(DG_NT)
+    k_dedisp_generic(const T *__restrict__ s, uint64_t ld, uint64_t nch,
+                     const uint32_t *__restrict__ delays, uint64_t ntrials, uint64_t n,
+                     float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
+                     uint64_t ntiles) {
+  __shared__ double wsum[DG_NT / 32][DG_DB];
+  const uint64_t t0 = (uint64_t)blockIdx.x * DG_TT;
+  const uint64_t d0 = (uint64_t)blockIdx.y * DG_DB;
+  float acc[DG_DB][DG_TPT];
+#pragma unroll
+  for (int d = 0; d < DG_DB; ++d)
+#pragma unroll
+    for (int i = 0; i < DG_TPT; ++i) acc[d][i] = 0.0f;
+  for (uint64_t c = 0; c < nch; ++c) {
+    const T *row = s + c * ld;
+#pragma unroll
+    for (int d = 0; d < DG_DB; ++d) {
+      uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
+      const uint64_t dl = __ldg(&delays[tr * nch + c]);
+#pragma unroll
+      for (int i = 0; i < DG_TPT; ++i) {
+        uint64_t t = t0 + (uint64_t)i * DG_NT + threadIdx.x;
+        float v = t < n ? (float)row[t + dl] : 0.0f;
+        acc[d][i] = __fadd_rn(acc[d][i], v);
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < DG_DB; ++d) {
+    double local = 0.0;
+    const uint64_t tr = d0 + d;
+#pragma unroll
+    for (int i = 0; i < DG_TPT; ++i) {
+      uint64_t t = t0 + (uint64_t)i * DG_NT + threadIdx.x;
+      if (t < n) {
+        if (tr < ntrials) out[tr * ldo + t] = acc[d][i];
+        local += (double)acc[d][i];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5][d] = local;
+  }
+  __syncthreads();
+  if (threadIdx.x < DG_DB && d0 + threadIdx.x < ntrials) {
+    double t = 0.0;
+    for (int w = 0; w < DG_NT / 32; ++w) t += wsum[w][threadIdx.x];
+    part[(d0 + threadIdx.x) * ntiles + blockIdx.x] = t;
+  }
+}
+
+// Ordered reduction of per-tile partial sums into the series sum per trial.
+__global__ void k_reduce_parts(const double *part, uint64_t ntiles, uint64_t ntrials,
+                               double *sums) {
+  uint64_t tr = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tr >= ntrials) return;
+  double s = 0.0;
+  for (uint64_t i = 0; i < ntiles; ++i) s += part[tr * ntiles + i];
+  sums[tr] = s;
+}
+
+}  // namespace
+
+uint64_t series_ld(uint64_t n) { return ((n + 63) / 64) * 64; }
+
+int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
+                         uint64_t n, float *d_out, uint64_t ldo, double *d_part,
+                         double *d_sums, uint64_t max_spread, unsigned *d_err,
+                         cudaStream_t st) {
+  const bool packed = o.kind == SAMPLE_U8 && (double)o.nch * o.max_value() <= 65535.0;
+  if (packed) {
+    const uint64_t ntiles = (n + DD_TT - 1) / DD_TT;
+    int rowcap = (int)(((uint64_t)DD_TT + max_spread + 32 + 15) & ~(uint64_t)15);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int smax = 0;
+    cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t budget = (size_t)smax - 4096;
+    int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, o.nch, budget / (2 * (size_t)rowcap)});
+    if (cc >= 1) {
+      size_t smem = 2 * (size_t)cc * rowcap;
+      PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+      dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
+      k_dedisp_u8<<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns, o.nch,
+                                               d_delays, ntrials, n, d_out, ldo, d_part, ntiles,
+                                               cc, rowcap, d_err);
+      PSR_CUDA(cudaGetLastError());
+      k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles,
+                                                                         ntrials, d_sums);
+      PSR_CUDA(cudaGetLastError());
+      return PSR_OK;
+    }
+  }
+  const uint64_t ntiles = (n + DG_TT - 1) / DG_TT;
+  dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DG_DB - 1) / DG_DB));
+  switch (o.kind) {
+    case SAMPLE_U8:
+      k_dedisp_generic<uint8_t><<<grid, DG_NT, 0, st>>>(o.samples.as<uint8_t>(), o.ld, o.nch,
+                                                        d_delays, ntrials, n, d_out, ldo,
+                                                        d_part, ntiles);
+      break;
+    case SAMPLE_U16:
+      k_dedisp_generic<uint16_t><<<grid, DG_NT, 0, st>>>(o.samples.as<uint16_t>(), o.ld,
+                                                         o.nch, d_delays, ntrials, n, d_out,
+                                                         ldo, d_part, ntiles);
+      break;
+    default:
+      k_dedisp_generic<float><<<grid, DG_NT, 0, st>>>(o.samples.as<float>(), o.ld, o.nch,
+                                                      d_delays, ntrials, n, d_out, ldo, d_part,
+                                                      ntiles);
+  }
+  PSR_CUDA(cudaGetLastError());
+  k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles, ntrials,
+                                                                     d_sums);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n) {
+  const bool packed = o.kind == SAMPLE_U8 && (double)o.nch * o.max_value() <= 65535.0;
+  return packed ? (n + DD_TT - 1) / DD_TT : (n + DG_TT - 1) / DG_TT;
+}
+
+}  // namespace psr

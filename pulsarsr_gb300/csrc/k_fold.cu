@@ -1,0 +1,282 @@
+// K8 folding (fold::profile_at, fold/src/lib.rs:16-80) and K9 grid refinement
+// (fold::refine, fold/src/lib.rs:81-97) for many trial periods in one launch.
+//
+// bin(t) = min(floor(fract(((t + offset) * tsamp) / period) * bins), bins-1)
+// in f64 exactly as the reference.  Bin sums are f64; the per-CTA partial
+// sums are combined in a fixed order.  For integer-valued series (sums of
+// integer samples) every partial sum is an exact integer, so the result is
+// independent of the order and equals the reference's sequential sum.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "psr_internal.h"
+
+namespace psr {
+namespace {
+
+constexpr int FOLD_NT = 256;
+constexpr int FOLD_MAXBINS = 1024;
+
+__global__ void __launch_bounds__(FOLD_NT)
+    k_fold(const float *__restrict__ x, uint64_t n, double tsamp,
+           const double *__restrict__ periods, uint64_t bins, uint64_t offset,
+           uint64_t per_cta, double *__restrict__ psums, unsigned long long *__restrict__ pcounts) {
+  extern __shared__ unsigned char sm_raw[];
+  double *s = reinterpret_cast<double *>(sm_raw);
+  unsigned *c = reinterpret_cast<unsigned *>(s + bins);
+  const uint64_t per = blockIdx.y;
+  const double period = periods[per];
+  for (uint64_t b = threadIdx.x; b < bins; b += blockDim.x) {
+    s[b] = 0.0;
+    c[b] = 0;
+  }
+  __syncthreads();
+  const uint64_t t0 = (uint64_t)blockIdx.x * per_cta;
+  const uint64_t t1 = min(t0 + per_cta, n);
+  const double dbins = (double)bins;
+  for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    const double q = __ddiv_rn(__dmul_rn((double)(t + offset), tsamp), period);
+    const double ph = __dsub_rn(q, trunc(q));
+    uint64_t b = (uint64_t)__dmul_rn(ph, dbins);
+    if (b > bins - 1) b = bins - 1;
+    atomicAdd(&s[b], (double)x[t]);
+    atomicAdd(&c[b], 1u);
+  }
+  __syncthreads();
+  const uint64_t slot = (per * gridDim.x + blockIdx.x) * bins;
+  for (uint64_t b = threadIdx.x; b < bins; b += blockDim.x) {
+    psums[slot + b] = s[b];
+    pcounts[slot + b] = c[b];
+  }
+}
+
+__global__ void k_fold_reduce(const double *__restrict__ psums,
+                              const unsigned long long *__restrict__ pcounts, uint64_t nparts,
+                              uint64_t bins, uint64_t nper, double *__restrict__ sums,
+                              unsigned long long *__restrict__ counts) {
+  const uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nper * bins) return;
+  const uint64_t per = id / bins, b = id % bins;
+  double s = 0.0;
+  unsigned long long cnt = 0;
+  for (uint64_t p = 0; p < nparts; ++p) {
+    s += psums[(per * nparts + p) * bins + b];
+    cnt += pcounts[(per * nparts + p) * bins + b];
+  }
+  sums[id] = s;
+  counts[id] = cnt;
+}
+
+// Series mean and variance in f64 (fold/src/lib.rs:63-68).
+__global__ void k_series_moments(const float *__restrict__ x, uint64_t n, double *out) {
+  __shared__ double red[32];
+  __shared__ double mean_s;
+  double a = 0.0;
+  for (uint64_t t = threadIdx.x; t < n; t += blockDim.x) a += (double)x[t];
+  for (int o = 16; o; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+    mean_s = s / (double)n;
+    out[0] = s;
+  }
+  __syncthreads();
+  const double m = mean_s;
+  double v = 0.0;
+  for (uint64_t t = threadIdx.x; t < n; t += blockDim.x) {
+    const double d = __dsub_rn((double)x[t], m);
+    v = __dadd_rn(v, __dmul_rn(d, d));
+  }
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+    out[1] = s;
+  }
+}
+
+// confirmation::measure (search/src/confirmation.rs:107-141): on/off sums.
+__global__ void k_measure(const float *__restrict__ x, uint64_t n, uint64_t offset, double tsamp,
+                          double period, uint64_t start_bin, uint64_t width_bins, uint64_t bins,
+                          double *__restrict__ part) {
+  __shared__ double red[6][32];
+  double acc[6] = {0, 0, 0, 0, 0, 0};  // n0, s0, q0, n1, s1, q1
+  const double dbins = (double)bins;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const double q = __ddiv_rn(__dmul_rn((double)(i + offset), tsamp), period);
+    uint64_t b = (uint64_t)__dmul_rn(__dsub_rn(q, trunc(q)), dbins);
+    if (b > bins - 1) b = bins - 1;
+    const int k = ((b + bins - start_bin) % bins) < width_bins ? 1 : 0;
+    const double v = (double)x[i];
+    acc[3 * k] += 1.0;
+    acc[3 * k + 1] = __dadd_rn(acc[3 * k + 1], v);
+    acc[3 * k + 2] = __dadd_rn(acc[3 * k + 2], __dmul_rn(v, v));
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double a = acc[j];
+    for (int o = 16; o; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) red[j][threadIdx.x >> 5] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double a = 0.0;
+    for (int w = 0; w < (int)(blockDim.x / 32); ++w) a += red[threadIdx.x][w];
+    part[blockIdx.x * 6 + threadIdx.x] = a;
+  }
+}
+
+int32_t key32(float x) {
+  int32_t i;
+  std::memcpy(&i, &x, 4);
+  return i ^ (int32_t)((uint32_t)(i >> 31) >> 1);
+}
+bool tless(float a, float b) { return key32(a) < key32(b); }
+
+float upper_median(std::vector<float> v) {
+  if (v.empty()) return 0.0f;
+  size_t i = v.size() / 2;
+  std::nth_element(v.begin(), v.begin() + i, v.end(), tless);
+  return v[i];
+}
+
+}  // namespace
+
+// Profile statistics from bin sums/counts (fold/src/lib.rs:39-79), host.
+void profile_stats(const double *sums, const unsigned long long *cnts, uint64_t bins,
+                   double smean, double svar, double period, psr_profile_stats *st,
+                   float *values, uint64_t *counts) {
+  std::vector<float> vals(bins);
+  for (uint64_t b = 0; b < bins; ++b)
+    vals[b] = cnts[b] > 0 ? (float)(sums[b] / (double)cnts[b]) : 0.0f;
+  const float center = upper_median(vals);
+  std::vector<float> off;
+  for (uint64_t b = 0; b < bins; ++b)
+    if (cnts[b] > 0) off.push_back(vals[b]);
+  std::sort(off.begin(), off.end(), tless);
+  off.resize(std::max<size_t>(off.size() * 3 / 4, 1));
+  double mean = -0.0;
+  for (float v : off) mean += (double)v;
+  mean /= (double)off.size();
+  double var = -0.0;
+  for (float v : off) {
+    const double d = (double)v - mean;
+    var += d * d;
+  }
+  const double sigma = std::sqrt(var / (double)off.size());
+  float peak = -INFINITY;
+  for (float v : vals) peak = std::fmax(peak, v);
+  st->period_s = period;
+  st->snr = sigma > 1e-12 ? ((double)peak - (double)center) / sigma : 0.0;
+  uint64_t populated = 0;
+  for (uint64_t b = 0; b < bins; ++b) populated += cnts[b] > 0;
+  if (svar > 1e-12 && populated > 1) {
+    double s = -0.0;
+    for (uint64_t b = 0; b < bins; ++b) {
+      const double d = (double)vals[b] - smean;
+      s += (double)cnts[b] * (d * d) / svar;
+    }
+    st->reduced_chi_square = s / (double)(populated - 1);
+  } else {
+    st->reduced_chi_square = 0.0;
+  }
+  if (values) std::copy(vals.begin(), vals.end(), values);
+  if (counts)
+    for (uint64_t b = 0; b < bins; ++b) counts[b] = cnts[b];
+}
+
+// Fold one device series at nper periods; stats/values/counts are arrays of
+// nper entries (values/counts nper*bins).
+int fold_profiles(const float *d_x, uint64_t n, double tsamp, const double *periods,
+                  uint64_t nper, uint64_t bins, uint64_t offset, psr_profile_stats *stats,
+                  float *values, uint64_t *counts, cudaStream_t st) {
+  if (bins < 4 || bins > FOLD_MAXBINS || n == 0) {
+    set_error("profile_at: 4 <= bins <= 1024 and a non-empty series are required");
+    return PSR_EINVAL;
+  }
+  const uint64_t per_cta = 8192;
+  const uint64_t nparts = (n + per_cta - 1) / per_cta;
+  DevBuf dper, psums, pcounts, sums, cnts, mom;
+  PSR_TRY(dper.ensure(nper * 8));
+  PSR_TRY(psums.ensure(nper * nparts * bins * 8));
+  PSR_TRY(pcounts.ensure(nper * nparts * bins * 8));
+  PSR_TRY(sums.ensure(nper * bins * 8));
+  PSR_TRY(cnts.ensure(nper * bins * 8));
+  PSR_TRY(mom.ensure(16));
+  PSR_CUDA(cudaMemcpyAsync(dper.p, periods, nper * 8, cudaMemcpyHostToDevice, st));
+  const size_t smem = bins * (8 + 4);
+  dim3 grid((unsigned)nparts, (unsigned)nper);
+  k_fold<<<grid, FOLD_NT, smem, st>>>(d_x, n, tsamp, dper.as<double>(), bins, offset, per_cta,
+                                      psums.as<double>(), pcounts.as<unsigned long long>());
+  PSR_CUDA(cudaGetLastError());
+  k_fold_reduce<<<(unsigned)((nper * bins + 255) / 256), 256, 0, st>>>(
+      psums.as<double>(), pcounts.as<unsigned long long>(), nparts, bins, nper,
+      sums.as<double>(), cnts.as<unsigned long long>());
+  k_series_moments<<<1, 1024, 0, st>>>(d_x, n, mom.as<double>());
+  PSR_CUDA(cudaGetLastError());
+  std::vector<double> hs(nper * bins), hm(2);
+  std::vector<unsigned long long> hc(nper * bins);
+  PSR_CUDA(cudaMemcpyAsync(hs.data(), sums.p, nper * bins * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hc.data(), cnts.p, nper * bins * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hm.data(), mom.p, 16, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  const double smean = hm[0] / (double)n;
+  const double svar = hm[1] / (double)n;
+  for (uint64_t p = 0; p < nper; ++p)
+    profile_stats(hs.data() + p * bins, hc.data() + p * bins, bins, smean, svar, periods[p],
+                  &stats[p], values ? values + p * bins : nullptr,
+                  counts ? counts + p * bins : nullptr);
+  return PSR_OK;
+}
+
+}  // namespace psr
+
+namespace psr {
+
+int measure_device(const float *d_x, uint64_t n, uint64_t offset, double tsamp, double period,
+                   uint64_t start_bin, uint64_t width_bins, uint64_t bins, psr_measurement *out,
+                   cudaStream_t st) {
+  const unsigned nb = (unsigned)std::min<uint64_t>((n + 1023) / 1024, 1024);
+  DevBuf part;
+  PSR_TRY(part.ensure((size_t)nb * 6 * 8));
+  k_measure<<<nb, 256, 0, st>>>(d_x, n, offset, tsamp, period, start_bin, width_bins, bins,
+                                part.as<double>());
+  PSR_CUDA(cudaGetLastError());
+  std::vector<double> h((size_t)nb * 6);
+  PSR_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  for (unsigned b = 0; b < nb; ++b)
+    for (int j = 0; j < 6; ++j) a[j] += h[(size_t)b * 6 + j];
+  const uint64_t cnt[2] = {(uint64_t)a[0], (uint64_t)a[3]};
+  const double sum[2] = {a[1], a[4]}, sum2[2] = {a[2], a[5]};
+  out->on_samples = cnt[1];
+  out->off_samples = cnt[0];
+  if (cnt[0] < 2 || cnt[1] < 2) {
+    out->snr = 0.0;
+    out->mean_difference = 0.0;
+    out->standard_error = 0.0;
+    return PSR_OK;
+  }
+  const double diff = sum[1] / (double)cnt[1] - sum[0] / (double)cnt[0];
+  auto var = [&](int k) {
+    return std::fmax((sum2[k] - sum[k] * sum[k] / (double)cnt[k]) / (double)(cnt[k] - 1), 0.0);
+  };
+  const double err = std::sqrt(var(1) / (double)cnt[1] + var(0) / (double)cnt[0]);
+  out->snr = err > 1e-10 ? diff / err : 0.0;
+  out->mean_difference = diff;
+  out->standard_error = err;
+  return PSR_OK;
+}
+
+}  // namespace psr

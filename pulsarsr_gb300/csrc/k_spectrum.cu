@@ -1,0 +1,533 @@
+// K5 power normalisation + birdies, K6 harmonic sums + peaks, K7 per-trial
+// sort/dedupe (search/src/lib.rs:45-144).
+//
+// Normalisation: every 64-bin block b is divided by
+//   scale_b = max(max(median(raw[lo..hi]) / ln2, floor), 1e-20),
+//   lo = max(64b-128, 1), hi = min(64b+192, len), floor = 1e-6 * mean(raw).
+// The median is exact: each 64-bin chunk is sorted once per CTA (warp bitonic
+// network), and the window's rank-(cnt/2) element is found by bisection over
+// the 32-bit patterns (non-negative floats order like their bits) counting
+// with binary searches in the <= 5 sorted chunks.  Normalised power is never
+// stored: pw(i) = raw[i] / scale[i>>6], zero for i == 0 and birdie bins.
+//
+// Harmonic sums follow the reference's f64 arithmetic exactly.  The f64 work
+// is only done where it can matter: h = 1 scores are pw(k) or pw(k+1) minus 1,
+// so a bin whose larger neighbour cannot reach the threshold is skipped
+// before the parabolic offset is computed; h >= 2 scores exist only where
+// pw(k) >= 4 (search/src/lib.rs:85-87).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "psr_internal.h"
+
+namespace psr {
+namespace {
+
+constexpr int SC_G = 128;                // blocks per CTA (one per thread)
+constexpr int SC_CH = SC_G + 4;          // chunks staged per CTA
+constexpr float LN2F = 0.693147180559945309f;
+
+__device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
+
+// Number of elements <= key in a sorted chunk of n keys (n <= 64).
+__device__ __forceinline__ int count_le(const uint32_t *a, int n, uint32_t key) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] <= key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Sort 64 keys held two per lane (index lane and lane+32) ascending.
+__device__ __forceinline__ void warp_sort64(uint32_t &x0, uint32_t &x1) {
+  const int lane = threadIdx.x & 31;
+  // Element index e = lane + 32*r; bitonic network over e in [0, 64).
+  for (int k = 2; k <= 64; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j == 32) {
+        // partners are x0 <-> x1 of the same lane (e and e+32)
+        const bool up = ((lane & k) == 0);  // e & k with k == 64: always 0 -> ascending
+        uint32_t a = x0, b = x1;
+        bool sw = up ? (a > b) : (a < b);
+        if (sw) {
+          x0 = b;
+          x1 = a;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          uint32_t v = r ? x1 : x0;
+          const int e = lane + 32 * r;
+          uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+          const bool up = ((e & k) == 0);
+          const bool lower = ((e & j) == 0);
+          uint32_t nv = (lower == up) ? min(v, o) : max(v, o);
+          if (r) x1 = nv;
+          else x0 = nv;
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(SC_G)
+    k_scales(const float *__restrict__ power, uint64_t ldp, uint64_t plen,
+             const double *__restrict__ psum, uint32_t npsum, float *__restrict__ scale,
+             uint64_t lds, uint64_t nblocks) {
+  __shared__ uint32_t ch[SC_CH][64];
+  __shared__ int cnt[SC_CH];
+  __shared__ float floor_s;
+  const uint64_t trial = blockIdx.y;
+  const float *raw = power + trial * ldp;
+  const long long b0 = (long long)blockIdx.x * SC_G;
+  const long long c_first = b0 - 2;  // chunk index of ch[0]
+  const long long last_chunk = (long long)((plen - 1) / 64);
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (uint32_t i = 0; i < npsum; ++i) s += psum[trial * npsum + i];
+    floor_s = (float)(s / (double)plen * 1e-6);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int ci = warp; ci < SC_CH; ci += SC_G / 32) {
+    const long long c = c_first + ci;
+    uint32_t x0 = 0xffffffffu, x1 = 0xffffffffu;
+    int n = 0;
+    if (c >= 0 && c <= last_chunk) {
+      const long long base = c * 64;
+      const long long e0 = base + lane, e1 = base + lane + 32;
+      if (e0 < (long long)plen && e0 >= 1) x0 = fbits(raw[e0]);
+      if (e1 < (long long)plen) x1 = fbits(raw[e1]);
+      n = (int)min(64ll, (long long)plen - base) - (c == 0 ? 1 : 0);
+    }
+    warp_sort64(x0, x1);
+    ch[ci][lane] = x0;
+    ch[ci][lane + 32] = x1;
+    if (lane == 0) cnt[ci] = n;
+  }
+  __syncthreads();
+  const long long b = b0 + threadIdx.x;
+  if (b >= (long long)nblocks) return;
+  const long long center = b * 64;
+  const long long lo = max(center - 128, 1ll);
+  const long long hi = min(center + 192, (long long)plen);
+  const int total = (int)(hi - lo);
+  const int r = total / 2;
+  // chunks of the window: b-2 .. b+2 (clipped), local indices threadIdx.x .. +4
+  int cl = threadIdx.x, chi = threadIdx.x + 4;
+  while (c_first + cl < 0) ++cl;
+  while (c_first + chi > last_chunk) --chi;
+  uint32_t kmin = 0xffffffffu, kmax = 0;
+  for (int c = cl; c <= chi; ++c)
+    if (cnt[c] > 0) {
+      kmin = min(kmin, ch[c][0]);
+      kmax = max(kmax, ch[c][cnt[c] - 1]);
+    }
+  // smallest key K with count(<= K) > r
+  uint32_t lo_k = kmin, hi_k = kmax;
+  while (lo_k < hi_k) {
+    const uint32_t mid = lo_k + ((hi_k - lo_k) >> 1);
+    int c_le = 0;
+    for (int c = cl; c <= chi; ++c) c_le += count_le(ch[c], cnt[c], mid);
+    if (c_le > r) hi_k = mid;
+    else lo_k = mid + 1;
+  }
+  const float med = __uint_as_float(lo_k);
+  const float sc = fmaxf(fmaxf(__fdiv_rn(med, LN2F), floor_s), 1e-20f);
+  scale[trial * lds + b] = sc;
+}
+
+struct RawCand {
+  double score;
+  double freq;
+  uint32_t k;
+  uint32_t h;
+};
+
+struct HarmArgs {
+  const float *power;
+  uint64_t ldp;
+  uint64_t plen;
+  const float *scale;
+  uint64_t lds;
+  const double *birdies;
+  int nbirdies;
+  double bin_hz;
+  double threshold;
+  uint64_t first;
+  uint64_t end[5];  // end_h for h = 1,2,4,8,16 (0 when the h loop is skipped)
+  RawCand *raw;
+  unsigned *raw_count;
+  uint64_t raw_cap;
+  unsigned *overflow;
+};
+
+__device__ __forceinline__ float pw(const HarmArgs &a, const float *raw, const float *sc,
+                                    uint64_t i) {
+  if (i == 0) return 0.0f;
+  float v = __fdiv_rn(raw[i], sc[i >> 6]);
+  if (a.nbirdies) {
+    const double f = (double)i * a.bin_hz;
+    for (int q = 0; q < a.nbirdies; ++q)
+      if (fabs(__dsub_rn(f, a.birdies[2 * q])) <= a.birdies[2 * q + 1]) return 0.0f;
+  }
+  return v;
+}
+
+// Parabolic offset (search/src/lib.rs:91-96).
+__device__ __forceinline__ double offset_at(const float *raw, uint64_t k) {
+  const double a = (double)raw[k - 1], b = (double)raw[k], c = (double)raw[k + 1];
+  const double curv = __dadd_rn(__dsub_rn(a, __dmul_rn(2.0, b)), c);
+  if (curv < 0.0) {
+    const double o = __ddiv_rn(__dmul_rn(0.5, __dsub_rn(a, c)), curv);
+    return fmin(fmax(o, -0.5), 0.5);
+  }
+  return 0.0;
+}
+
+__device__ __forceinline__ double inv_sqrt_div(double x, int hi) {
+  // (sum - h) / sqrt(h): sqrt(h) correctly rounded as in Rust's f64::sqrt.
+  switch (hi) {
+    case 0: return x;
+    case 1: return __ddiv_rn(x, 1.4142135623730951);
+    case 2: return __dmul_rn(x, 0.5);
+    case 3: return __ddiv_rn(x, 2.8284271247461903);
+    default: return __dmul_rn(x, 0.25);
+  }
+}
+
+// Full score of harmonic level hi (h = 1 << hi) at bin k (k in [first, end]).
+__device__ double score_at(const HarmArgs &a, const float *raw, const float *sc, uint64_t k,
+                           int hi) {
+  const int h = 1 << hi;
+  if (h > 1 && pw(a, raw, sc, k) < 4.0f) return -INFINITY;
+  const double off = offset_at(raw, k);
+  const double kf = __dadd_rn((double)k, off);
+  double sum = -0.0;
+  for (int j = 1; j <= h; ++j) {
+    const double pos = __dmul_rn(kf, (double)j);
+    uint64_t idx = (uint64_t)round(pos);
+    if (idx > a.plen - 1) idx = a.plen - 1;
+    sum = __dadd_rn(sum, (double)pw(a, raw, sc, idx));
+  }
+  return inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
+}
+
+__device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64_t k, int hi,
+                     double score) {
+  const unsigned slot = atomicAdd(&a.raw_count[trial], 1u);
+  if (slot >= a.raw_cap) {
+    atomicOr(a.overflow, 1u);
+    return;
+  }
+  const double off = offset_at(raw, k);
+  RawCand c;
+  c.score = score;
+  c.freq = __dmul_rn(__dadd_rn((double)k, off), a.bin_hz);
+  c.k = (uint32_t)k;
+  c.h = (uint32_t)hi;
+  a.raw[trial * a.raw_cap + slot] = c;
+}
+
+__global__ void k_harmonic(HarmArgs a) {
+  const uint64_t trial = blockIdx.y;
+  const float *raw = a.power + trial * a.ldp;
+  const float *sc = a.scale + trial * a.lds;
+  const uint64_t k = a.first + 1 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.end[0] == 0 || k + 1 > a.end[0]) return;  // k in [first+1, end_1 - 1]
+  // h = 1: score(k) is pw(k) - 1 or pw(k+1) - 1.
+  const float p0 = pw(a, raw, sc, k), p1 = pw(a, raw, sc, k + 1);
+  if ((double)fmaxf(p0, p1) - 1.0 >= a.threshold) {
+    const double s = score_at(a, raw, sc, k, 0);
+    if (s >= a.threshold) {
+      const double sm = score_at(a, raw, sc, k - 1, 0);
+      const double sp = score_at(a, raw, sc, k + 1, 0);
+      if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
+    }
+  }
+  if (p0 < 4.0f) return;
+  for (int hi = 1; hi < 5; ++hi) {
+    const uint64_t e = a.end[hi];
+    if (e == 0 || k + 1 > e) continue;  // k must lie in [first+1, end_h - 1]
+    const double s = score_at(a, raw, sc, k, hi);
+    if (s >= a.threshold) {
+      const double sm = score_at(a, raw, sc, k - 1, hi);
+      const double sp = score_at(a, raw, sc, k + 1, hi);
+      if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
+    }
+  }
+}
+
+// Orderable key: score descending, then (h, k) ascending = the reference's
+// insertion order under its stable sort (search/src/lib.rs:130).
+__device__ __forceinline__ unsigned long long score_key_desc(double s) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(s);
+  unsigned long long asc = (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+  return ~asc;
+}
+
+constexpr int SEL_CAP = 2048;
+constexpr int SEL_NT = 1024;
+
+struct SelArgs {
+  const RawCand *raw;
+  const unsigned *raw_count;
+  uint64_t raw_cap;
+  const double *trial_dm;
+  double tol;  // 1 / (len * tsamp)
+  uint64_t max_candidates;
+  psr_candidate *kept;
+  unsigned *kept_count;
+};
+
+__device__ __forceinline__ bool key_less(unsigned long long ka, uint32_t sa,
+                                         unsigned long long kb, uint32_t sb) {
+  return ka < kb || (ka == kb && sa < sb);
+}
+
+__global__ void __launch_bounds__(SEL_NT) k_select(SelArgs a) {
+  __shared__ unsigned long long key[SEL_CAP];
+  __shared__ uint32_t seq[SEL_CAP];
+  __shared__ uint32_t idx[SEL_CAP];
+  __shared__ double kept_f[64];
+  __shared__ int nk;
+  const uint64_t trial = blockIdx.x;
+  const RawCand *rc = a.raw + trial * a.raw_cap;
+  const unsigned n = min(a.raw_count[trial], (unsigned)a.raw_cap);
+  psr_candidate *out = a.kept + trial * a.max_candidates;
+  const double dm = a.trial_dm[trial];
+  if (threadIdx.x == 0) nk = 0;
+  if (n <= SEL_CAP) {
+    unsigned P = 1;
+    while (P < n) P <<= 1;
+    for (unsigned i = threadIdx.x; i < P; i += blockDim.x) {
+      if (i < n) {
+        key[i] = score_key_desc(rc[i].score);
+        seq[i] = (rc[i].h << 24) | rc[i].k;
+        idx[i] = i;
+      } else {
+        key[i] = ~0ull;
+        seq[i] = 0xffffffffu;
+        idx[i] = 0xffffffffu;
+      }
+    }
+    __syncthreads();
+    for (unsigned k = 2; k <= P; k <<= 1)
+      for (unsigned j = k >> 1; j > 0; j >>= 1) {
+        for (unsigned i = threadIdx.x; i < P; i += blockDim.x) {
+          const unsigned l = i ^ j;
+          if (l > i) {
+            const bool up = (i & k) == 0;
+            const bool gt = key_less(key[l], seq[l], key[i], seq[i]);
+            if (gt == up) {
+              unsigned long long tk = key[i];
+              key[i] = key[l];
+              key[l] = tk;
+              uint32_t ts = seq[i];
+              seq[i] = seq[l];
+              seq[l] = ts;
+              uint32_t ti = idx[i];
+              idx[i] = idx[l];
+              idx[l] = ti;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    // Sequential dedupe by warp 0 (search/src/lib.rs:131-143).
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      int kc = 0;
+      for (unsigned i = 0; i < n && (uint64_t)kc < a.max_candidates; ++i) {
+        const RawCand c = rc[idx[i]];
+        bool dup = false;
+        for (int q = lane; q < kc; q += 32) dup |= fabs(__dsub_rn(kept_f[q], c.freq)) < a.tol;
+        dup = __any_sync(0xffffffffu, dup);
+        if (!dup) {
+          if (lane == 0) {
+            kept_f[kc] = c.freq;
+            psr_candidate o;
+            o.frequency_hz = c.freq;
+            o.period_s = __ddiv_rn(1.0, c.freq);
+            o.dm = dm;
+            o.harmonics = 1ull << c.h;
+            o.score = c.score;
+            out[kc] = o;
+          }
+          ++kc;
+          __syncwarp();
+        }
+      }
+      if (lane == 0) a.kept_count[trial] = (unsigned)kc;
+    }
+    return;
+  }
+  // More raw candidates than fit in shared memory: repeated arg-max over the
+  // unsorted list (exact order; only reached by pathological spectra).
+  __shared__ unsigned long long best_k[SEL_NT / 32];
+  __shared__ uint32_t best_s[SEL_NT / 32], best_i[SEL_NT / 32];
+  __shared__ unsigned long long last_k;
+  __shared__ uint32_t last_s;
+  if (threadIdx.x == 0) {
+    last_k = 0;
+    last_s = 0;
+  }
+  __syncthreads();
+  bool started = false;
+  for (;;) {
+    unsigned long long bk = ~0ull;
+    uint32_t bs = 0xffffffffu, bi = 0xffffffffu;
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+      const unsigned long long kk = score_key_desc(rc[i].score);
+      const uint32_t ss = (rc[i].h << 24) | rc[i].k;
+      if (started && !key_less(last_k, last_s, kk, ss)) continue;  // already consumed
+      if (key_less(kk, ss, bk, bs)) {
+        bk = kk;
+        bs = ss;
+        bi = i;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, o);
+      uint32_t os = __shfl_xor_sync(0xffffffffu, bs, o);
+      uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (key_less(ok, os, bk, bs)) {
+        bk = ok;
+        bs = os;
+        bi = oi;
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+      best_k[threadIdx.x >> 5] = bk;
+      best_s[threadIdx.x >> 5] = bs;
+      best_i[threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long k0 = ~0ull;
+      uint32_t s0 = 0xffffffffu, i0 = 0xffffffffu;
+      for (int w = 0; w < SEL_NT / 32; ++w)
+        if (key_less(best_k[w], best_s[w], k0, s0)) {
+          k0 = best_k[w];
+          s0 = best_s[w];
+          i0 = best_i[w];
+        }
+      best_i[0] = i0;
+      if (i0 != 0xffffffffu) {
+        last_k = k0;
+        last_s = s0;
+        const RawCand c = rc[i0];
+        bool dup = false;
+        for (int q = 0; q < nk; ++q) dup |= fabs(__dsub_rn(kept_f[q], c.freq)) < a.tol;
+        if (!dup) {
+          kept_f[nk] = c.freq;
+          psr_candidate o;
+          o.frequency_hz = c.freq;
+          o.period_s = __ddiv_rn(1.0, c.freq);
+          o.dm = dm;
+          o.harmonics = 1ull << c.h;
+          o.score = c.score;
+          out[nk] = o;
+          ++nk;
+        }
+      }
+    }
+    __syncthreads();
+    started = true;
+    if (best_i[0] == 0xffffffffu || (uint64_t)nk >= a.max_candidates) break;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.kept_count[trial] = (unsigned)nk;
+}
+
+}  // namespace
+
+int spectrum_enqueue_ex(const FftPlan &p, const SpecConfig &c, const float *d_power,
+                        uint64_t ldp, const double *d_psum, uint32_t npsum,
+                        const double *d_trial_dm, uint64_t ntrials, SpecWork &w,
+                        cudaStream_t st) {
+  const uint64_t plen = p.M + 1;
+  const uint64_t nblocks = (plen + 63) / 64;
+  const uint64_t lds = ((nblocks + 63) / 64) * 64;
+  if (c.max_candidates > 64) {
+    set_error("search: at most 64 candidates per trial are supported");
+    return PSR_EINVAL;
+  }
+  PSR_TRY(w.scale.ensure(ntrials * lds * 4));
+  if (w.raw_cap == 0) w.raw_cap = 2048;
+  PSR_TRY(w.raw.ensure(ntrials * w.raw_cap * sizeof(RawCand)));
+  PSR_TRY(w.raw_count.ensure(ntrials * 4));
+  PSR_TRY(w.kept.ensure(ntrials * std::max<uint64_t>(c.max_candidates, 1) * sizeof(psr_candidate)));
+  PSR_TRY(w.kept_count.ensure(ntrials * 4));
+  PSR_TRY(w.overflow.ensure(16));
+  PSR_TRY(w.birdies.ensure(std::max<size_t>(c.birdies.size(), 2) * 8));
+  if (!c.birdies.empty())
+    PSR_CUDA(cudaMemcpyAsync(w.birdies.p, c.birdies.data(), c.birdies.size() * 8,
+                             cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaMemsetAsync(w.raw_count.p, 0, ntrials * 4, st));
+  PSR_CUDA(cudaMemsetAsync(w.overflow.p, 0, 16, st));
+  {
+    dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
+    k_scales<<<grid, SC_G, 0, st>>>(d_power, ldp, plen, d_psum, npsum, w.scale.as<float>(), lds,
+                                    nblocks);
+    PSR_CUDA(cudaGetLastError());
+  }
+  // search/src/lib.rs:62, 73-78
+  const double size = (double)p.N;
+  const double bin_hz = 1.0 / (size * c.tsamp);
+  HarmArgs a{};
+  a.power = d_power;
+  a.ldp = ldp;
+  a.plen = plen;
+  a.scale = w.scale.as<float>();
+  a.lds = lds;
+  a.birdies = w.birdies.as<double>();
+  a.nbirdies = (int)(c.birdies.size() / 2);
+  a.bin_hz = bin_hz;
+  a.threshold = c.threshold;
+  const double firstf = std::fmax(std::ceil(c.min_hz / bin_hz), 1.0);
+  const uint64_t first = (uint64_t)firstf;
+  const double lastf = std::floor(std::fmin(c.max_hz, 0.5 / c.tsamp) / bin_hz);
+  const uint64_t last = std::min<uint64_t>(lastf <= 0.0 ? 0 : (uint64_t)lastf, plen - 2);
+  a.first = first;
+  for (int hi = 0; hi < 5; ++hi) {
+    const uint64_t h = 1ull << hi;
+    const uint64_t e = std::min(last, (plen - 2) / h);
+    a.end[hi] = (e <= first + 1) ? 0 : e;
+  }
+  a.raw = w.raw.as<RawCand>();
+  a.raw_count = w.raw_count.as<unsigned>();
+  a.raw_cap = w.raw_cap;
+  a.overflow = w.overflow.as<unsigned>();
+  if (a.end[0] > first + 1) {
+    const uint64_t nk = a.end[0] - first - 1;
+    dim3 grid((unsigned)((nk + 255) / 256), (unsigned)ntrials);
+    k_harmonic<<<grid, 256, 0, st>>>(a);
+    PSR_CUDA(cudaGetLastError());
+  }
+  SelArgs s{};
+  s.raw = a.raw;
+  s.raw_count = a.raw_count;
+  s.raw_cap = w.raw_cap;
+  s.trial_dm = d_trial_dm;
+  s.tol = 1.0 / ((double)p.len * c.tsamp);
+  s.max_candidates = c.max_candidates;
+  s.kept = w.kept.as<psr_candidate>();
+  s.kept_count = w.kept_count.as<unsigned>();
+  k_select<<<(unsigned)ntrials, SEL_NT, 0, st>>>(s);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+int spectrum_check_overflow(SpecWork &w, uint64_t, cudaStream_t st, bool &overflow) {
+  unsigned v = 0;
+  PSR_CUDA(cudaMemcpyAsync(&v, w.overflow.p, 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  overflow = v != 0;
+  return PSR_OK;
+}
+
+}  // namespace psr

@@ -1,0 +1,422 @@
+// K1 unpack (fbank::decode) and K2 RFI masking (rfi::mask) on the device.
+//
+// Layout: samples are channel-major, row c at c*ld, stored in their integer
+// width (u8 for nbits <= 8, u16, f32).  Decisions of rfi::mask depend on the
+// reference's sequential f32 sums (rfi/src/lib.rs:35-43, 59-67); every sum
+// whose order matters is computed by one thread in reference order, and sums
+// that are provably exact (integer samples, total <= 2^24) are computed in
+// parallel, which gives the identical f32 value.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "psr_internal.h"
+
+namespace psr {
+
+namespace {
+
+constexpr int UNPACK_TT = 256;  // times per tile
+constexpr int UNPACK_TC = 32;   // channels per tile
+
+template <class T>
+__global__ void k_unpack(const uint8_t *__restrict__ payload, T *__restrict__ out,
+                         uint64_t ns, uint64_t nch, uint64_t ld, int nbits,
+                         unsigned long long *err_index) {
+  __shared__ T tile[UNPACK_TC][UNPACK_TT + 4];
+  const uint64_t t0 = (uint64_t)blockIdx.x * UNPACK_TT;
+  const uint64_t c0 = (uint64_t)blockIdx.y * UNPACK_TC;
+  for (int idx = threadIdx.x; idx < UNPACK_TT * UNPACK_TC; idx += blockDim.x) {
+    int tl = idx / UNPACK_TC, cl = idx % UNPACK_TC;
+    uint64_t t = t0 + tl, c = c0 + cl;
+    T v = T(0);
+    if (t < ns && c < nch) {
+      uint64_t i = t * nch + c;
+      if constexpr (sizeof(T) == 1) {
+        if (nbits == 8) {
+          v = payload[i];
+        } else {
+          // SIGPROC packs low-bit samples LSB first (fbank/src/lib.rs:175-179).
+          uint64_t bit = i * (uint64_t)nbits;
+          v = (T)((payload[bit >> 3] >> (bit & 7)) & ((1u << nbits) - 1u));
+        }
+      } else if constexpr (sizeof(T) == 2) {
+        v = (T)(payload[2 * i] | ((unsigned)payload[2 * i + 1] << 8));
+      } else {
+        uint32_t b = (uint32_t)payload[4 * i] | ((uint32_t)payload[4 * i + 1] << 8) |
+                     ((uint32_t)payload[4 * i + 2] << 16) | ((uint32_t)payload[4 * i + 3] << 24);
+        float f = __uint_as_float(b);
+        if (!isfinite(f)) atomicMin(err_index, (unsigned long long)i);
+        v = f;
+      }
+    }
+    tile[cl][tl] = v;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < UNPACK_TT * UNPACK_TC; idx += blockDim.x) {
+    int cl = idx / UNPACK_TT, tl = idx % UNPACK_TT;
+    uint64_t t = t0 + tl, c = c0 + cl;
+    if (t < ns && c < nch) out[c * ld + t] = tile[cl][tl];
+  }
+}
+
+// ------------------------------------------------------------ radix select
+// Total-order key of an f32 (Rust f32::total_cmp) as an unsigned integer.
+__device__ __forceinline__ uint32_t fkey(float f) {
+  uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Block-wide exact selection of the element of rank r (ascending) among n
+// keys key(i); top_shift is the shift of the highest non-constant digit.
+template <class KeyFn>
+__device__ uint32_t block_select(KeyFn key, uint64_t n, uint64_t r, int top_shift,
+                                 unsigned *hist, uint32_t *bcast) {
+  uint32_t prefix = 0, mask = 0;
+  for (int shift = top_shift; shift >= 0; shift -= 8) {
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d] = 0;
+    __syncthreads();
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      uint32_t k = key(i);
+      if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint64_t cum = 0;
+      uint32_t digit = 255;
+      for (int d = 0; d < 256; ++d) {
+        if (cum + hist[d] > r) {
+          digit = (uint32_t)d;
+          break;
+        }
+        cum += hist[d];
+      }
+      r -= cum;
+      bcast[0] = digit;
+      bcast[1] = (uint32_t)(r & 0xffffffffu);
+      bcast[2] = (uint32_t)(r >> 32);
+    }
+    __syncthreads();
+    uint32_t digit = bcast[0];
+    r = (uint64_t)bcast[1] | ((uint64_t)bcast[2] << 32);
+    prefix |= digit << shift;
+    mask |= 255u << shift;
+    __syncthreads();
+  }
+  return prefix;
+}
+
+__global__ void k_median_f32(const float *__restrict__ v, uint64_t n, float *out) {
+  __shared__ unsigned hist[256];
+  __shared__ uint32_t bc[3];
+  if (n == 0) {
+    if (threadIdx.x == 0) *out = 0.0f;
+    return;
+  }
+  uint32_t k = block_select([&](uint64_t i) { return fkey(v[i]); }, n, n / 2, 24, hist, bc);
+  if (threadIdx.x == 0) *out = fkey_inv(k);
+}
+
+// Per-channel exact median of the original row (rfi/src/lib.rs:78).
+template <class T>
+__global__ void k_chan_median(const T *__restrict__ s, uint64_t ns, uint64_t ld,
+                              float *__restrict__ med) {
+  __shared__ unsigned hist[256];
+  __shared__ uint32_t bc[3];
+  const T *row = s + (uint64_t)blockIdx.x * ld;
+  uint32_t k;
+  if constexpr (sizeof(T) == 1) {
+    k = block_select([&](uint64_t i) { return (uint32_t)row[i]; }, ns, ns / 2, 0, hist, bc);
+    if (threadIdx.x == 0) med[blockIdx.x] = (float)k;
+  } else if constexpr (sizeof(T) == 2) {
+    k = block_select([&](uint64_t i) { return (uint32_t)row[i]; }, ns, ns / 2, 8, hist, bc);
+    if (threadIdx.x == 0) med[blockIdx.x] = (float)k;
+  } else {
+    k = block_select([&](uint64_t i) { return fkey(row[i]); }, ns, ns / 2, 24, hist, bc);
+    if (threadIdx.x == 0) med[blockIdx.x] = fkey_inv(k);
+  }
+}
+
+// Exact integer channel totals (for the provably-exact f32 fast path).
+template <class T>
+__global__ void k_chan_total(const T *__restrict__ s, uint64_t ns, uint64_t ld,
+                             unsigned long long *__restrict__ tot) {
+  const T *row = s + (uint64_t)blockIdx.y * ld;
+  unsigned long long acc = 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ns;
+       t += (uint64_t)gridDim.x * blockDim.x)
+    acc += (unsigned long long)row[t];
+  for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&tot[blockIdx.y], acc);
+}
+
+template <class T>
+__device__ __forceinline__ float as_f32(T v) {
+  return (float)v;
+}
+
+// Channel means and variances (rfi/src/lib.rs:35-43): one thread per channel
+// in reference order.  The mean's sum is taken from the exact integer total
+// when every partial sum is an integer <= 2^24 (identical f32 result).
+template <class T>
+__global__ void k_chan_mean_var(const T *__restrict__ s, uint64_t ns, uint64_t ld,
+                                uint64_t nch, const unsigned long long *__restrict__ tot,
+                                float *__restrict__ means, float *__restrict__ vars) {
+  uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nch) return;
+  const T *row = s + c * ld;
+  float sum;
+  if (sizeof(T) < 4 && tot[c] <= (1ull << 24)) {
+    sum = (float)tot[c];
+  } else {
+    sum = -0.0f;
+    for (uint64_t t = 0; t < ns; ++t) sum = __fadd_rn(sum, as_f32(row[t]));
+  }
+  const float m = __fdiv_rn(sum, (float)ns);
+  float acc = -0.0f;
+  if constexpr (sizeof(T) == 1) {
+    // 16 samples per aligned vector load; rows start 64-byte aligned.
+    const uint4 *v = reinterpret_cast<const uint4 *>(row);
+    uint64_t nv = ns / 16, t = 0;
+    for (uint64_t q = 0; q < nv; ++q) {
+      uint4 w = v[q];
+      uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          float d = __fsub_rn((float)((words[a] >> (8 * b)) & 255u), m);
+          acc = __fadd_rn(acc, __fmul_rn(d, d));
+        }
+      t += 16;
+    }
+    for (; t < ns; ++t) {
+      float d = __fsub_rn((float)row[t], m);
+      acc = __fadd_rn(acc, __fmul_rn(d, d));
+    }
+  } else {
+    for (uint64_t t = 0; t < ns; ++t) {
+      float d = __fsub_rn(as_f32(row[t]), m);
+      acc = __fadd_rn(acc, __fmul_rn(d, d));
+    }
+  }
+  means[c] = m;
+  vars[c] = __fdiv_rn(acc, (float)ns);
+}
+
+// Per-(channel, block) sequential f32 sums (rfi/src/lib.rs:62-64).
+template <class T>
+__global__ void k_block_sums(const T *__restrict__ s, uint64_t ns, uint64_t ld,
+                             uint64_t nch, uint64_t bs, uint64_t blocks_n,
+                             float *__restrict__ bsum) {
+  uint64_t id = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= nch * blocks_n) return;
+  uint64_t c = id / blocks_n, b = id % blocks_n;
+  uint64_t start = b * bs, end = min(start + bs, ns);
+  const T *row = s + c * ld;
+  float acc = -0.0f;
+  for (uint64_t t = start; t < end; ++t) acc = __fadd_rn(acc, as_f32(row[t]));
+  bsum[c * blocks_n + b] = acc;
+}
+
+// rfi::outliers (rfi/src/lib.rs:13-22) for one vector, inside one block.
+__device__ void block_outliers(const float *v, uint64_t n, float threshold,
+                               float *dev_scratch, unsigned char *flags,
+                               unsigned *hist, uint32_t *bc) {
+  float center = 0.0f;
+  if (n > 0) {
+    uint32_t k = block_select([&](uint64_t i) { return fkey(v[i]); }, n, n / 2, 24, hist, bc);
+    center = fkey_inv(k);
+  }
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x)
+    dev_scratch[i] = fabsf(__fsub_rn(v[i], center));
+  __syncthreads();
+  float mad = 0.0f;
+  if (n > 0) {
+    uint32_t k = block_select([&](uint64_t i) { return fkey(dev_scratch[i]); }, n, n / 2, 24,
+                              hist, bc);
+    mad = fkey_inv(k);
+  }
+  float scale = fmaxf(fmaxf(__fmul_rn(1.4826f, mad), __fmul_rn(fabsf(center), 1e-4f)), 1e-6f);
+  float lim = __fmul_rn(threshold, scale);
+  for (uint64_t i = threadIdx.x; i < n; i += blockDim.x)
+    flags[i] = fabsf(__fsub_rn(v[i], center)) > lim ? 1 : 0;
+  __syncthreads();
+}
+
+// Channel decision (rfi/src/lib.rs:44-48); writes chbad[] and active count.
+__global__ void k_channel_decide(const float *means, const float *vars, uint64_t nch,
+                                 float threshold, float *scratch, unsigned char *f1,
+                                 unsigned char *f2, unsigned char *chbad,
+                                 unsigned long long *active) {
+  __shared__ unsigned hist[256];
+  __shared__ uint32_t bc[3];
+  block_outliers(means, nch, threshold, scratch, f1, hist, bc);
+  block_outliers(vars, nch, threshold, scratch, f2, hist, bc);
+  for (uint64_t c = threadIdx.x; c < nch; c += blockDim.x)
+    chbad[c] = (f1[c] || f2[c] || vars[c] < 1e-12f) ? 1 : 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long a = 0;
+    for (uint64_t c = 0; c < nch; ++c) a += chbad[c] ? 0 : 1;
+    *active = a;
+  }
+}
+
+// Block means over good channels in channel order (rfi/src/lib.rs:55-69).
+__global__ void k_block_means(const float *bsum, const unsigned char *chbad, uint64_t nch,
+                              uint64_t ns, uint64_t bs, uint64_t blocks_n,
+                              const unsigned long long *active, float *bmeans) {
+  uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= blocks_n) return;
+  float sum = 0.0f;
+  for (uint64_t c = 0; c < nch; ++c)
+    if (!chbad[c]) sum = __fadd_rn(sum, bsum[c * blocks_n + b]);
+  uint64_t start = b * bs, end = min(start + bs, ns);
+  unsigned long long a = *active;
+  if (a < 1) a = 1;
+  bmeans[b] = __fdiv_rn(sum, (float)((end - start) * a));
+}
+
+__global__ void k_block_decide(const float *bmeans, uint64_t blocks_n, float threshold,
+                               float *scratch, unsigned char *blkbad) {
+  __shared__ unsigned hist[256];
+  __shared__ uint32_t bc[3];
+  block_outliers(bmeans, blocks_n, threshold, scratch, blkbad, hist, bc);
+}
+
+// Replace masked samples with the channel median (rfi/src/lib.rs:76-89).
+template <class T>
+__global__ void k_fill(T *__restrict__ s, uint64_t ns, uint64_t ld, uint64_t bs,
+                       const unsigned char *__restrict__ chbad,
+                       const unsigned char *__restrict__ blkbad,
+                       const float *__restrict__ med) {
+  uint64_t c = blockIdx.y;
+  T typical = (T)med[c];
+  bool whole = chbad[c] != 0;
+  T *row = s + c * ld;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ns;
+       t += (uint64_t)gridDim.x * blockDim.x)
+    if (whole || blkbad[t / bs]) row[t] = typical;
+}
+
+}  // namespace
+
+int DeviceObs::alloc() {
+  ld = ((ns + 64 + 63) / 64) * 64;
+  size_t bytes = (size_t)ld * nch * sample_bytes(kind) + 256;
+  PSR_TRY(samples.ensure(bytes));
+  PSR_CUDA(cudaMemset(samples.p, 0, bytes));
+  return PSR_OK;
+}
+
+int launch_unpack(const DeviceObs &o, unsigned long long *d_err, cudaStream_t st) {
+  dim3 grid((unsigned)((o.ns + UNPACK_TT - 1) / UNPACK_TT),
+            (unsigned)((o.nch + UNPACK_TC - 1) / UNPACK_TC));
+  const uint8_t *p = o.payload.as<uint8_t>();
+  switch (o.kind) {
+    case SAMPLE_U8:
+      k_unpack<uint8_t><<<grid, 256, 0, st>>>(p, o.samples.as<uint8_t>(), o.ns, o.nch, o.ld,
+                                              (int)o.h.nbits, d_err);
+      break;
+    case SAMPLE_U16:
+      k_unpack<uint16_t><<<grid, 256, 0, st>>>(p, o.samples.as<uint16_t>(), o.ns, o.nch, o.ld,
+                                               (int)o.h.nbits, d_err);
+      break;
+    default:
+      k_unpack<float><<<grid, 256, 0, st>>>(p, o.samples.as<float>(), o.ns, o.nch, o.ld,
+                                            (int)o.h.nbits, d_err);
+  }
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+int launch_median_f32(const float *d_vals, uint64_t n, float *d_out, unsigned int *,
+                      cudaStream_t st) {
+  k_median_f32<<<1, 1024, 0, st>>>(d_vals, n, d_out);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+template <class T>
+static int rfi_enqueue_t(DeviceObs &o, uint64_t bs, float thr, RfiWork &w, cudaStream_t st) {
+  const uint64_t nch = o.nch, ns = o.ns;
+  const uint64_t blocks_n = (ns + bs - 1) / bs;
+  w.blocks_n = blocks_n;
+  PSR_TRY(w.means.ensure(nch * 4));
+  PSR_TRY(w.vars.ensure(nch * 4));
+  PSR_TRY(w.med.ensure(nch * 4));
+  PSR_TRY(w.bsum.ensure(nch * blocks_n * 4));
+  PSR_TRY(w.bmeans.ensure(blocks_n * 4));
+  PSR_TRY(w.chbad.ensure(nch));
+  PSR_TRY(w.blkbad.ensure(blocks_n));
+  PSR_TRY(w.scratch.ensure(std::max(nch, blocks_n) * 4));
+  PSR_TRY(w.flags.ensure(2 * nch));
+  PSR_TRY(w.hist.ensure(nch * 8 + 8));
+  T *s = o.samples.as<T>();
+  unsigned long long *tot = w.hist.as<unsigned long long>();
+  PSR_CUDA(cudaMemsetAsync(tot, 0, nch * 8 + 8, st));
+  if (sizeof(T) < 4) {
+    dim3 g((unsigned)std::min<uint64_t>((ns + 255) / 256, 64), (unsigned)nch);
+    k_chan_total<T><<<g, 256, 0, st>>>(s, ns, o.ld, tot);
+  }
+  k_chan_mean_var<T><<<(unsigned)((nch + 31) / 32), 32, 0, st>>>(
+      s, ns, o.ld, nch, tot, w.means.as<float>(), w.vars.as<float>());
+  k_block_sums<T><<<(unsigned)((nch * blocks_n + 127) / 128), 128, 0, st>>>(
+      s, ns, o.ld, nch, bs, blocks_n, w.bsum.as<float>());
+  k_chan_median<T><<<(unsigned)nch, 512, 0, st>>>(s, ns, o.ld, w.med.as<float>());
+  unsigned char *fl = w.flags.as<unsigned char>();
+  k_channel_decide<<<1, 1024, 0, st>>>(w.means.as<float>(), w.vars.as<float>(), nch, thr,
+                                       w.scratch.as<float>(), fl, fl + nch,
+                                       w.chbad.as<unsigned char>(), tot + nch);
+  k_block_means<<<(unsigned)((blocks_n + 127) / 128), 128, 0, st>>>(
+      w.bsum.as<float>(), w.chbad.as<unsigned char>(), nch, ns, bs, blocks_n, tot + nch,
+      w.bmeans.as<float>());
+  k_block_decide<<<1, 1024, 0, st>>>(w.bmeans.as<float>(), blocks_n, thr,
+                                     w.scratch.as<float>(), w.blkbad.as<unsigned char>());
+  dim3 gf((unsigned)std::min<uint64_t>((ns + 255) / 256, 256), (unsigned)nch);
+  k_fill<T><<<gf, 256, 0, st>>>(s, ns, o.ld, bs, w.chbad.as<unsigned char>(),
+                                w.blkbad.as<unsigned char>(), w.med.as<float>());
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+int rfi_enqueue(DeviceObs &o, uint64_t bs, float thr, RfiWork &w, cudaStream_t st) {
+  if (bs == 0 || !(thr > 0.0f) || !std::isfinite(thr)) {
+    set_error("rfi::mask: block_samples > 0 and a finite positive threshold are required");
+    return PSR_EINVAL;
+  }
+  switch (o.kind) {
+    case SAMPLE_U8: return rfi_enqueue_t<uint8_t>(o, bs, thr, w, st);
+    case SAMPLE_U16: return rfi_enqueue_t<uint16_t>(o, bs, thr, w, st);
+    default: return rfi_enqueue_t<float>(o, bs, thr, w, st);
+  }
+}
+
+int rfi_collect(const DeviceObs &o, uint64_t bs, RfiWork &w, cudaStream_t st, RfiResult &res) {
+  std::vector<unsigned char> ch(o.nch), bl(w.blocks_n);
+  PSR_CUDA(cudaMemcpyAsync(ch.data(), w.chbad.p, o.nch, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(bl.data(), w.blkbad.p, w.blocks_n, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  res.channels.clear();
+  res.blocks.clear();
+  for (uint64_t c = 0; c < o.nch; ++c)
+    if (ch[c]) res.channels.push_back(c);
+  for (uint64_t b = 0; b < w.blocks_n; ++b)
+    if (bl[b]) res.blocks.push_back(b);
+  // rfi/src/lib.rs:75-94
+  uint64_t count = res.channels.size() * o.ns;
+  uint64_t good = o.nch - res.channels.size();
+  for (uint64_t b : res.blocks) {
+    uint64_t start = b * bs, end = std::min(start + bs, o.ns);
+    count += (end - start) * good;
+  }
+  res.masked_fraction = (double)count / (double)(o.nch * o.ns);
+  return PSR_OK;
+}
+
+}  // namespace psr

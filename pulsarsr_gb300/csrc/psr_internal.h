@@ -1,0 +1,188 @@
+// Internal declarations shared by the libpsr translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/psr.h"
+
+namespace psr {
+
+// ------------------------------------------------------------ errors
+void set_error(const std::string &msg);
+const std::string &last_error();
+
+struct Status {
+  int code = PSR_OK;
+  bool ok() const { return code == PSR_OK; }
+};
+
+#define PSR_CUDA(call)                                                     \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) {                                               \
+      ::psr::set_error(std::string("CUDA error in ") + #call + ": " +      \
+                       cudaGetErrorString(e_));                            \
+      return PSR_ECUDA;                                                    \
+    }                                                                      \
+  } while (0)
+
+#define PSR_TRY(expr)                 \
+  do {                                \
+    int rc_ = (expr);                 \
+    if (rc_ != PSR_OK) return rc_;    \
+  } while (0)
+
+// Owning device allocation (sized once, reused).
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int ensure(size_t n) {
+    if (n <= bytes && p) return PSR_OK;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      set_error(std::string("CUDA error in cudaMalloc(") + std::to_string(n) +
+                " bytes): " + cudaGetErrorString(e));
+      return PSR_ECUDA;
+    }
+    bytes = n;
+    return PSR_OK;
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
+// Sample storage type of the device filterbank.
+enum SampleKind { SAMPLE_U8 = 0, SAMPLE_U16 = 1, SAMPLE_F32 = 2 };
+
+inline int sample_bytes(SampleKind k) { return k == SAMPLE_U8 ? 1 : (k == SAMPLE_U16 ? 2 : 4); }
+inline SampleKind kind_for_bits(int64_t nbits) {
+  return nbits <= 8 ? SAMPLE_U8 : (nbits == 16 ? SAMPLE_U16 : SAMPLE_F32);
+}
+
+// Channel-major samples on the device: row c starts at c*ld elements.  ld is
+// a multiple of 64 elements and rows carry >= 64 elements of zero padding so
+// that 16-byte aligned tile copies never leave the allocation.
+struct DeviceObs {
+  psr_header h{};
+  uint64_t ns = 0;
+  uint64_t nch = 0;
+  SampleKind kind = SAMPLE_U8;
+  uint64_t ld = 0;
+  DevBuf samples;
+  DevBuf payload;   // packed bytes as read (time-major)
+  uint64_t payload_bytes = 0;
+  int alloc();      // samples for (nch, ns, kind)
+  // Maximum sample value (integer kinds) used for exactness decisions.
+  double max_value() const {
+    if (kind == SAMPLE_U8) return (double)((1u << (h.nbits < 8 ? h.nbits : 8)) - 1);
+    if (kind == SAMPLE_U16) return 65535.0;
+    return 0.0;
+  }
+};
+
+// Host-side restatements that stay on the host (FP64 tables, small sorts).
+bool host_delays(const double *f, size_t n, double tsamp, double dm,
+                 std::vector<uint64_t> &out);
+int parse_header(const uint8_t *b, uint64_t len, psr_header &h);
+
+// ---------------------------------------------------------- kernels
+// Unpack the packed time-major payload into channel-major samples.
+// err_index receives min(t*nch+ch) of a non-finite f32 sample (or ~0).
+int launch_unpack(const DeviceObs &o, unsigned long long *d_err_index,
+                  cudaStream_t st);
+
+// RFI mask (rfi::mask) on the device samples.  Scratch is owned by RfiWork.
+struct RfiWork {
+  DevBuf means, vars, med, bsum, bmeans, chbad, blkbad, scratch, flags, hist;
+  uint64_t blocks_n = 0;
+};
+struct RfiResult {
+  std::vector<uint64_t> channels, blocks;
+  double masked_fraction = 0.0;
+};
+int rfi_enqueue(DeviceObs &o, uint64_t block_samples, float threshold,
+                RfiWork &w, cudaStream_t st);
+int rfi_collect(const DeviceObs &o, uint64_t block_samples, RfiWork &w,
+                cudaStream_t st, RfiResult &res);
+
+// Exact upper median of n device floats (radix select), result to d_out.
+int launch_median_f32(const float *d_vals, uint64_t n, float *d_out,
+                      unsigned int *d_hist_scratch, cudaStream_t st);
+
+
+// ---------------------------------------------------------- spectra
+struct FftPlan {
+  uint64_t len = 0;   // series length
+  uint64_t N = 0;     // real FFT size
+  uint64_t M = 0;     // complex size N/2
+  int m = 0;          // log2 M
+  uint64_t M1 = 0, M2 = 0;
+  DevBuf Q;           // quarter twiddle table, N/4 + 1 float2
+  int init(uint64_t series_len, cudaStream_t st);
+  uint64_t bins() const { return M + 1; }
+  uint64_t pass2_ctas() const;
+};
+
+struct SpecConfig {
+  double tsamp = 0;
+  double min_hz = 1, max_hz = 0, threshold = 6;
+  uint64_t max_candidates = 32;
+  std::vector<double> birdies;  // pairs
+};
+struct SpecWork {
+  DevBuf scale, raw, raw_count, kept, kept_count, birdies, overflow, trial_dm;
+  uint64_t raw_cap = 0;
+};
+int spectrum_check_overflow(SpecWork &w, uint64_t ntrials, cudaStream_t st,
+                            bool &overflow);
+
+// Row stride (floats) of a dedispersed series buffer of length n.
+uint64_t series_ld(uint64_t n);
+// Delay table [ntrials][nch] (u32) for the trial DMs, the widest delay spread
+// of a channel within 8 consecutive trials, and the largest delay.
+int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
+                     std::vector<uint32_t> &tab, uint64_t &max_spread, uint64_t &max_delay);
+int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
+                         uint64_t n, float *d_out, uint64_t ldo, double *d_part, double *d_sums,
+                         uint64_t max_spread, unsigned *d_err, cudaStream_t st);
+uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
+int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
+                        const double *d_sums, uint64_t ntrials, float2 *d_work, float *d_power,
+                        uint64_t ldp, double *d_psum, cudaStream_t st);
+int spectrum_enqueue_ex(const FftPlan &p, const SpecConfig &c, const float *d_power,
+                        uint64_t ldp, const double *d_psum, uint32_t npsum,
+                        const double *d_trial_dm, uint64_t ntrials, SpecWork &w,
+                        cudaStream_t st);
+
+// ------------------------------------------------------------- fold
+// Host statistics of a folded profile (fold/src/lib.rs:39-79).
+void profile_stats(const double *sums, const unsigned long long *cnts, uint64_t bins,
+                   double smean, double svar, double period, psr_profile_stats *st,
+                   float *values, uint64_t *counts);
+// confirmation::measure on a device series.
+int measure_device(const float *d_x, uint64_t n, uint64_t offset, double tsamp, double period,
+                   uint64_t start_bin, uint64_t width_bins, uint64_t bins, psr_measurement *out,
+                   cudaStream_t st);
+int fold_profiles(const float *d_series, uint64_t n, double tsamp,
+                  const double *periods, uint64_t nper, uint64_t bins,
+                  uint64_t sample_offset, psr_profile_stats *stats,
+                  float *values, uint64_t *counts, cudaStream_t st);
+
+}  // namespace psr

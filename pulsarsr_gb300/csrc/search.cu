@@ -1,0 +1,218 @@
+// The trial loop of `psr search` (cli/src/main.rs:462-473) on the device:
+// for a chunk of trial DMs, dedisperse -> FFT power -> normalise -> harmonic
+// sums -> per-trial candidate lists, with every buffer allocated once.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "search.h"
+
+namespace psr {
+
+int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntrials_,
+                          uint64_t n_, const SpecConfig &cfg, cudaStream_t st) {
+  if (ntrials_ == 0) {
+    set_error("search: empty DM plan");
+    return PSR_EINVAL;
+  }
+  ntrials = ntrials_;
+  n = n_;
+  spec = cfg;
+  nch = o.nch;
+  std::vector<uint32_t> tab;
+  uint64_t maxd = 0;
+  PSR_TRY(make_delay_table(o, trials, ntrials, tab, max_spread, maxd));
+  if (n < 2 || n > o.ns - maxd) {
+    set_error("invalid dedispersion input: invalid output length");
+    return PSR_EDEDISPERSE;
+  }
+  PSR_TRY(delays.ensure(tab.size() * 4));
+  PSR_CUDA(cudaMemcpyAsync(delays.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st));
+  PSR_TRY(trial_dm.ensure(ntrials * 8));
+  PSR_CUDA(cudaMemcpyAsync(trial_dm.p, trials, ntrials * 8, cudaMemcpyHostToDevice, st));
+  PSR_TRY(fft.init(n, st));
+  ldo = series_ld(n);
+  ldp = ((fft.M + 1 + 63) / 64) * 64;
+  if (chunk == 0) chunk = 64;
+  chunk = std::min(chunk, ntrials);
+  nparts = dedisperse_part_count(o, n);
+  npsum = (uint32_t)fft.pass2_ctas();
+  PSR_TRY(series.ensure(chunk * ldo * 4 + 256));
+  PSR_TRY(parts.ensure(chunk * nparts * 8));
+  PSR_TRY(sums.ensure(chunk * 8));
+  PSR_TRY(work.ensure(fft.m > 12 ? chunk * fft.M * 8 : 16));
+  PSR_TRY(power.ensure(chunk * ldp * 4));
+  PSR_TRY(psum.ensure(chunk * npsum * 8));
+  const uint64_t maxc = std::max<uint64_t>(cfg.max_candidates, 1);
+  PSR_TRY(kept.ensure(ntrials * maxc * sizeof(psr_candidate)));
+  PSR_TRY(kept_count.ensure(ntrials * 4));
+  PSR_TRY(err.ensure(16));
+  PSR_CUDA(cudaMemsetAsync(err.p, 0, 16, st));
+  nchunks = (ntrials + chunk - 1) / chunk;
+  PSR_TRY(chunk_overflow.ensure(nchunks * 4 + 16));
+  return PSR_OK;
+}
+
+int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st) {
+  const uint64_t t0 = ci * chunk;
+  const uint64_t nt = std::min(chunk, ntrials - t0);
+  PSR_TRY(record(ST_DEDISP, true, st));
+  PSR_TRY(launch_dedisperse_ex(o, delays.as<uint32_t>() + t0 * o.nch, nt, n, series.as<float>(),
+                               ldo, parts.as<double>(), sums.as<double>(), max_spread,
+                               err.as<unsigned>(), st));
+  PSR_TRY(record(ST_DEDISP, false, st));
+  if (!host_sums.empty())
+    PSR_CUDA(cudaMemcpyAsync(sums.p, host_sums.data() + t0, nt * 8, cudaMemcpyHostToDevice, st));
+  PSR_TRY(record(ST_FFT, true, st));
+  PSR_TRY(launch_raw_power_ex(fft, series.as<float>(), ldo, sums.as<double>(), nt,
+                              work.as<float2>(), power.as<float>(), ldp, psum.as<double>(), st));
+  PSR_TRY(record(ST_FFT, false, st));
+  // The spectrum stage writes straight into this chunk's slice of kept[].
+  const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
+  SpecWork &w = sw;
+  PSR_TRY(record(ST_SPEC, true, st));
+  PSR_TRY(spectrum_enqueue_ex(fft, spec, power.as<float>(), ldp, psum.as<double>(), npsum,
+                              trial_dm.as<double>() + t0, nt, w, st));
+  PSR_TRY(record(ST_SPEC, false, st));
+  PSR_CUDA(cudaMemcpyAsync(kept.as<psr_candidate>() + t0 * maxc, w.kept.p,
+                           nt * maxc * sizeof(psr_candidate), cudaMemcpyDeviceToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(kept_count.as<unsigned>() + t0, w.kept_count.p, nt * 4,
+                           cudaMemcpyDeviceToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(chunk_overflow.as<unsigned>() + ci, w.overflow.p, 4,
+                           cudaMemcpyDeviceToDevice, st));
+  return PSR_OK;
+}
+
+int SearchEngine::record(int stage, bool begin, cudaStream_t st) {
+  if (!profile) return PSR_OK;
+  cudaEvent_t e;
+  PSR_CUDA(cudaEventCreate(&e));
+  PSR_CUDA(cudaEventRecord(e, st));
+  (begin ? ev_begin : ev_end)[stage].push_back(e);
+  if (!begin) stage_launches[stage] += 1;
+  return PSR_OK;
+}
+
+int SearchEngine::harvest() {
+  for (int s = 0; s < ST_COUNT; ++s) {
+    for (size_t i = 0; i < ev_begin[s].size() && i < ev_end[s].size(); ++i) {
+      float ms = 0.0f;
+      PSR_CUDA(cudaEventElapsedTime(&ms, ev_begin[s][i], ev_end[s][i]));
+      stage_ms[s] += ms;
+    }
+    for (cudaEvent_t e : ev_begin[s]) cudaEventDestroy(e);
+    for (cudaEvent_t e : ev_end[s]) cudaEventDestroy(e);
+    ev_begin[s].clear();
+    ev_end[s].clear();
+  }
+  return PSR_OK;
+}
+
+SearchEngine::~SearchEngine() {
+  for (int s = 0; s < ST_COUNT; ++s) {
+    for (cudaEvent_t e : ev_begin[s]) cudaEventDestroy(e);
+    for (cudaEvent_t e : ev_end[s]) cudaEventDestroy(e);
+  }
+}
+
+int SearchEngine::enqueue(const DeviceObs &o, cudaStream_t st) {
+  for (uint64_t ci = 0; ci < nchunks; ++ci) PSR_TRY(enqueue_chunk(o, ci, st));
+  return PSR_OK;
+}
+
+int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
+  std::vector<unsigned> ov(nchunks);
+  unsigned e = 0;
+  PSR_CUDA(cudaMemcpyAsync(ov.data(), chunk_overflow.p, nchunks * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  if (e) {
+    set_error("dedispersion: a bounded wait for a staged tile gave up");
+    return PSR_ETIMEOUT;
+  }
+  PSR_TRY(harvest());
+  for (uint64_t ci = 0; ci < nchunks; ++ci) {
+    int guard = 0;
+    while (ov[ci]) {
+      // Raw candidate storage overflowed for this chunk: grow it and redo.
+      if (++guard > 8) {
+        set_error("search: raw candidate storage overflow");
+        return PSR_ECAPACITY;
+      }
+      sw.raw_cap *= 4;
+      PSR_TRY(enqueue_chunk(o, ci, st));
+      unsigned v = 0;
+      PSR_CUDA(cudaMemcpyAsync(&v, chunk_overflow.as<unsigned>() + ci, 4,
+                               cudaMemcpyDeviceToHost, st));
+      PSR_CUDA(cudaStreamSynchronize(st));
+      ov[ci] = v;
+    }
+  }
+  return PSR_OK;
+}
+
+int SearchEngine::collect(cudaStream_t st, uint64_t *counts, psr_candidate *out, uint64_t cap,
+                          uint64_t *n_total) {
+  const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
+  std::vector<unsigned> kc(ntrials);
+  std::vector<psr_candidate> all(ntrials * maxc);
+  PSR_CUDA(cudaMemcpyAsync(kc.data(), kept_count.p, ntrials * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(all.data(), kept.p, all.size() * sizeof(psr_candidate),
+                           cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  uint64_t k = 0;
+  for (uint64_t i = 0; i < ntrials; ++i) {
+    if (counts) counts[i] = kc[i];
+    for (unsigned j = 0; j < kc[i]; ++j) {
+      if (out && k < cap) out[k] = all[i * maxc + j];
+      ++k;
+    }
+  }
+  *n_total = k;
+  if (out && k > cap) {
+    set_error("search: candidate buffer too small (" + std::to_string(k) + " needed)");
+    return PSR_ECAPACITY;
+  }
+  return PSR_OK;
+}
+
+}  // namespace psr
+
+namespace psr {
+
+// Delay tables in FP64 on the host (dedisperse/src/lib.rs:9-34).
+int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
+                     std::vector<uint32_t> &tab, uint64_t &max_spread, uint64_t &max_delay) {
+  std::vector<double> freqs(o.nch);
+  for (uint64_t c = 0; c < o.nch; ++c) freqs[c] = o.h.fch1 + (double)c * o.h.foff;
+  tab.assign(ntrials * o.nch, 0);
+  std::vector<uint64_t> d;
+  max_delay = 0;
+  for (uint64_t i = 0; i < ntrials; ++i) {
+    if (!host_delays(freqs.data(), o.nch, o.h.tsamp, trials[i], d)) return PSR_EDEDISPERSE;
+    for (uint64_t c = 0; c < o.nch; ++c) {
+      max_delay = std::max(max_delay, d[c]);
+      tab[i * o.nch + c] = (uint32_t)std::min<uint64_t>(d[c], 0xffffffffull);
+    }
+  }
+  if (max_delay > o.ns) {
+    set_error("invalid dedispersion input: delay exceeds observation");
+    return PSR_EDEDISPERSE;
+  }
+  // Widest delay spread of any channel inside a block of 8 consecutive trials.
+  max_spread = 0;
+  for (uint64_t b = 0; b < ntrials; b += 8)
+    for (uint64_t c = 0; c < o.nch; ++c) {
+      uint32_t lo = 0xffffffffu, hi = 0;
+      for (uint64_t i = b; i < std::min<uint64_t>(b + 8, ntrials); ++i) {
+        lo = std::min(lo, tab[i * o.nch + c]);
+        hi = std::max(hi, tab[i * o.nch + c]);
+      }
+      max_spread = std::max<uint64_t>(max_spread, hi - lo);
+    }
+  return PSR_OK;
+}
+
+}  // namespace psr

@@ -1,0 +1,41 @@
+// Search engine shared by the C ABI entry points and the session.
+#pragma once
+#include "psr_internal.h"
+
+namespace psr {
+
+struct SearchEngine {
+  uint64_t chunk = 64;  // trials per chunk (tunable)
+  uint64_t ntrials = 0, n = 0, nch = 0, ldo = 0, ldp = 0, nparts = 0, nchunks = 0;
+  uint64_t max_spread = 0;
+  uint32_t npsum = 0;
+  FftPlan fft;
+  SpecConfig spec;
+  SpecWork sw;
+  std::vector<double> host_sums;  // series sums supplied by the caller (optional)
+  // Optional per-stage timing: events recorded around every stage launch on
+  // the engine's stream; stage_ms accumulates their elapsed times.
+  enum { ST_DEDISP = 0, ST_FFT = 1, ST_SPEC = 2, ST_COUNT = 3 };
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_begin[ST_COUNT], ev_end[ST_COUNT];
+  double stage_ms[ST_COUNT] = {0, 0, 0};
+  uint64_t stage_launches[ST_COUNT] = {0, 0, 0};
+  int record(int stage, bool begin, cudaStream_t st);
+  int harvest();  // after a sync: add elapsed times, forget the events
+  ~SearchEngine();
+  DevBuf delays, trial_dm, series, parts, sums, work, power, psum, kept, kept_count, err,
+      chunk_overflow;
+
+  // Delay tables, FFT plan and buffers for ntrials trials of length n.
+  int prepare(const DeviceObs &o, const double *trials, uint64_t ntrials, uint64_t n,
+              const SpecConfig &cfg, cudaStream_t st);
+  int enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st);
+  // All chunks, asynchronously.
+  int enqueue(const DeviceObs &o, cudaStream_t st);
+  // Synchronise; redo chunks whose raw candidate storage overflowed.
+  int finish(const DeviceObs &o, cudaStream_t st);
+  int collect(cudaStream_t st, uint64_t *counts, psr_candidate *out, uint64_t cap,
+              uint64_t *n_total);
+};
+
+}  // namespace psr

@@ -1,0 +1,93 @@
+"""C ABI checks that need no GPU: the library builds, loads and exports every
+function include/psr.h declares; host-side functions match the oracle."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "psr.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(psr_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from pulsarsr_gb300 import build
+    build.build()
+    from pulsarsr_gb300 import _lib
+    return _lib.lib()
+
+
+def test_exports_every_declared_symbol(L):
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_version(L):
+    import pulsarsr_gb300
+    assert "sm_103a" in pulsarsr_gb300.version()
+
+
+def test_parse_header_matches_oracle_and_errors(L, oracle):
+    from pulsarsr_gb300 import FormatError, IoError, fbank, synth
+    raw = synth.header_bytes(96, 4, 7.2e-5, 1448.0, -1.0) + bytes(96 // 2 * 4)
+    h = fbank.parse_header(raw)
+    o = oracle.parse_header(raw)
+    assert (h.nchans, h.nbits, h.tsamp, h.fch1, h.foff, h.data_offset) == \
+        (o["nchans"], o["nbits"], o["tsamp"], o["fch1"], o["foff"], o["data_offset"])
+    with pytest.raises(FormatError, match="unknown keyword surprise"):
+        fbank.parse_header(synth._s("HEADER_START") + synth._s("surprise"))
+    with pytest.raises(FormatError, match="missing HEADER_START"):
+        fbank.parse_header(synth._s("HEADER_BEGIN"))
+    with pytest.raises(IoError):
+        fbank.parse_header(synth._s("HEADER_START")[:-2])
+
+
+@pytest.mark.parametrize("dm", [0.0, 0.25, 62.0, 62.389, 499.86, 3000.0])
+def test_delays_match_oracle(L, oracle, dm):
+    from pulsarsr_gb300 import dedisperse
+    for freqs, tsamp in ((1447.5 - np.arange(96), 7.2e-5), (1450 - 1.5625 * np.arange(64), 64e-6),
+                         (1200 + np.arange(4096) * (400 / 4096), 64e-6)):
+        assert np.array_equal(dedisperse.delays(freqs, tsamp, dm), oracle.delays(freqs, tsamp, dm))
+
+
+def test_plan_and_step_match_oracle(L, oracle):
+    from pulsarsr_gb300 import DedisperseError, dedisperse
+    f = 1447.5 - np.arange(96)
+    assert dedisperse.dm_step(f, 7.2e-5) == oracle.dm_step(f, 7.2e-5)
+    step = dedisperse.dm_step(f, 7.2e-5)
+    assert np.array_equal(dedisperse.plan(0, 500, step), oracle.plan(0, 500, step))
+    assert dedisperse.delays([1000., 2000.], 0.001, 1.).tolist() == [3, 0]
+    with pytest.raises(DedisperseError, match="invalid DM bounds/step"):
+        dedisperse.plan(0., 5., 0.)
+    with pytest.raises(DedisperseError, match="positive frequencies"):
+        dedisperse.delays([0.], 1., 1.)
+    with pytest.raises(DedisperseError, match="more than 100000"):
+        dedisperse.plan(0., 1e6, 1.)
+
+
+def test_sift_matches_oracle(L, oracle):
+    from pulsarsr_gb300 import search
+    rng = np.random.default_rng(7)
+    n = 400
+    c = np.zeros(n, dtype=search.CAND_DTYPE)
+    c["frequency_hz"] = rng.choice([10.0, 20.0, 30.0, 47.3, 100.0], n) + rng.normal(0, 0.01, n)
+    c["period_s"] = 1 / c["frequency_hz"]
+    c["dm"] = rng.choice([0.0, 5.0, 62.0], n)
+    c["harmonics"] = rng.choice([1, 2, 4], n)
+    c["score"] = np.round(rng.normal(10, 3, n), 1)  # ties exercise the stable order
+    for reject in (False, True):
+        a = search.sift(c, 0.02, 7, reject)
+        b = oracle.sift(c, 0.02, 7, reject)
+        assert a.tobytes() == b.tobytes()
+    c2 = np.array([(100., .01, 20., 1, 10.), (200., .005, 21., 1, 8.), (100.01, .01, 19., 1, 9.),
+                   (137., 1 / 137., 0., 1, 20.)], dtype=search.CAND_DTYPE)
+    k = search.sift(c2, 0.1, 10, True)
+    assert len(k) == 1 and k[0]["dm"] == 20.
