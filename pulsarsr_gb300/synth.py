@@ -139,12 +139,14 @@ def config_c1(seed: int = 1) -> Observation:
 
 
 def config_c2(seed: int = 2) -> Observation:
-    """GBT L-band tutorial shape: 96 x 1 MHz channels from 1448 MHz, 4-bit,
-    72 us, 531000 samples; 4-bit noise around level 8 with +-20% channel
-    gains; a 4.6214 ms pulsar at DM 62.4 (3% duty, folded SNR ~30), a
-    28.76 Hz zero-DM tone and 5 broadband bursts."""
-    return Observation(nchans=96, nbits=4, nsamples=531000, tsamp=72e-6, fch1=1448.0,
+    """GBT L-band tutorial shape: 96 x 1 MHz channels, first channel at
+    1447.5 MHz as in the tutorial file's header (so the default DM step gives
+    the reference's 2000-trial plan over 0-500), 4-bit, 72 us, 531000
+    samples; 4-bit noise around level 8 with +-20% channel gains; a 4.6214 ms
+    pulsar at DM 62.4 (3% duty, folded SNR ~30), a 28.76 Hz zero-DM tone and
+    5 broadband bursts."""
+    return Observation(nchans=96, nbits=4, nsamples=531000, tsamp=72e-6, fch1=1447.5,
                        foff=-1.0, seed=seed, noise_mean=8.0, noise_sigma=2.0, gain_spread=0.2,
-                       pulsars=[Pulsar(0.0046214, 62.4, 0.03, 0.15)], tone_hz=28.76,
+                       pulsars=[Pulsar(0.0046214, 62.4, 0.03, 0.04)], tone_hz=28.76,
                        tone_amplitude=0.05, bursts=5, burst_amplitude=1.0,
                        name="config2 GBT-shaped synthetic")
