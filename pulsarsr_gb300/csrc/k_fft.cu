@@ -29,9 +29,7 @@
 namespace psr {
 namespace {
 
-struct Cx {
-  float x, y;
-};
+constexpr int LB = 16;  // loads in flight per thread when staging a tile
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
   return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
 }
@@ -215,7 +213,7 @@ __device__ __forceinline__ float trial_mean(const double *sums, uint64_t trial, 
 }
 
 // Whole transform in one CTA per trial (M <= 4096).
-__global__ void k_fft_small(const float *__restrict__ series, uint64_t lds, uint64_t len,
+__global__ void __launch_bounds__(512) k_fft_small(const float *__restrict__ series, uint64_t lds, uint64_t len,
                             const double *__restrict__ sums, const float2 *__restrict__ Q,
                             int lq, uint32_t N, uint32_t M, float *__restrict__ power,
                             uint64_t ldp, double *__restrict__ psum) {
@@ -248,7 +246,7 @@ __global__ void k_fft_small(const float *__restrict__ series, uint64_t lds, uint
 }
 
 // Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
-__global__ void k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
+__global__ void __launch_bounds__(512) k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
                             const double *__restrict__ sums, const float2 *__restrict__ Q,
                             int lq, uint32_t N, uint32_t M, uint32_t M1, uint32_t M2, int C,
                             float2 *__restrict__ work) {
@@ -262,10 +260,21 @@ __global__ void k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint
   const float mean = trial_mean(sums, trial, len);
   build_wl(Wl, (int)M1, N, Q, lq);
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
-  for (int idx = threadIdx.x; idx < (int)M1 * C; idx += blockDim.x) {
-    const int col = idx % C, n1 = idx / C;
-    const uint64_t n = (uint64_t)n1 * M2 + n2_0 + col;
-    sm[n1 * S + col] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+  const int total = (int)M1 * C;
+  // Batches of LB independent loads per thread keep many requests in flight.
+  for (int base = 0; base < total; base += LB * (int)blockDim.x) {
+    float2 v[LB];
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const uint64_t n = (uint64_t)(idx / C) * M2 + n2_0 + (idx % C);
+      v[u] = (idx < total && n < nz) ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      if (idx < total) sm[(idx / C) * S + (idx % C)] = v[u];
+    }
   }
   __syncthreads();
   subfft(sm, S, C, (int)M1, Wl);
@@ -283,7 +292,7 @@ __global__ void k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint
 // Pass 2: row sub-FFTs of length M2 for a group of rows and their mirrors,
 // then the real post-processing and |X|^2.  Group 0 holds rows 0 and M1/2;
 // group g >= 1 holds rows kb..kb+h-1 (kb = 1 + (g-1)*H) and M1-kb..M1-kb-h+1.
-__global__ void k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q,
+__global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q,
                             int lq, uint32_t N, uint32_t M, uint32_t M1, uint32_t M2, int C,
                             float *__restrict__ power, uint64_t ldp,
                             double *__restrict__ psum, uint32_t ngroups) {
@@ -306,12 +315,23 @@ __global__ void k_fft_pass2(const float2 *__restrict__ work, const float2 *__res
   }
   const int ncols = 2 * h;
   build_wl(Wl, (int)M2, N, Q, lq);
-  for (int idx = threadIdx.x; idx < (int)M2 * ncols; idx += blockDim.x) {
-    const int pos = idx % (int)M2, ci = idx / (int)M2;
-    uint32_t k1;
-    if (g == 0) k1 = ci == 0 ? 0 : M1 / 2;
-    else k1 = ci < h ? kb + ci : M1 - (kb + (ci - h));
-    sm[pos * S + ci] = in[(uint64_t)k1 * M2 + pos];
+  const int total = (int)M2 * ncols;
+  for (int base = 0; base < total; base += LB * (int)blockDim.x) {
+    float2 v[LB];
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const int pos = idx % (int)M2, ci = idx / (int)M2;
+      uint32_t k1;
+      if (g == 0) k1 = ci == 0 ? 0 : M1 / 2;
+      else k1 = ci < h ? kb + ci : M1 - (kb + (ci - h));
+      v[u] = idx < total ? in[(uint64_t)k1 * M2 + pos] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      if (idx < total) sm[(idx % (int)M2) * S + idx / (int)M2] = v[u];
+    }
   }
   __syncthreads();
   subfft(sm, S, ncols, (int)M2, Wl);

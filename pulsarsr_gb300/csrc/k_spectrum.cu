@@ -31,15 +31,17 @@ constexpr float LN2F = 0.693147180559945309f;
 
 __device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
 
-// Number of elements <= key in a sorted chunk of n keys (n <= 64).
-__device__ __forceinline__ int count_le(const uint32_t *a, int n, uint32_t key) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (a[mid] <= key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
+// Number of elements <= key in a sorted chunk of 64 keys (invalid slots hold
+// 0xffffffff, above every finite float pattern).  Branchless, 7 probes.
+__device__ __forceinline__ int count_le64(const uint32_t *a, uint32_t key) {
+  int pos = (a[31] <= key) ? 32 : 0;
+  pos += (a[pos + 15] <= key) ? 16 : 0;
+  pos += (a[pos + 7] <= key) ? 8 : 0;
+  pos += (a[pos + 3] <= key) ? 4 : 0;
+  pos += (a[pos + 1] <= key) ? 2 : 0;
+  pos += (a[pos] <= key) ? 1 : 0;
+  pos += (a[pos] <= key) ? 1 : 0;
+  return pos;
 }
 
 // Sort 64 keys held two per lane (index lane and lane+32) ascending.
@@ -74,17 +76,21 @@ __device__ __forceinline__ void warp_sort64(uint32_t &x0, uint32_t &x1) {
   }
 }
 
+// Chunks are stored with a 65-word stride so that threads probing the same
+// index of different chunks hit different banks.
+constexpr int SC_STRIDE = 65;
+
 __global__ void __launch_bounds__(SC_G)
     k_scales(const float *__restrict__ power, uint64_t ldp, uint64_t plen,
              const double *__restrict__ psum, uint32_t npsum, float *__restrict__ scale,
              uint64_t lds, uint64_t nblocks) {
-  __shared__ uint32_t ch[SC_CH][64];
+  __shared__ uint32_t ch[SC_CH * SC_STRIDE];
   __shared__ int cnt[SC_CH];
   __shared__ float floor_s;
   const uint64_t trial = blockIdx.y;
   const float *raw = power + trial * ldp;
   const long long b0 = (long long)blockIdx.x * SC_G;
-  const long long c_first = b0 - 2;  // chunk index of ch[0]
+  const long long c_first = b0 - 2;  // chunk index of local chunk 0
   const long long last_chunk = (long long)((plen - 1) / 64);
   if (threadIdx.x == 0) {
     double s = 0.0;
@@ -96,7 +102,7 @@ __global__ void __launch_bounds__(SC_G)
     const long long c = c_first + ci;
     uint32_t x0 = 0xffffffffu, x1 = 0xffffffffu;
     int n = 0;
-    if (c >= 0 && c <= last_chunk) {
+    if (c >= 0 && c <= last_chunk) {  // out-of-range chunks stay all-sentinel
       const long long base = c * 64;
       const long long e0 = base + lane, e1 = base + lane + 32;
       if (e0 < (long long)plen && e0 >= 1) x0 = fbits(raw[e0]);
@@ -104,8 +110,8 @@ __global__ void __launch_bounds__(SC_G)
       n = (int)min(64ll, (long long)plen - base) - (c == 0 ? 1 : 0);
     }
     warp_sort64(x0, x1);
-    ch[ci][lane] = x0;
-    ch[ci][lane + 32] = x1;
+    ch[ci * SC_STRIDE + lane] = x0;
+    ch[ci * SC_STRIDE + lane + 32] = x1;
     if (lane == 0) cnt[ci] = n;
   }
   __syncthreads();
@@ -114,24 +120,24 @@ __global__ void __launch_bounds__(SC_G)
   const long long center = b * 64;
   const long long lo = max(center - 128, 1ll);
   const long long hi = min(center + 192, (long long)plen);
-  const int total = (int)(hi - lo);
-  const int r = total / 2;
-  // chunks of the window: b-2 .. b+2 (clipped), local indices threadIdx.x .. +4
-  int cl = threadIdx.x, chi = threadIdx.x + 4;
-  while (c_first + cl < 0) ++cl;
-  while (c_first + chi > last_chunk) --chi;
-  uint32_t kmin = 0xffffffffu, kmax = 0;
-  for (int c = cl; c <= chi; ++c)
-    if (cnt[c] > 0) {
-      kmin = min(kmin, ch[c][0]);
-      kmax = max(kmax, ch[c][cnt[c] - 1]);
+  const int r = (int)(hi - lo) / 2;
+  // The window is local chunks threadIdx.x .. threadIdx.x + 4 (chunks b-2..b+2).
+  const uint32_t *w = ch + threadIdx.x * SC_STRIDE;
+  uint32_t lo_k = 0xffffffffu, hi_k = 0;
+#pragma unroll
+  for (int d = 0; d < 5; ++d) {
+    const int n = cnt[threadIdx.x + d];
+    if (n > 0) {
+      lo_k = min(lo_k, w[d * SC_STRIDE]);
+      hi_k = max(hi_k, w[d * SC_STRIDE + n - 1]);
     }
-  // smallest key K with count(<= K) > r
-  uint32_t lo_k = kmin, hi_k = kmax;
+  }
+  // smallest key K with count(<= K) > r; it is an element of the window
   while (lo_k < hi_k) {
     const uint32_t mid = lo_k + ((hi_k - lo_k) >> 1);
     int c_le = 0;
-    for (int c = cl; c <= chi; ++c) c_le += count_le(ch[c], cnt[c], mid);
+#pragma unroll
+    for (int d = 0; d < 5; ++d) c_le += count_le64(w + d * SC_STRIDE, mid);
     if (c_le > r) hi_k = mid;
     else lo_k = mid + 1;
   }
@@ -157,6 +163,7 @@ struct HarmArgs {
   int nbirdies;
   double bin_hz;
   double threshold;
+  float t1;  // smallest float v with (double)v - 1.0 >= threshold
   uint64_t first;
   uint64_t end[5];  // end_h for h = 1,2,4,8,16 (0 when the h loop is skipped)
   RawCand *raw;
@@ -232,15 +239,65 @@ __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64
   a.raw[trial * a.raw_cap + slot] = c;
 }
 
-__global__ void k_harmonic(HarmArgs a) {
+// All harmonic levels h >= 2 of one bin whose fundamental passes the gate:
+// one parabolic offset, positions (k+off)*j computed once, cumulative f64
+// sums in j order (the reference's per-h sums are the same prefix sums).
+__device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, const float *sc,
+                          uint64_t k) {
+  int hmax = 0;
+#pragma unroll
+  for (int hi = 1; hi < 5; ++hi)
+    if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
+  if (hmax == 0) return;
+  const double off = offset_at(raw, k);
+  const double kf = __dadd_rn((double)k, off);
+  double sum = -0.0;
+  int j = 1;
+  for (int hi = 1; hi <= hmax; ++hi) {
+    const int h = 1 << hi;
+    for (; j <= h; ++j) {
+      uint64_t idx = (uint64_t)round(__dmul_rn(kf, (double)j));
+      if (idx > a.plen - 1) idx = a.plen - 1;
+      sum = __dadd_rn(sum, (double)pw(a, raw, sc, idx));
+    }
+    const double s = inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
+    if (s >= a.threshold) {
+      const double sm = score_at(a, raw, sc, k - 1, hi);
+      const double sp = score_at(a, raw, sc, k + 1, hi);
+      if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
+    }
+  }
+}
+
+constexpr int HM_NT = 256;
+constexpr int HM_KPT = 4;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
+
+// Every bin is first tested with exact f32 gates: an h = 1 peak needs
+// max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value minus 1
+// reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and h >= 2
+// scores exist only where pw(k) >= 4.  The rare bins that pass are queued in
+// shared memory and evaluated with every lane busy.
+__global__ void __launch_bounds__(HM_NT) k_harmonic(HarmArgs a) {
+  __shared__ uint32_t q1[HM_NT * HM_KPT], q2[HM_NT * HM_KPT];
+  __shared__ int n1, n2;
   const uint64_t trial = blockIdx.y;
   const float *raw = a.power + trial * a.ldp;
   const float *sc = a.scale + trial * a.lds;
-  const uint64_t k = a.first + 1 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a.end[0] == 0 || k + 1 > a.end[0]) return;  // k in [first+1, end_1 - 1]
-  // h = 1: score(k) is pw(k) - 1 or pw(k+1) - 1.
-  const float p0 = pw(a, raw, sc, k), p1 = pw(a, raw, sc, k + 1);
-  if ((double)fmaxf(p0, p1) - 1.0 >= a.threshold) {
+  if (threadIdx.x == 0) n1 = n2 = 0;
+  __syncthreads();
+  const uint64_t kb = a.first + 1 + (uint64_t)blockIdx.x * HM_NT * HM_KPT;
+#pragma unroll
+  for (int i = 0; i < HM_KPT; ++i) {
+    const uint64_t k = kb + (uint64_t)i * HM_NT + threadIdx.x;
+    if (k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
+    const float p0 = pw(a, raw, sc, k), p1 = pw(a, raw, sc, k + 1);
+    const uint32_t rel = (uint32_t)(k - kb);
+    if (fmaxf(p0, p1) >= a.t1) q1[atomicAdd(&n1, 1)] = rel;
+    if (p0 >= 4.0f) q2[atomicAdd(&n2, 1)] = rel;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n1; i += blockDim.x) {
+    const uint64_t k = kb + q1[i];
     const double s = score_at(a, raw, sc, k, 0);
     if (s >= a.threshold) {
       const double sm = score_at(a, raw, sc, k - 1, 0);
@@ -248,17 +305,7 @@ __global__ void k_harmonic(HarmArgs a) {
       if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
     }
   }
-  if (p0 < 4.0f) return;
-  for (int hi = 1; hi < 5; ++hi) {
-    const uint64_t e = a.end[hi];
-    if (e == 0 || k + 1 > e) continue;  // k must lie in [first+1, end_h - 1]
-    const double s = score_at(a, raw, sc, k, hi);
-    if (s >= a.threshold) {
-      const double sm = score_at(a, raw, sc, k - 1, hi);
-      const double sp = score_at(a, raw, sc, k + 1, hi);
-      if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
-    }
-  }
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) harm_item(a, trial, raw, sc, kb + q2[i]);
 }
 
 // Orderable key: score descending, then (h, k) ascending = the reference's
@@ -445,45 +492,56 @@ __global__ void __launch_bounds__(SEL_NT) k_select(SelArgs a) {
 
 }  // namespace
 
-int spectrum_enqueue_ex(const FftPlan &p, const SpecConfig &c, const float *d_power,
-                        uint64_t ldp, const double *d_psum, uint32_t npsum,
-                        const double *d_trial_dm, uint64_t ntrials, SpecWork &w,
-                        cudaStream_t st) {
-  const uint64_t plen = p.M + 1;
-  const uint64_t nblocks = (plen + 63) / 64;
-  const uint64_t lds = ((nblocks + 63) / 64) * 64;
-  if (c.max_candidates > 64) {
-    set_error("search: at most 64 candidates per trial are supported");
+// Buffers for up to `outer` trials of raw candidates and `inner` trials of
+// normalisation scales; uploads the birdie list.
+int spectrum_prepare(const FftPlan &p, const SpecConfig &c, uint64_t outer, uint64_t inner,
+                     SpecWork &w, cudaStream_t st) {
+  if (c.max_candidates > 64 || c.max_candidates < 1) {
+    set_error("search: 1..64 candidates per trial are supported");
     return PSR_EINVAL;
   }
-  PSR_TRY(w.scale.ensure(ntrials * lds * 4));
+  const uint64_t plen = p.M + 1;
+  const uint64_t nblocks = (plen + 63) / 64;
+  w.lds = ((nblocks + 63) / 64) * 64;
   if (w.raw_cap == 0) w.raw_cap = 2048;
-  PSR_TRY(w.raw.ensure(ntrials * w.raw_cap * sizeof(RawCand)));
-  PSR_TRY(w.raw_count.ensure(ntrials * 4));
-  PSR_TRY(w.kept.ensure(ntrials * std::max<uint64_t>(c.max_candidates, 1) * sizeof(psr_candidate)));
-  PSR_TRY(w.kept_count.ensure(ntrials * 4));
+  PSR_TRY(w.scale.ensure(inner * w.lds * 4));
+  PSR_TRY(w.raw.ensure(outer * w.raw_cap * sizeof(RawCand)));
+  PSR_TRY(w.raw_count.ensure(outer * 4));
   PSR_TRY(w.overflow.ensure(16));
   PSR_TRY(w.birdies.ensure(std::max<size_t>(c.birdies.size(), 2) * 8));
   if (!c.birdies.empty())
     PSR_CUDA(cudaMemcpyAsync(w.birdies.p, c.birdies.data(), c.birdies.size() * 8,
                              cudaMemcpyHostToDevice, st));
-  PSR_CUDA(cudaMemsetAsync(w.raw_count.p, 0, ntrials * 4, st));
+  return PSR_OK;
+}
+
+int spectrum_reset(SpecWork &w, uint64_t outer_trials, cudaStream_t st) {
+  PSR_CUDA(cudaMemsetAsync(w.raw_count.p, 0, outer_trials * 4, st));
   PSR_CUDA(cudaMemsetAsync(w.overflow.p, 0, 16, st));
+  return PSR_OK;
+}
+
+// Normalisation scales and harmonic peaks of `ntrials` spectra; their raw
+// candidates go to slots [slot0, slot0 + ntrials) of the outer chunk.
+int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_power,
+                       uint64_t ldp, const double *d_psum, uint32_t npsum, uint64_t ntrials,
+                       uint64_t slot0, SpecWork &w, cudaStream_t st) {
+  const uint64_t plen = p.M + 1;
+  const uint64_t nblocks = (plen + 63) / 64;
   {
     dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
-    k_scales<<<grid, SC_G, 0, st>>>(d_power, ldp, plen, d_psum, npsum, w.scale.as<float>(), lds,
-                                    nblocks);
+    k_scales<<<grid, SC_G, 0, st>>>(d_power, ldp, plen, d_psum, npsum, w.scale.as<float>(),
+                                    w.lds, nblocks);
     PSR_CUDA(cudaGetLastError());
   }
   // search/src/lib.rs:62, 73-78
-  const double size = (double)p.N;
-  const double bin_hz = 1.0 / (size * c.tsamp);
+  const double bin_hz = 1.0 / ((double)p.N * c.tsamp);
   HarmArgs a{};
   a.power = d_power;
   a.ldp = ldp;
   a.plen = plen;
   a.scale = w.scale.as<float>();
-  a.lds = lds;
+  a.lds = w.lds;
   a.birdies = w.birdies.as<double>();
   a.nbirdies = (int)(c.birdies.size() / 2);
   a.bin_hz = bin_hz;
@@ -498,35 +556,44 @@ int spectrum_enqueue_ex(const FftPlan &p, const SpecConfig &c, const float *d_po
     const uint64_t e = std::min(last, (plen - 2) / h);
     a.end[hi] = (e <= first + 1) ? 0 : e;
   }
-  a.raw = w.raw.as<RawCand>();
-  a.raw_count = w.raw_count.as<unsigned>();
+  a.raw = w.raw.as<RawCand>() + slot0 * w.raw_cap;
+  a.raw_count = w.raw_count.as<unsigned>() + slot0;
   a.raw_cap = w.raw_cap;
   a.overflow = w.overflow.as<unsigned>();
+  {
+    // exact f32 form of the h = 1 prefilter (double)max(pw) - 1.0 >= threshold
+    float v = (float)(c.threshold + 1.0);
+    if (std::isnan(v)) v = INFINITY;
+    for (int it = 0; it < 64 && (double)v - 1.0 >= c.threshold; ++it)
+      v = std::nextafter(v, -INFINITY);
+    for (int it = 0; it < 64 && !((double)v - 1.0 >= c.threshold); ++it)
+      v = std::nextafter(v, INFINITY);
+    a.t1 = v;
+  }
   if (a.end[0] > first + 1) {
     const uint64_t nk = a.end[0] - first - 1;
-    dim3 grid((unsigned)((nk + 255) / 256), (unsigned)ntrials);
-    k_harmonic<<<grid, 256, 0, st>>>(a);
+    dim3 grid((unsigned)((nk + HM_NT * HM_KPT - 1) / (HM_NT * HM_KPT)), (unsigned)ntrials);
+    k_harmonic<<<grid, HM_NT, 0, st>>>(a);
     PSR_CUDA(cudaGetLastError());
   }
+  return PSR_OK;
+}
+
+// Sort/dedupe the raw candidates of `ntrials` trials into kept[][max_candidates].
+int spectrum_select(const FftPlan &p, const SpecConfig &c, const double *d_trial_dm,
+                    uint64_t ntrials, SpecWork &w, psr_candidate *d_kept, unsigned *d_kept_count,
+                    cudaStream_t st) {
   SelArgs s{};
-  s.raw = a.raw;
-  s.raw_count = a.raw_count;
+  s.raw = w.raw.as<RawCand>();
+  s.raw_count = w.raw_count.as<unsigned>();
   s.raw_cap = w.raw_cap;
   s.trial_dm = d_trial_dm;
   s.tol = 1.0 / ((double)p.len * c.tsamp);
   s.max_candidates = c.max_candidates;
-  s.kept = w.kept.as<psr_candidate>();
-  s.kept_count = w.kept_count.as<unsigned>();
+  s.kept = d_kept;
+  s.kept_count = d_kept_count;
   k_select<<<(unsigned)ntrials, SEL_NT, 0, st>>>(s);
   PSR_CUDA(cudaGetLastError());
-  return PSR_OK;
-}
-
-int spectrum_check_overflow(SpecWork &w, uint64_t, cudaStream_t st, bool &overflow) {
-  unsigned v = 0;
-  PSR_CUDA(cudaMemcpyAsync(&v, w.overflow.p, 4, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaStreamSynchronize(st));
-  overflow = v != 0;
   return PSR_OK;
 }
 

@@ -159,6 +159,42 @@ __device__ __forceinline__ float as_f32(T v) {
   return (float)v;
 }
 
+// Element e of a 16-byte vector of T.
+template <class T>
+__device__ __forceinline__ float vec_elem(const uint4 &w, int e) {
+  const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+  if constexpr (sizeof(T) == 1) return (float)((words[e >> 2] >> (8 * (e & 3))) & 255u);
+  else if constexpr (sizeof(T) == 2) return (float)((words[e >> 1] >> (16 * (e & 1))) & 0xffffu);
+  else return __uint_as_float(words[e]);
+}
+
+// Visit row[0..ns) strictly in order, keeping SEQ_DEPTH 16-byte loads in
+// flight ahead of the (latency-bound) sequential consumer f.
+constexpr int SEQ_DEPTH = 8;
+template <class T, class F>
+__device__ __forceinline__ void seq_visit(const T *row, uint64_t ns, F &&f) {
+  constexpr int E = 16 / (int)sizeof(T);
+  const uint4 *v = reinterpret_cast<const uint4 *>(row);  // rows are 64-byte aligned
+  const uint64_t nv = ns / E;
+  uint4 nxt[SEQ_DEPTH];
+#pragma unroll
+  for (int i = 0; i < SEQ_DEPTH; ++i) nxt[i] = (uint64_t)i < nv ? v[i] : make_uint4(0, 0, 0, 0);
+  for (uint64_t q = 0; q < nv; q += SEQ_DEPTH) {
+    uint4 cur[SEQ_DEPTH];
+#pragma unroll
+    for (int i = 0; i < SEQ_DEPTH; ++i) {
+      cur[i] = nxt[i];
+      if (q + SEQ_DEPTH + i < nv) nxt[i] = v[q + SEQ_DEPTH + i];
+    }
+#pragma unroll
+    for (int i = 0; i < SEQ_DEPTH; ++i)
+      if (q + i < nv)
+#pragma unroll
+        for (int e = 0; e < E; ++e) f(vec_elem<T>(cur[i], e));
+  }
+  for (uint64_t t = nv * E; t < ns; ++t) f(as_f32(row[t]));
+}
+
 // Channel means and variances (rfi/src/lib.rs:35-43): one thread per channel
 // in reference order.  The mean's sum is taken from the exact integer total
 // when every partial sum is an integer <= 2^24 (identical f32 result).
@@ -174,36 +210,14 @@ __global__ void k_chan_mean_var(const T *__restrict__ s, uint64_t ns, uint64_t l
     sum = (float)tot[c];
   } else {
     sum = -0.0f;
-    for (uint64_t t = 0; t < ns; ++t) sum = __fadd_rn(sum, as_f32(row[t]));
+    seq_visit(row, ns, [&](float x) { sum = __fadd_rn(sum, x); });
   }
   const float m = __fdiv_rn(sum, (float)ns);
   float acc = -0.0f;
-  if constexpr (sizeof(T) == 1) {
-    // 16 samples per aligned vector load; rows start 64-byte aligned.
-    const uint4 *v = reinterpret_cast<const uint4 *>(row);
-    uint64_t nv = ns / 16, t = 0;
-    for (uint64_t q = 0; q < nv; ++q) {
-      uint4 w = v[q];
-      uint32_t words[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          float d = __fsub_rn((float)((words[a] >> (8 * b)) & 255u), m);
-          acc = __fadd_rn(acc, __fmul_rn(d, d));
-        }
-      t += 16;
-    }
-    for (; t < ns; ++t) {
-      float d = __fsub_rn((float)row[t], m);
-      acc = __fadd_rn(acc, __fmul_rn(d, d));
-    }
-  } else {
-    for (uint64_t t = 0; t < ns; ++t) {
-      float d = __fsub_rn(as_f32(row[t]), m);
-      acc = __fadd_rn(acc, __fmul_rn(d, d));
-    }
-  }
+  seq_visit(row, ns, [&](float x) {
+    const float d = __fsub_rn(x, m);
+    acc = __fadd_rn(acc, __fmul_rn(d, d));
+  });
   means[c] = m;
   vars[c] = __fdiv_rn(acc, (float)ns);
 }

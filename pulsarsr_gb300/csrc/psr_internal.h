@@ -147,11 +147,19 @@ struct SpecConfig {
   std::vector<double> birdies;  // pairs
 };
 struct SpecWork {
-  DevBuf scale, raw, raw_count, kept, kept_count, birdies, overflow, trial_dm;
-  uint64_t raw_cap = 0;
+  DevBuf scale, raw, raw_count, birdies, overflow;
+  uint64_t raw_cap = 0;  // raw (pre-dedupe) candidates per trial
+  uint64_t lds = 0;      // row stride of scale[]
 };
-int spectrum_check_overflow(SpecWork &w, uint64_t ntrials, cudaStream_t st,
-                            bool &overflow);
+int spectrum_prepare(const FftPlan &p, const SpecConfig &c, uint64_t outer, uint64_t inner,
+                     SpecWork &w, cudaStream_t st);
+int spectrum_reset(SpecWork &w, uint64_t outer_trials, cudaStream_t st);
+int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_power,
+                       uint64_t ldp, const double *d_psum, uint32_t npsum, uint64_t ntrials,
+                       uint64_t slot0, SpecWork &w, cudaStream_t st);
+int spectrum_select(const FftPlan &p, const SpecConfig &c, const double *d_trial_dm,
+                    uint64_t ntrials, SpecWork &w, psr_candidate *d_kept, unsigned *d_kept_count,
+                    cudaStream_t st);
 
 // Row stride (floats) of a dedispersed series buffer of length n.
 uint64_t series_ld(uint64_t n);
@@ -166,10 +174,6 @@ uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
 int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
                         const double *d_sums, uint64_t ntrials, float2 *d_work, float *d_power,
                         uint64_t ldp, double *d_psum, cudaStream_t st);
-int spectrum_enqueue_ex(const FftPlan &p, const SpecConfig &c, const float *d_power,
-                        uint64_t ldp, const double *d_psum, uint32_t npsum,
-                        const double *d_trial_dm, uint64_t ntrials, SpecWork &w,
-                        cudaStream_t st);
 
 // ------------------------------------------------------------- fold
 // Host statistics of a folded profile (fold/src/lib.rs:39-79).

@@ -35,16 +35,22 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   PSR_TRY(fft.init(n, st));
   ldo = series_ld(n);
   ldp = ((fft.M + 1 + 63) / 64) * 64;
-  if (chunk == 0) chunk = 64;
+  if (chunk == 0) chunk = 256;
   chunk = std::min(chunk, ntrials);
+  if (inner == 0) {
+    const uint64_t per = (fft.m > 12 ? fft.M * 8 : 0) + ldp * 4;
+    inner = std::max<uint64_t>(1, (96ull << 20) / per);
+  }
+  inner = std::min(inner, chunk);
   nparts = dedisperse_part_count(o, n);
   npsum = (uint32_t)fft.pass2_ctas();
   PSR_TRY(series.ensure(chunk * ldo * 4 + 256));
   PSR_TRY(parts.ensure(chunk * nparts * 8));
   PSR_TRY(sums.ensure(chunk * 8));
-  PSR_TRY(work.ensure(fft.m > 12 ? chunk * fft.M * 8 : 16));
-  PSR_TRY(power.ensure(chunk * ldp * 4));
-  PSR_TRY(psum.ensure(chunk * npsum * 8));
+  PSR_TRY(work.ensure(fft.m > 12 ? inner * fft.M * 8 : 16));
+  PSR_TRY(power.ensure(inner * ldp * 4));
+  PSR_TRY(psum.ensure(inner * npsum * 8));
+  PSR_TRY(spectrum_prepare(fft, spec, chunk, inner, sw, st));
   const uint64_t maxc = std::max<uint64_t>(cfg.max_candidates, 1);
   PSR_TRY(kept.ensure(ntrials * maxc * sizeof(psr_candidate)));
   PSR_TRY(kept_count.ensure(ntrials * 4));
@@ -65,22 +71,26 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
   PSR_TRY(record(ST_DEDISP, false, st));
   if (!host_sums.empty())
     PSR_CUDA(cudaMemcpyAsync(sums.p, host_sums.data() + t0, nt * 8, cudaMemcpyHostToDevice, st));
-  PSR_TRY(record(ST_FFT, true, st));
-  PSR_TRY(launch_raw_power_ex(fft, series.as<float>(), ldo, sums.as<double>(), nt,
-                              work.as<float2>(), power.as<float>(), ldp, psum.as<double>(), st));
-  PSR_TRY(record(ST_FFT, false, st));
-  // The spectrum stage writes straight into this chunk's slice of kept[].
+  PSR_TRY(spectrum_reset(sw, nt, st));
+  for (uint64_t i0 = 0; i0 < nt; i0 += inner) {
+    const uint64_t ni = std::min(inner, nt - i0);
+    PSR_TRY(record(ST_FFT, true, st));
+    PSR_TRY(launch_raw_power_ex(fft, series.as<float>() + i0 * ldo, ldo, sums.as<double>() + i0,
+                                ni, work.as<float2>(), power.as<float>(), ldp,
+                                psum.as<double>(), st));
+    PSR_TRY(record(ST_FFT, false, st));
+    PSR_TRY(record(ST_SPEC, true, st));
+    PSR_TRY(spectrum_harmonics(fft, spec, power.as<float>(), ldp, psum.as<double>(), npsum, ni,
+                               i0, sw, st));
+    PSR_TRY(record(ST_SPEC, false, st));
+  }
   const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
-  SpecWork &w = sw;
   PSR_TRY(record(ST_SPEC, true, st));
-  PSR_TRY(spectrum_enqueue_ex(fft, spec, power.as<float>(), ldp, psum.as<double>(), npsum,
-                              trial_dm.as<double>() + t0, nt, w, st));
+  PSR_TRY(spectrum_select(fft, spec, trial_dm.as<double>() + t0, nt, sw,
+                          kept.as<psr_candidate>() + t0 * maxc, kept_count.as<unsigned>() + t0,
+                          st));
   PSR_TRY(record(ST_SPEC, false, st));
-  PSR_CUDA(cudaMemcpyAsync(kept.as<psr_candidate>() + t0 * maxc, w.kept.p,
-                           nt * maxc * sizeof(psr_candidate), cudaMemcpyDeviceToDevice, st));
-  PSR_CUDA(cudaMemcpyAsync(kept_count.as<unsigned>() + t0, w.kept_count.p, nt * 4,
-                           cudaMemcpyDeviceToDevice, st));
-  PSR_CUDA(cudaMemcpyAsync(chunk_overflow.as<unsigned>() + ci, w.overflow.p, 4,
+  PSR_CUDA(cudaMemcpyAsync(chunk_overflow.as<unsigned>() + ci, sw.overflow.p, 4,
                            cudaMemcpyDeviceToDevice, st));
   return PSR_OK;
 }
@@ -142,6 +152,7 @@ int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
         return PSR_ECAPACITY;
       }
       sw.raw_cap *= 4;
+      PSR_TRY(spectrum_prepare(fft, spec, chunk, inner, sw, st));
       PSR_TRY(enqueue_chunk(o, ci, st));
       unsigned v = 0;
       PSR_CUDA(cudaMemcpyAsync(&v, chunk_overflow.as<unsigned>() + ci, 4,

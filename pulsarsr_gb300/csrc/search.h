@@ -5,7 +5,12 @@
 namespace psr {
 
 struct SearchEngine {
-  uint64_t chunk = 64;  // trials per chunk (tunable)
+  // Trials per outer chunk (dedispersion and candidate selection run over
+  // the whole chunk) and per inner chunk (FFT, normalisation and harmonic
+  // sums, sized so the FFT intermediate and the spectra stay in L2).
+  // 0 = automatic.
+  uint64_t chunk = 0;
+  uint64_t inner = 0;
   uint64_t ntrials = 0, n = 0, nch = 0, ldo = 0, ldp = 0, nparts = 0, nchunks = 0;
   uint64_t max_spread = 0;
   uint32_t npsum = 0;
