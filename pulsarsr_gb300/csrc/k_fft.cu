@@ -279,13 +279,26 @@ __global__ void __launch_bounds__(512) k_fft_pass1(const float *__restrict__ ser
   __syncthreads();
   subfft(sm, S, C, (int)M1, Wl);
   float2 *out = work + trial * (uint64_t)M;
-  for (int idx = threadIdx.x; idx < (int)M1 * C; idx += blockDim.x) {
-    const int col = idx % C, k1 = idx / C;
-    const uint32_t n2 = n2_0 + (uint32_t)col;
-    float2 v = sm[k1 * S + col];
-    const uint32_t e = n2 * (uint32_t)k1;
-    if (e != 0) v = cmul(v, twN(Q, 2u * e, lq));
-    out[(uint64_t)k1 * M2 + n2] = v;
+  // Twiddle loads for LB outputs are issued before any is consumed.
+  for (int base = 0; base < total; base += LB * (int)blockDim.x) {
+    float2 w[LB];
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const uint32_t e = (n2_0 + (uint32_t)(idx % C)) * (uint32_t)(idx / C);
+      w[u] = (idx < total && e != 0) ? twN(Q, 2u * e, lq) : make_float2(1.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      if (idx < total) {
+        const int col = idx % C, k1 = idx / C;
+        const uint32_t n2 = n2_0 + (uint32_t)col;
+        float2 v = sm[k1 * S + col];
+        if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
+        out[(uint64_t)k1 * M2 + n2] = v;
+      }
+    }
   }
 }
 
@@ -357,19 +370,35 @@ __global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ wo
       acc += (double)p;
     }
   } else {
-    for (int idx = threadIdx.x; idx < (int)M2 * h; idx += blockDim.x) {
-      const int p = idx % h;
-      const uint32_t k2 = (uint32_t)(idx / h);
-      const uint32_t k1 = kb + (uint32_t)p;
-      const uint32_t k = k1 + M1 * k2;
-      const uint32_t mk = M - k;
-      const float2 zk = sm[k2 * S + p];
-      const float2 zm = sm[(M2 - 1 - k2) * S + h + p];
-      const float pk = post_power(zk, zm, twN(Q, k, lq));
-      const float pm = post_power(zm, zk, twN(Q, mk, lq));
-      out[k] = pk;
-      out[mk] = pm;
-      acc += (double)pk + (double)pm;
+    constexpr int PB = LB / 2;  // bins per batch (two twiddles each)
+    const int tot2 = (int)M2 * h;
+    for (int base = 0; base < tot2; base += PB * (int)blockDim.x) {
+      float2 wk[PB], wm[PB];
+#pragma unroll
+      for (int u = 0; u < PB; ++u) {
+        const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+        const uint32_t k = kb + (uint32_t)(idx % h) + M1 * (uint32_t)(idx / h);
+        const bool in = idx < tot2;
+        wk[u] = in ? twN(Q, k, lq) : make_float2(1.0f, 0.0f);
+        wm[u] = in ? twN(Q, M - k, lq) : make_float2(1.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < PB; ++u) {
+        const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+        if (idx < tot2) {
+          const int p = idx % h;
+          const uint32_t k2 = (uint32_t)(idx / h);
+          const uint32_t k = kb + (uint32_t)p + M1 * k2;
+          const uint32_t mk = M - k;
+          const float2 zk = sm[k2 * S + p];
+          const float2 zm = sm[(M2 - 1 - k2) * S + h + p];
+          const float pk = post_power(zk, zm, wk[u]);
+          const float pm = post_power(zm, zk, wm[u]);
+          out[k] = pk;
+          out[mk] = pm;
+          acc += (double)pk + (double)pm;
+        }
+      }
     }
   }
   __shared__ double red[32];

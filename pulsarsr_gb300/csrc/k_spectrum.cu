@@ -92,23 +92,38 @@ __global__ void __launch_bounds__(SC_G)
   const long long b0 = (long long)blockIdx.x * SC_G;
   const long long c_first = b0 - 2;  // chunk index of local chunk 0
   const long long last_chunk = (long long)((plen - 1) / 64);
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (uint32_t i = 0; i < npsum; ++i) s += psum[trial * npsum + i];
-    floor_s = (float)(s / (double)plen * 1e-6);
-  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {  // floor: mean of the raw power from the FFT's partial sums
+    double s = 0.0;
+    for (uint32_t i = lane; i < npsum; i += 32) s += psum[trial * npsum + i];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) floor_s = (float)(s / (double)plen * 1e-6);
+  }
+  // Stage the bins of all chunks (coalesced, 16 loads in flight per thread);
+  // out-of-range chunks and bin 0 hold the sentinel 0xffffffff.
+  constexpr int NV = SC_CH * 64;
+  const long long e_first = c_first * 64;
+  for (int base = 0; base < NV; base += 16 * SC_G) {
+    uint32_t v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int i = base + u * SC_G + (int)threadIdx.x;
+      const long long e = e_first + i;
+      v[u] = (i < NV && e >= 1 && e < (long long)plen) ? fbits(raw[e]) : 0xffffffffu;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int i = base + u * SC_G + (int)threadIdx.x;
+      if (i < NV) ch[(i >> 6) * SC_STRIDE + (i & 63)] = v[u];
+    }
+  }
+  __syncthreads();
   for (int ci = warp; ci < SC_CH; ci += SC_G / 32) {
     const long long c = c_first + ci;
-    uint32_t x0 = 0xffffffffu, x1 = 0xffffffffu;
     int n = 0;
-    if (c >= 0 && c <= last_chunk) {  // out-of-range chunks stay all-sentinel
-      const long long base = c * 64;
-      const long long e0 = base + lane, e1 = base + lane + 32;
-      if (e0 < (long long)plen && e0 >= 1) x0 = fbits(raw[e0]);
-      if (e1 < (long long)plen) x1 = fbits(raw[e1]);
-      n = (int)min(64ll, (long long)plen - base) - (c == 0 ? 1 : 0);
-    }
+    if (c >= 0 && c <= last_chunk)
+      n = (int)min(64ll, (long long)plen - c * 64) - (c == 0 ? 1 : 0);
+    uint32_t x0 = ch[ci * SC_STRIDE + lane], x1 = ch[ci * SC_STRIDE + lane + 32];
     warp_sort64(x0, x1);
     ch[ci * SC_STRIDE + lane] = x0;
     ch[ci * SC_STRIDE + lane + 32] = x1;
@@ -239,36 +254,6 @@ __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64
   a.raw[trial * a.raw_cap + slot] = c;
 }
 
-// All harmonic levels h >= 2 of one bin whose fundamental passes the gate:
-// one parabolic offset, positions (k+off)*j computed once, cumulative f64
-// sums in j order (the reference's per-h sums are the same prefix sums).
-__device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, const float *sc,
-                          uint64_t k) {
-  int hmax = 0;
-#pragma unroll
-  for (int hi = 1; hi < 5; ++hi)
-    if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
-  if (hmax == 0) return;
-  const double off = offset_at(raw, k);
-  const double kf = __dadd_rn((double)k, off);
-  double sum = -0.0;
-  int j = 1;
-  for (int hi = 1; hi <= hmax; ++hi) {
-    const int h = 1 << hi;
-    for (; j <= h; ++j) {
-      uint64_t idx = (uint64_t)round(__dmul_rn(kf, (double)j));
-      if (idx > a.plen - 1) idx = a.plen - 1;
-      sum = __dadd_rn(sum, (double)pw(a, raw, sc, idx));
-    }
-    const double s = inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
-    if (s >= a.threshold) {
-      const double sm = score_at(a, raw, sc, k - 1, hi);
-      const double sp = score_at(a, raw, sc, k + 1, hi);
-      if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
-    }
-  }
-}
-
 constexpr int HM_NT = 256;
 constexpr int HM_KPT = 4;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
 
@@ -305,7 +290,40 @@ __global__ void __launch_bounds__(HM_NT) k_harmonic(HarmArgs a) {
       if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
     }
   }
-  for (int i = threadIdx.x; i < n2; i += blockDim.x) harm_item(a, trial, raw, sc, kb + q2[i]);
+  // One warp per gated bin: lane j-1 gathers harmonic j; every lane then adds
+  // the gathered values in j order (identical f64 sums on all lanes).
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int it = warp; it < n2; it += HM_NT / 32) {
+    const uint64_t k = kb + q2[it];
+    int hmax = 0;
+#pragma unroll
+    for (int hi = 1; hi < 5; ++hi)
+      if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
+    if (hmax == 0) continue;  // uniform across the warp
+    double off = 0.0;
+    if (lane == 0) off = offset_at(raw, k);
+    off = __shfl_sync(0xffffffffu, off, 0);
+    const double kf = __dadd_rn((double)k, off);
+    const int H = 1 << hmax;
+    double v = 0.0;
+    if (lane < H) {
+      uint64_t idx = (uint64_t)round(__dmul_rn(kf, (double)(lane + 1)));
+      if (idx > a.plen - 1) idx = a.plen - 1;
+      v = (double)pw(a, raw, sc, idx);
+    }
+    double sum = -0.0;
+    int j = 0;
+    for (int hi = 1; hi <= hmax; ++hi) {
+      const int h = 1 << hi;
+      for (; j < h; ++j) sum = __dadd_rn(sum, __shfl_sync(0xffffffffu, v, j));
+      const double s = inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
+      if (lane == 0 && s >= a.threshold) {
+        const double sm = score_at(a, raw, sc, k - 1, hi);
+        const double sp = score_at(a, raw, sc, k + 1, hi);
+        if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
+      }
+    }
+  }
 }
 
 // Orderable key: score descending, then (h, k) ascending = the reference's

@@ -159,67 +159,73 @@ __device__ __forceinline__ float as_f32(T v) {
   return (float)v;
 }
 
-// Element e of a 16-byte vector of T.
-template <class T>
-__device__ __forceinline__ float vec_elem(const uint4 &w, int e) {
-  const uint32_t words[4] = {w.x, w.y, w.z, w.w};
-  if constexpr (sizeof(T) == 1) return (float)((words[e >> 2] >> (8 * (e & 3))) & 255u);
-  else if constexpr (sizeof(T) == 2) return (float)((words[e >> 1] >> (16 * (e & 1))) & 0xffffu);
-  else return __uint_as_float(words[e]);
-}
+// Channel means and variances (rfi/src/lib.rs:35-43), in reference order,
+// with the per-sample work taken off the sequential chain: one
+// CTA per channel; warps 1.. write the f32 terms of the next segment into a
+// shared-memory double buffer while thread 0 adds the current segment's terms
+// in reference order.  The chain then costs one FADD latency per sample.
+constexpr int PC_NT = 256;
+constexpr int PC_SEG = 2048;
 
-// Visit row[0..ns) strictly in order, keeping SEQ_DEPTH 16-byte loads in
-// flight ahead of the (latency-bound) sequential consumer f.
-constexpr int SEQ_DEPTH = 8;
-template <class T, class F>
-__device__ __forceinline__ void seq_visit(const T *row, uint64_t ns, F &&f) {
-  constexpr int E = 16 / (int)sizeof(T);
-  const uint4 *v = reinterpret_cast<const uint4 *>(row);  // rows are 64-byte aligned
-  const uint64_t nv = ns / E;
-  uint4 nxt[SEQ_DEPTH];
-#pragma unroll
-  for (int i = 0; i < SEQ_DEPTH; ++i) nxt[i] = (uint64_t)i < nv ? v[i] : make_uint4(0, 0, 0, 0);
-  for (uint64_t q = 0; q < nv; q += SEQ_DEPTH) {
-    uint4 cur[SEQ_DEPTH];
-#pragma unroll
-    for (int i = 0; i < SEQ_DEPTH; ++i) {
-      cur[i] = nxt[i];
-      if (q + SEQ_DEPTH + i < nv) nxt[i] = v[q + SEQ_DEPTH + i];
-    }
-#pragma unroll
-    for (int i = 0; i < SEQ_DEPTH; ++i)
-      if (q + i < nv)
-#pragma unroll
-        for (int e = 0; e < E; ++e) f(vec_elem<T>(cur[i], e));
-  }
-  for (uint64_t t = nv * E; t < ns; ++t) f(as_f32(row[t]));
-}
-
-// Channel means and variances (rfi/src/lib.rs:35-43): one thread per channel
-// in reference order.  The mean's sum is taken from the exact integer total
-// when every partial sum is an integer <= 2^24 (identical f32 result).
-template <class T>
-__global__ void k_chan_mean_var(const T *__restrict__ s, uint64_t ns, uint64_t ld,
-                                uint64_t nch, const unsigned long long *__restrict__ tot,
-                                float *__restrict__ means, float *__restrict__ vars) {
-  uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nch) return;
-  const T *row = s + c * ld;
-  float sum;
-  if (sizeof(T) < 4 && tot[c] <= (1ull << 24)) {
-    sum = (float)tot[c];
-  } else {
-    sum = -0.0f;
-    seq_visit(row, ns, [&](float x) { sum = __fadd_rn(sum, x); });
-  }
-  const float m = __fdiv_rn(sum, (float)ns);
+template <class T, class Term>
+__device__ float pc_sequential_sum(const T *row, uint64_t ns, float *buf, Term term) {
+  const uint64_t nseg = (ns + PC_SEG - 1) / PC_SEG;
   float acc = -0.0f;
-  seq_visit(row, ns, [&](float x) {
+  auto produce = [&](uint64_t seg, float *dst) {
+    const uint64_t t0 = seg * PC_SEG;
+    const int cnt = (int)min((uint64_t)PC_SEG, ns - t0);
+    for (int i = (int)threadIdx.x - 32; i < cnt; i += PC_NT - 32) dst[i] = term(as_f32(row[t0 + i]));
+  };
+  if (threadIdx.x >= 32) produce(0, buf);
+  __syncthreads();
+  for (uint64_t seg = 0; seg < nseg; ++seg) {
+    float *cur = buf + (seg & 1) * PC_SEG;
+    if (threadIdx.x >= 32) {
+      if (seg + 1 < nseg) produce(seg + 1, buf + ((seg + 1) & 1) * PC_SEG);
+    } else if (threadIdx.x == 0) {
+      const int cnt = (int)min((uint64_t)PC_SEG, ns - seg * PC_SEG);
+      const float4 *c4 = reinterpret_cast<const float4 *>(cur);
+      int i = 0;
+#pragma unroll 8
+      for (; i + 4 <= cnt; i += 4) {
+        const float4 q = c4[i >> 2];
+        acc = __fadd_rn(acc, q.x);
+        acc = __fadd_rn(acc, q.y);
+        acc = __fadd_rn(acc, q.z);
+        acc = __fadd_rn(acc, q.w);
+      }
+      for (; i < cnt; ++i) acc = __fadd_rn(acc, cur[i]);
+    }
+    __syncthreads();
+  }
+  return acc;  // valid in thread 0
+}
+
+template <class T>
+__global__ void __launch_bounds__(PC_NT)
+    k_chan_mean_var_pc(const T *__restrict__ s, uint64_t ns, uint64_t ld,
+                       const unsigned long long *__restrict__ tot, float *__restrict__ means,
+                       float *__restrict__ vars) {
+  __shared__ __align__(16) float buf[2 * PC_SEG];
+  __shared__ float mean_s;
+  const uint64_t c = blockIdx.x;
+  const T *row = s + c * ld;
+  if (sizeof(T) < 4 && tot[c] <= (1ull << 24)) {
+    if (threadIdx.x == 0) mean_s = __fdiv_rn((float)tot[c], (float)ns);
+  } else {
+    const float sum = pc_sequential_sum(row, ns, buf, [](float x) { return x; });
+    if (threadIdx.x == 0) mean_s = __fdiv_rn(sum, (float)ns);
+  }
+  __syncthreads();
+  const float m = mean_s;
+  const float acc = pc_sequential_sum(row, ns, buf, [m](float x) {
     const float d = __fsub_rn(x, m);
-    acc = __fadd_rn(acc, __fmul_rn(d, d));
+    return __fmul_rn(d, d);
   });
-  means[c] = m;
-  vars[c] = __fdiv_rn(acc, (float)ns);
+  if (threadIdx.x == 0) {
+    means[c] = m;
+    vars[c] = __fdiv_rn(acc, (float)ns);
+  }
 }
 
 // Per-(channel, block) sequential f32 sums (rfi/src/lib.rs:62-64).
@@ -378,8 +384,8 @@ static int rfi_enqueue_t(DeviceObs &o, uint64_t bs, float thr, RfiWork &w, cudaS
     dim3 g((unsigned)std::min<uint64_t>((ns + 255) / 256, 64), (unsigned)nch);
     k_chan_total<T><<<g, 256, 0, st>>>(s, ns, o.ld, tot);
   }
-  k_chan_mean_var<T><<<(unsigned)((nch + 31) / 32), 32, 0, st>>>(
-      s, ns, o.ld, nch, tot, w.means.as<float>(), w.vars.as<float>());
+  k_chan_mean_var_pc<T><<<(unsigned)nch, PC_NT, 0, st>>>(s, ns, o.ld, tot, w.means.as<float>(),
+                                                        w.vars.as<float>());
   k_block_sums<T><<<(unsigned)((nch * blocks_n + 127) / 128), 128, 0, st>>>(
       s, ns, o.ld, nch, bs, blocks_n, w.bsum.as<float>());
   k_chan_median<T><<<(unsigned)nch, 512, 0, st>>>(s, ns, o.ld, w.med.as<float>());
