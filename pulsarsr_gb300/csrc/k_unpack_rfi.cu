@@ -171,10 +171,22 @@ template <class T, class Term>
 __device__ float pc_sequential_sum(const T *row, uint64_t ns, float *buf, Term term) {
   const uint64_t nseg = (ns + PC_SEG - 1) / PC_SEG;
   float acc = -0.0f;
+  constexpr int NP = PC_NT - 32;                 // producer threads
+  constexpr int NI = (PC_SEG + NP - 1) / NP;     // samples per producer thread
   auto produce = [&](uint64_t seg, float *dst) {
     const uint64_t t0 = seg * PC_SEG;
     const int cnt = (int)min((uint64_t)PC_SEG, ns - t0);
-    for (int i = (int)threadIdx.x - 32; i < cnt; i += PC_NT - 32) dst[i] = term(as_f32(row[t0 + i]));
+    float v[NI];
+#pragma unroll
+    for (int u = 0; u < NI; ++u) {  // all loads issued before any is used
+      const int i = (int)threadIdx.x - 32 + u * NP;
+      v[u] = i < cnt ? as_f32(row[t0 + i]) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < NI; ++u) {
+      const int i = (int)threadIdx.x - 32 + u * NP;
+      if (i < cnt) dst[i] = term(v[u]);
+    }
   };
   if (threadIdx.x >= 32) produce(0, buf);
   __syncthreads();
