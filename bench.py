@@ -167,6 +167,8 @@ def run_ours(args):
     rt = cudart()
     rt.cudaSetDevice(C.c_int(local))
     obs, raw, trials, discovery = workload(args.config)
+    if args.trials:
+        trials = trials[:args.trials]
     hdr = fbank.parse_header(raw)
     payload = np.frombuffer(raw, dtype=np.uint8)[hdr.data_offset:].copy()
     # pinned host payload for the e2e leg
@@ -350,6 +352,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--trials", type=int, default=0,
+                    help="search only the first N trial DMs (small profiling case)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

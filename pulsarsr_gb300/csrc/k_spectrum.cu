@@ -5,9 +5,9 @@
 //   scale_b = max(max(median(raw[lo..hi]) / ln2, floor), 1e-20),
 //   lo = max(64b-128, 1), hi = min(64b+192, len), floor = 1e-6 * mean(raw).
 // The median is exact: each 64-bin chunk is sorted once per CTA (warp bitonic
-// network), and the window's rank-(cnt/2) element is found by bisection over
-// the 32-bit patterns (non-negative floats order like their bits) counting
-// with binary searches in the <= 5 sorted chunks.  Normalised power is never
+// network; non-negative floats order like their bit patterns), elements
+// provably below the window's rank-(cnt/2) element are skipped with binary
+// searches, and a 5-way merge walk over the sorted chunks finds it.  Normalised power is never
 // stored: pw(i) = raw[i] / scale[i>>6], zero for i == 0 and birdie bins.
 //
 // Harmonic sums follow the reference's f64 arithmetic exactly.  The f64 work
@@ -85,13 +85,11 @@ __global__ void __launch_bounds__(SC_G)
              const double *__restrict__ psum, uint32_t npsum, float *__restrict__ scale,
              uint64_t lds, uint64_t nblocks) {
   __shared__ uint32_t ch[SC_CH * SC_STRIDE];
-  __shared__ int cnt[SC_CH];
   __shared__ float floor_s;
   const uint64_t trial = blockIdx.y;
   const float *raw = power + trial * ldp;
   const long long b0 = (long long)blockIdx.x * SC_G;
   const long long c_first = b0 - 2;  // chunk index of local chunk 0
-  const long long last_chunk = (long long)((plen - 1) / 64);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {  // floor: mean of the raw power from the FFT's partial sums
     double s = 0.0;
@@ -119,15 +117,10 @@ __global__ void __launch_bounds__(SC_G)
   }
   __syncthreads();
   for (int ci = warp; ci < SC_CH; ci += SC_G / 32) {
-    const long long c = c_first + ci;
-    int n = 0;
-    if (c >= 0 && c <= last_chunk)
-      n = (int)min(64ll, (long long)plen - c * 64) - (c == 0 ? 1 : 0);
     uint32_t x0 = ch[ci * SC_STRIDE + lane], x1 = ch[ci * SC_STRIDE + lane + 32];
     warp_sort64(x0, x1);
     ch[ci * SC_STRIDE + lane] = x0;
     ch[ci * SC_STRIDE + lane + 32] = x1;
-    if (lane == 0) cnt[ci] = n;
   }
   __syncthreads();
   const long long b = b0 + threadIdx.x;
@@ -136,27 +129,48 @@ __global__ void __launch_bounds__(SC_G)
   const long long lo = max(center - 128, 1ll);
   const long long hi = min(center + 192, (long long)plen);
   const int r = (int)(hi - lo) / 2;
-  // The window is local chunks threadIdx.x .. threadIdx.x + 4 (chunks b-2..b+2).
+  // The window is local chunks threadIdx.x .. threadIdx.x + 4 (chunks b-2..b+2),
+  // each sorted and padded with sentinels above every value.
   const uint32_t *w = ch + threadIdx.x * SC_STRIDE;
-  uint32_t lo_k = 0xffffffffu, hi_k = 0;
+  // Lower bound: y = min_i A_i[r/5].  Every chunk holds at most r/5 elements
+  // below y, so at most r elements of the window are below y and the
+  // rank-r element is >= y; those elements are skipped.
+  const int q = min(r / 5, 63);
+  uint32_t y = 0xffffffffu;
+#pragma unroll
+  for (int d = 0; d < 5; ++d) y = min(y, w[d * SC_STRIDE + q]);
+  int p[5];
+  int skipped = 0;
 #pragma unroll
   for (int d = 0; d < 5; ++d) {
-    const int n = cnt[threadIdx.x + d];
-    if (n > 0) {
-      lo_k = min(lo_k, w[d * SC_STRIDE]);
-      hi_k = max(hi_k, w[d * SC_STRIDE + n - 1]);
-    }
+    p[d] = y == 0u ? 0 : count_le64(w + d * SC_STRIDE, y - 1u);  // elements < y
+    skipped += p[d];
   }
-  // smallest key K with count(<= K) > r; it is an element of the window
-  while (lo_k < hi_k) {
-    const uint32_t mid = lo_k + ((hi_k - lo_k) >> 1);
-    int c_le = 0;
+  // 5-way merge walk over the rest: advance the smallest head r - skipped
+  // times; the smallest head is then the rank-r element.
+  uint32_t hd[5];
 #pragma unroll
-    for (int d = 0; d < 5; ++d) c_le += count_le64(w + d * SC_STRIDE, mid);
-    if (c_le > r) hi_k = mid;
-    else lo_k = mid + 1;
+  for (int d = 0; d < 5; ++d) hd[d] = w[d * SC_STRIDE + p[d]];
+  for (int step = skipped; step < r; ++step) {
+    uint32_t m = hd[0];
+    int am = 0;
+#pragma unroll
+    for (int d = 1; d < 5; ++d)
+      if (hd[d] < m) {
+        m = hd[d];
+        am = d;
+      }
+#pragma unroll
+    for (int d = 0; d < 5; ++d)
+      if (d == am) {
+        ++p[d];
+        hd[d] = p[d] < 64 ? w[d * SC_STRIDE + p[d]] : 0xffffffffu;
+      }
   }
-  const float med = __uint_as_float(lo_k);
+  uint32_t med_k = hd[0];
+#pragma unroll
+  for (int d = 1; d < 5; ++d) med_k = min(med_k, hd[d]);
+  const float med = __uint_as_float(med_k);
   const float sc = fmaxf(fmaxf(__fdiv_rn(med, LN2F), floor_s), 1e-20f);
   scale[trial * lds + b] = sc;
 }
@@ -254,29 +268,102 @@ __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64
   a.raw[trial * a.raw_cap + slot] = c;
 }
 
-constexpr int HM_NT = 256;
-constexpr int HM_KPT = 4;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
+constexpr int HM_NT = 512;
+constexpr int HM_KPT = 16;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
+constexpr int HM_BINS = HM_NT * HM_KPT;
+
+// round(RN(kf * j)) for a positive normal double kf and 1 <= j <= 16, in
+// exact 64-bit integer arithmetic: kf = m * 2^E (53-bit m), the product m*j
+// is exact in 57 bits, rounded to 53 bits (nearest, ties to even) as the FPU
+// would, then rounded to an integer half away from zero as f64::round does.
+// Bit-identical to (uint64_t)round(__dmul_rn(kf, (double)j)).
+__device__ __forceinline__ uint64_t round_mul(double kf, uint32_t j) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(kf);
+  const int E = (int)((bits >> 52) & 0x7ff) - 1075;
+  const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  unsigned long long q = m * (unsigned long long)j;
+  int F = E;
+  const int nb = 64 - __clzll((long long)q);
+  if (nb > 53) {
+    const int sh = nb - 53;
+    const unsigned long long rem = q & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    q >>= sh;
+    F += sh;
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+    if (q >> 53) {
+      q >>= 1;
+      ++F;
+    }
+  }
+  if (F >= 0) return q << F;
+  const int s = -F;
+  if (s >= 64) return 0;
+  const unsigned long long ip = q >> s, fr = q & ((1ull << s) - 1ull);
+  return ip + (fr >= (1ull << (s - 1)) ? 1ull : 0ull);
+}
+
+// All harmonic levels h >= 2 of one gated bin (pw(k) >= 4), one lane per
+// bin: the offset is computed once, the harmonic positions and gathers are
+// issued together, and the f64 sums accumulate in j order (the reference's
+// per-h sums are the same prefix sums).
+__device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, const float *sc,
+                          uint64_t k) {
+  int hmax = 0;
+#pragma unroll
+  for (int hi = 1; hi < 5; ++hi)
+    if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
+  if (hmax == 0) return;
+  const double kf = __dadd_rn((double)k, offset_at(raw, k));
+  const int H = 1 << hmax;
+  float v[16];
+#pragma unroll
+  for (int j = 1; j <= 16; ++j) {
+    float x = 0.0f;
+    if (j <= H) {
+      uint64_t idx = round_mul(kf, (uint32_t)j);
+      if (idx > a.plen - 1) idx = a.plen - 1;
+      x = pw(a, raw, sc, idx);
+    }
+    v[j - 1] = x;
+  }
+  double sum = -0.0;
+#pragma unroll
+  for (int hi = 1; hi < 5; ++hi) {
+    if (hi > hmax) break;
+    const int h = 1 << hi;
+    // harmonics j = h/2+1 .. h (v[j-1]); for h = 2 also j = 1
+#pragma unroll
+    for (int j = (hi == 1 ? 0 : h / 2); j < h; ++j) sum = __dadd_rn(sum, (double)v[j]);
+    const double s = inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
+    if (s >= a.threshold) {
+      const double sm = score_at(a, raw, sc, k - 1, hi);
+      const double sp = score_at(a, raw, sc, k + 1, hi);
+      if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
+    }
+  }
+}
 
 // Every bin is first tested with exact f32 gates: an h = 1 peak needs
 // max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value minus 1
 // reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and h >= 2
 // scores exist only where pw(k) >= 4.  The rare bins that pass are queued in
-// shared memory and evaluated with every lane busy.
-__global__ void __launch_bounds__(HM_NT) k_harmonic(HarmArgs a) {
-  __shared__ uint32_t q1[HM_NT * HM_KPT], q2[HM_NT * HM_KPT];
+// shared memory (a CTA covers 8192 bins, so the queue fills whole warps) and
+// then evaluated one bin per lane.
+__global__ void __launch_bounds__(HM_NT, 1) k_harmonic(HarmArgs a) {
+  __shared__ uint16_t q1[HM_BINS], q2[HM_BINS];
   __shared__ int n1, n2;
   const uint64_t trial = blockIdx.y;
   const float *raw = a.power + trial * a.ldp;
   const float *sc = a.scale + trial * a.lds;
   if (threadIdx.x == 0) n1 = n2 = 0;
   __syncthreads();
-  const uint64_t kb = a.first + 1 + (uint64_t)blockIdx.x * HM_NT * HM_KPT;
-#pragma unroll
+  const uint64_t kb = a.first + 1 + (uint64_t)blockIdx.x * HM_BINS;
+#pragma unroll 4
   for (int i = 0; i < HM_KPT; ++i) {
     const uint64_t k = kb + (uint64_t)i * HM_NT + threadIdx.x;
     if (k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
     const float p0 = pw(a, raw, sc, k), p1 = pw(a, raw, sc, k + 1);
-    const uint32_t rel = (uint32_t)(k - kb);
+    const uint16_t rel = (uint16_t)(k - kb);
     if (fmaxf(p0, p1) >= a.t1) q1[atomicAdd(&n1, 1)] = rel;
     if (p0 >= 4.0f) q2[atomicAdd(&n2, 1)] = rel;
   }
@@ -290,40 +377,7 @@ __global__ void __launch_bounds__(HM_NT) k_harmonic(HarmArgs a) {
       if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
     }
   }
-  // One warp per gated bin: lane j-1 gathers harmonic j; every lane then adds
-  // the gathered values in j order (identical f64 sums on all lanes).
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int it = warp; it < n2; it += HM_NT / 32) {
-    const uint64_t k = kb + q2[it];
-    int hmax = 0;
-#pragma unroll
-    for (int hi = 1; hi < 5; ++hi)
-      if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
-    if (hmax == 0) continue;  // uniform across the warp
-    double off = 0.0;
-    if (lane == 0) off = offset_at(raw, k);
-    off = __shfl_sync(0xffffffffu, off, 0);
-    const double kf = __dadd_rn((double)k, off);
-    const int H = 1 << hmax;
-    double v = 0.0;
-    if (lane < H) {
-      uint64_t idx = (uint64_t)round(__dmul_rn(kf, (double)(lane + 1)));
-      if (idx > a.plen - 1) idx = a.plen - 1;
-      v = (double)pw(a, raw, sc, idx);
-    }
-    double sum = -0.0;
-    int j = 0;
-    for (int hi = 1; hi <= hmax; ++hi) {
-      const int h = 1 << hi;
-      for (; j < h; ++j) sum = __dadd_rn(sum, __shfl_sync(0xffffffffu, v, j));
-      const double s = inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
-      if (lane == 0 && s >= a.threshold) {
-        const double sm = score_at(a, raw, sc, k - 1, hi);
-        const double sp = score_at(a, raw, sc, k + 1, hi);
-        if (s > sm && s >= sp) emit(a, trial, raw, k, hi, s);
-      }
-    }
-  }
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) harm_item(a, trial, raw, sc, kb + q2[i]);
 }
 
 // Orderable key: score descending, then (h, k) ascending = the reference's
