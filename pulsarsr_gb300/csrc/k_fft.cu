@@ -17,8 +17,10 @@
 //   internal twiddles W_R^(n2*k1).
 // A CTA transforms C columns held in shared memory as [position][C+1]
 // (padding keeps both the row-wise global loads and the Stockham accesses
-// free of bank conflicts).  All stages are in place: every thread loads its
-// butterflies' inputs, the block synchronises, then stores.
+// free of bank conflicts).  Every size is a template parameter, so all index
+// arithmetic reduces to shifts and masks; each thread owns exactly one
+// radix-16 butterfly per stage.  Stages are in place: every thread loads its
+// inputs, the block synchronises, then stores.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -29,7 +31,16 @@
 namespace psr {
 namespace {
 
-constexpr int LB = 16;  // loads in flight per thread when staging a tile
+constexpr int LB = 8;  // global loads in flight per thread when staging a tile
+
+__host__ __device__ constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
+__host__ __device__ constexpr int cols_for(int L) {
+  return L >= 8192 ? 1 : (8192 / L > 16 ? 16 : 8192 / L);
+}
+__host__ __device__ constexpr int threads_for(int L, int C) {
+  return ((L / 16) * C < 32 ? 32 : (L / 16) * C);
+}
+
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
   return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
 }
@@ -54,10 +65,10 @@ __device__ __forceinline__ float2 twN(const float2 *__restrict__ Q, uint32_t x, 
   }
 }
 
-__device__ __forceinline__ void dft2(float2 *v) {
-  float2 a = v[0], b = v[1];
-  v[0] = cadd(a, b);
-  v[1] = csub(a, b);
+__device__ __forceinline__ void dft2(float2 &v0, float2 &v1) {
+  const float2 a = v0, b = v1;
+  v0 = cadd(a, b);
+  v1 = csub(a, b);
 }
 __device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 &v3) {
   float2 a = cadd(v0, v2), b = csub(v0, v2);
@@ -68,14 +79,15 @@ __device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 
   v3 = csub(b, d);
 }
 // Wl[y] = W_L^y; W_R^y = Wl[y * L / R].
-__device__ __forceinline__ void dft8(float2 *v, const float2 *Wl, int L) {
+template <int L>
+__device__ __forceinline__ void dft8(float2 *v, const float2 *Wl) {
   float2 u[4][2];
 #pragma unroll
   for (int n2 = 0; n2 < 4; ++n2) {
-    float2 t[2] = {v[n2], v[n2 + 4]};
-    dft2(t);
-    u[n2][0] = t[0];
-    u[n2][1] = t[1];
+    float2 a = v[n2], b = v[n2 + 4];
+    dft2(a, b);
+    u[n2][0] = a;
+    u[n2][1] = b;
   }
 #pragma unroll
   for (int n2 = 1; n2 < 4; ++n2) u[n2][1] = cmul(u[n2][1], Wl[n2 * (L / 8)]);
@@ -89,7 +101,8 @@ __device__ __forceinline__ void dft8(float2 *v, const float2 *Wl, int L) {
     v[k1 + 6] = d;
   }
 }
-__device__ __forceinline__ void dft16(float2 *v, const float2 *Wl, int L) {
+template <int L>
+__device__ __forceinline__ void dft16(float2 *v, const float2 *Wl) {
   float2 u[4][4];
 #pragma unroll
   for (int n2 = 0; n2 < 4; ++n2) {
@@ -115,71 +128,74 @@ __device__ __forceinline__ void dft16(float2 *v, const float2 *Wl, int L) {
   }
 }
 
-template <int R>
-__device__ __forceinline__ void dftR(float2 *v, const float2 *Wl, int L) {
-  if constexpr (R == 2) dft2(v);
+template <int R, int L>
+__device__ __forceinline__ void dftR(float2 *v, const float2 *Wl) {
+  if constexpr (R == 2) dft2(v[0], v[1]);
   else if constexpr (R == 4) dft4(v[0], v[1], v[2], v[3]);
-  else if constexpr (R == 8) dft8(v, Wl, L);
-  else dft16(v, Wl, L);
+  else if constexpr (R == 8) dft8<L>(v, Wl);
+  else dft16<L>(v, Wl);
 }
 
-// One in-place Stockham stage on C columns of length L (stride S).
-template <int R>
-__device__ void stockham_stage(float2 *sm, int S, int C, int L, int Ns, const float2 *Wl) {
-  constexpr int BPT = 16 / R;  // butterflies per thread (nthreads >= L/16 * C)
-  const int nb = L / R;
-  const int total = nb * C;
+// One in-place Stockham stage (radix R, Ns = product of earlier radices) on
+// C columns of length L; NT threads, each owning 16/R butterflies.
+template <int R, int L, int C, int NT, int Ns>
+__device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
+  constexpr int S = C + 1;
+  constexpr int nb = L / R;
+  constexpr int total = nb * C;
+  constexpr int BPT = (total + NT - 1) / NT;
   float2 v[BPT][R];
-  int jj[BPT], cc[BPT];
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
-    const int w = threadIdx.x + i * blockDim.x;
-    jj[i] = -1;
-    if (w < total) {
+    const int w = (int)threadIdx.x + i * NT;
+    if (total % NT == 0 || w < total) {
       const int col = w % C, j = w / C;
-      jj[i] = j;
-      cc[i] = col;
 #pragma unroll
       for (int r = 0; r < R; ++r) v[i][r] = sm[(j + r * nb) * S + col];
-      const int k = j & (Ns - 1);
-      if (Ns > 1 && k != 0) {
-        const int step = L / (Ns * R);
+      if constexpr (Ns > 1) {
+        const int k = j % Ns;
+        if (k != 0) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[i][r] = cmul(v[i][r], Wl[r * k * step]);
+          for (int r = 1; r < R; ++r) v[i][r] = cmul(v[i][r], Wl[r * k * (L / (Ns * R))]);
+        }
       }
-      dftR<R>(v[i], Wl, L);
+      dftR<R, L>(v[i], Wl);
     }
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < BPT; ++i) {
-    if (jj[i] >= 0) {
-      const int j = jj[i], k = j & (Ns - 1);
-      const int base = (j / Ns) * Ns * R + k;
+    const int w = (int)threadIdx.x + i * NT;
+    if (total % NT == 0 || w < total) {
+      const int col = w % C, j = w / C;
+      const int base = (j / Ns) * Ns * R + j % Ns;
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[(base + r * Ns) * S + cc[i]] = v[i][r];
+      for (int r = 0; r < R; ++r) sm[(base + r * Ns) * S + col] = v[i][r];
     }
   }
   __syncthreads();
 }
 
-__device__ void subfft(float2 *sm, int S, int C, int L, const float2 *Wl) {
-  int q = 0;
-  while ((1 << q) < L) ++q;
-  int Ns = 1;
-  for (int s = 0; s < q / 4; ++s) {
-    stockham_stage<16>(sm, S, C, L, Ns, Wl);
-    Ns *= 16;
-  }
-  switch (q % 4) {
-    case 1: stockham_stage<2>(sm, S, C, L, Ns, Wl); break;
-    case 2: stockham_stage<4>(sm, S, C, L, Ns, Wl); break;
-    case 3: stockham_stage<8>(sm, S, C, L, Ns, Wl); break;
-    default: break;
+template <int L, int C, int NT, int s>
+__device__ __forceinline__ void stages16(float2 *sm, const float2 *Wl) {
+  if constexpr (s < ilog2(L) / 4) {
+    stage<16, L, C, NT, (1 << (4 * s))>(sm, Wl);
+    stages16<L, C, NT, s + 1>(sm, Wl);
   }
 }
 
-__device__ void build_wl(float2 *Wl, int L, uint32_t N, const float2 *Q, int lq) {
+template <int L, int C, int NT>
+__device__ __forceinline__ void subfft(float2 *sm, const float2 *Wl) {
+  constexpr int q = ilog2(L);
+  constexpr int NsLast = 1 << (4 * (q / 4));
+  stages16<L, C, NT, 0>(sm, Wl);
+  if constexpr (q % 4 == 1) stage<2, L, C, NT, NsLast>(sm, Wl);
+  else if constexpr (q % 4 == 2) stage<4, L, C, NT, NsLast>(sm, Wl);
+  else if constexpr (q % 4 == 3) stage<8, L, C, NT, NsLast>(sm, Wl);
+}
+
+template <int L>
+__device__ __forceinline__ void build_wl(float2 *Wl, uint32_t N, const float2 *Q, int lq) {
   const uint32_t stride = N / (uint32_t)L;
   for (int y = threadIdx.x; y < L; y += blockDim.x) Wl[y] = twN(Q, (uint32_t)y * stride, lq);
 }
@@ -212,85 +228,99 @@ __device__ __forceinline__ float trial_mean(const double *sums, uint64_t trial, 
   return (float)(sums[trial] / (double)len);
 }
 
-// Whole transform in one CTA per trial (M <= 4096).
-__global__ void __launch_bounds__(512) k_fft_small(const float *__restrict__ series, uint64_t lds, uint64_t len,
-                            const double *__restrict__ sums, const float2 *__restrict__ Q,
-                            int lq, uint32_t N, uint32_t M, float *__restrict__ power,
-                            uint64_t ldp, double *__restrict__ psum) {
-  extern __shared__ float2 dyn[];
-  float2 *Wl = dyn;          // M entries
-  float2 *sm = dyn + M;      // M x 2 (C = 1, S = 2)
-  const uint64_t trial = blockIdx.x;
-  const float *row = series + trial * lds;
-  const float mean = trial_mean(sums, trial, len);
-  build_wl(Wl, (int)M, N, Q, lq);
-  for (uint32_t n = threadIdx.x; n < M; n += blockDim.x) sm[n * 2] = load_z(row, len, n, mean);
-  __syncthreads();
-  subfft(sm, 2, 1, (int)M, Wl);
-  double acc = 0.0;
-  float *out = power + trial * ldp;
-  for (uint32_t k = threadIdx.x; k <= M; k += blockDim.x) {
-    const float p = post_power(sm[(k % M) * 2], sm[((M - k) % M) * 2], twN(Q, k, lq));
-    out[k] = p;
-    acc += (double)p;
-  }
-  __shared__ double red[32];
+template <int NT>
+__device__ __forceinline__ void block_sum_store(double acc, double *dst) {
+  __shared__ double red[NT / 32 > 0 ? NT / 32 : 1];
+#pragma unroll
   for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int w = 0; w < (int)((blockDim.x + 31) / 32); ++w) t += red[w];
-    psum[trial] = t;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) t += red[w];
+    *dst = t;
   }
 }
 
-// Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
-__global__ void __launch_bounds__(512) k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
-                            const double *__restrict__ sums, const float2 *__restrict__ Q,
-                            int lq, uint32_t N, uint32_t M, uint32_t M1, uint32_t M2, int C,
-                            float2 *__restrict__ work) {
+// Whole transform in one CTA per trial (M <= 4096).
+template <int M>
+__global__ void __launch_bounds__(threads_for(M, 1))
+    k_fft_small(const float *__restrict__ series, uint64_t lds, uint64_t len,
+                const double *__restrict__ sums, const float2 *__restrict__ Q, int lq,
+                uint32_t N, float *__restrict__ power, uint64_t ldp,
+                double *__restrict__ psum) {
+  constexpr int NT = threads_for(M, 1);
   extern __shared__ float2 dyn[];
-  float2 *Wl = dyn;        // M1 entries
-  float2 *sm = dyn + M1;   // M1 x (C+1)
-  const int S = C + 1;
+  float2 *Wl = dyn;      // M entries
+  float2 *sm = dyn + M;  // M x 2 (C = 1, S = 2)
+  const uint64_t trial = blockIdx.x;
+  const float *row = series + trial * lds;
+  const float mean = trial_mean(sums, trial, len);
+  build_wl<M>(Wl, N, Q, lq);
+  for (int n = threadIdx.x; n < M; n += NT) sm[n * 2] = load_z(row, len, (uint64_t)n, mean);
+  __syncthreads();
+  subfft<M, 1, NT>(sm, Wl);
+  double acc = 0.0;
+  float *out = power + trial * ldp;
+  for (int k = threadIdx.x; k <= M; k += NT) {
+    const float p = post_power(sm[(k % M) * 2], sm[((M - k) % M) * 2], twN(Q, (uint32_t)k, lq));
+    out[k] = p;
+    acc += (double)p;
+  }
+  block_sum_store<NT>(acc, psum + trial);
+}
+
+// Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
+template <int M1, int M2>
+__global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
+    k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
+                const double *__restrict__ sums, const float2 *__restrict__ Q, int lq,
+                uint32_t N, float2 *__restrict__ work) {
+  constexpr int C = cols_for(M1), S = C + 1, NT = threads_for(M1, C);
+  constexpr uint32_t M = (uint32_t)M1 * M2;
+  extern __shared__ float2 dyn[];
+  float2 *Wl = dyn;       // M1 entries
+  float2 *sm = dyn + M1;  // M1 x (C+1)
   const uint64_t trial = blockIdx.y;
   const uint32_t n2_0 = blockIdx.x * (uint32_t)C;
   const float *row = series + trial * lds;
   const float mean = trial_mean(sums, trial, len);
-  build_wl(Wl, (int)M1, N, Q, lq);
+  build_wl<M1>(Wl, N, Q, lq);
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
-  const int total = (int)M1 * C;
+  constexpr int total = M1 * C;
   // Batches of LB independent loads per thread keep many requests in flight.
-  for (int base = 0; base < total; base += LB * (int)blockDim.x) {
+#pragma unroll 1
+  for (int base = 0; base < total; base += LB * NT) {
     float2 v[LB];
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const int idx = base + u * NT + (int)threadIdx.x;
       const uint64_t n = (uint64_t)(idx / C) * M2 + n2_0 + (idx % C);
       v[u] = (idx < total && n < nz) ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
     }
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const int idx = base + u * NT + (int)threadIdx.x;
       if (idx < total) sm[(idx / C) * S + (idx % C)] = v[u];
     }
   }
   __syncthreads();
-  subfft(sm, S, C, (int)M1, Wl);
+  subfft<M1, C, NT>(sm, Wl);
   float2 *out = work + trial * (uint64_t)M;
   // Twiddle loads for LB outputs are issued before any is consumed.
-  for (int base = 0; base < total; base += LB * (int)blockDim.x) {
+#pragma unroll 1
+  for (int base = 0; base < total; base += LB * NT) {
     float2 w[LB];
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const int idx = base + u * NT + (int)threadIdx.x;
       const uint32_t e = (n2_0 + (uint32_t)(idx % C)) * (uint32_t)(idx / C);
       w[u] = (idx < total && e != 0) ? twN(Q, 2u * e, lq) : make_float2(1.0f, 0.0f);
     }
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+      const int idx = base + u * NT + (int)threadIdx.x;
       if (idx < total) {
         const int col = idx % C, k1 = idx / C;
         const uint32_t n2 = n2_0 + (uint32_t)col;
@@ -305,15 +335,17 @@ __global__ void __launch_bounds__(512) k_fft_pass1(const float *__restrict__ ser
 // Pass 2: row sub-FFTs of length M2 for a group of rows and their mirrors,
 // then the real post-processing and |X|^2.  Group 0 holds rows 0 and M1/2;
 // group g >= 1 holds rows kb..kb+h-1 (kb = 1 + (g-1)*H) and M1-kb..M1-kb-h+1.
-__global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q,
-                            int lq, uint32_t N, uint32_t M, uint32_t M1, uint32_t M2, int C,
-                            float *__restrict__ power, uint64_t ldp,
-                            double *__restrict__ psum, uint32_t ngroups) {
+// Unused columns of the last group are transformed but never read.
+template <int M1, int M2>
+__global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
+    k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q, int lq,
+                uint32_t N, float *__restrict__ power, uint64_t ldp, double *__restrict__ psum,
+                uint32_t ngroups) {
+  constexpr int C = cols_for(M2), S = C + 1, NT = threads_for(M2, C), H = C / 2;
+  constexpr uint32_t M = (uint32_t)M1 * M2;
   extern __shared__ float2 dyn[];
-  float2 *Wl = dyn;        // M2 entries
-  float2 *sm = dyn + M2;   // M2 x (C+1)
-  const int S = C + 1;
-  const int H = C / 2;
+  float2 *Wl = dyn;       // M2 entries
+  float2 *sm = dyn + M2;  // M2 x (C+1)
   const uint64_t trial = blockIdx.y;
   const uint32_t g = blockIdx.x;
   const float2 *in = work + trial * (uint64_t)M;
@@ -327,14 +359,15 @@ __global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ wo
     h = (int)min((uint32_t)H, (uint32_t)(M1 / 2 - kb));
   }
   const int ncols = 2 * h;
-  build_wl(Wl, (int)M2, N, Q, lq);
-  const int total = (int)M2 * ncols;
-  for (int base = 0; base < total; base += LB * (int)blockDim.x) {
+  build_wl<M2>(Wl, N, Q, lq);
+  const int total = M2 * ncols;
+#pragma unroll 1
+  for (int base = 0; base < total; base += LB * NT) {
     float2 v[LB];
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
-      const int pos = idx % (int)M2, ci = idx / (int)M2;
+      const int idx = base + u * NT + (int)threadIdx.x;
+      const int pos = idx % M2, ci = idx / M2;
       uint32_t k1;
       if (g == 0) k1 = ci == 0 ? 0 : M1 / 2;
       else k1 = ci < h ? kb + ci : M1 - (kb + (ci - h));
@@ -342,15 +375,15 @@ __global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ wo
     }
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
-      if (idx < total) sm[(idx % (int)M2) * S + idx / (int)M2] = v[u];
+      const int idx = base + u * NT + (int)threadIdx.x;
+      if (idx < total) sm[(idx % M2) * S + idx / M2] = v[u];
     }
   }
   __syncthreads();
-  subfft(sm, S, ncols, (int)M2, Wl);
+  subfft<M2, C, NT>(sm, Wl);
   double acc = 0.0;
   if (g == 0) {
-    for (uint32_t idx = threadIdx.x; idx < 2 * M2; idx += blockDim.x) {
+    for (uint32_t idx = threadIdx.x; idx < 2 * M2; idx += NT) {
       const uint32_t k2 = idx % M2, which = idx / M2;
       uint32_t k, mk2;
       if (which == 0) {
@@ -371,20 +404,21 @@ __global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ wo
     }
   } else {
     constexpr int PB = LB / 2;  // bins per batch (two twiddles each)
-    const int tot2 = (int)M2 * h;
-    for (int base = 0; base < tot2; base += PB * (int)blockDim.x) {
+    const int tot2 = M2 * h;
+#pragma unroll 1
+    for (int base = 0; base < tot2; base += PB * NT) {
       float2 wk[PB], wm[PB];
 #pragma unroll
       for (int u = 0; u < PB; ++u) {
-        const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+        const int idx = base + u * NT + (int)threadIdx.x;
         const uint32_t k = kb + (uint32_t)(idx % h) + M1 * (uint32_t)(idx / h);
-        const bool in = idx < tot2;
-        wk[u] = in ? twN(Q, k, lq) : make_float2(1.0f, 0.0f);
-        wm[u] = in ? twN(Q, M - k, lq) : make_float2(1.0f, 0.0f);
+        const bool inb = idx < tot2;
+        wk[u] = inb ? twN(Q, k, lq) : make_float2(1.0f, 0.0f);
+        wm[u] = inb ? twN(Q, M - k, lq) : make_float2(1.0f, 0.0f);
       }
 #pragma unroll
       for (int u = 0; u < PB; ++u) {
-        const int idx = base + u * (int)blockDim.x + (int)threadIdx.x;
+        const int idx = base + u * NT + (int)threadIdx.x;
         if (idx < tot2) {
           const int p = idx % h;
           const uint32_t k2 = (uint32_t)(idx / h);
@@ -401,37 +435,68 @@ __global__ void __launch_bounds__(512) k_fft_pass2(const float2 *__restrict__ wo
       }
     }
   }
-  __shared__ double red[32];
-  for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)((blockDim.x + 31) / 32); ++w) t += red[w];
-    psum[trial * ngroups + g] = t;
-  }
+  block_sum_store<NT>(acc, psum + trial * ngroups + g);
 }
 
-int cols_for(uint32_t L) {
-  int c = (int)(8192u / L);
-  if (c > 16) c = 16;
-  if (c < 1) c = 1;
-  return c;
+struct FftArgs {
+  const float *series;
+  uint64_t lds, len;
+  const double *sums;
+  const float2 *Q;
+  int lq;
+  uint32_t N;
+  uint64_t ntrials;
+  float2 *work;
+  float *power;
+  uint64_t ldp;
+  double *psum;
+  cudaStream_t st;
+};
+
+template <int M>
+int run_small(const FftArgs &a) {
+  const size_t smem = (size_t)M * sizeof(float2) * 3;
+  PSR_CUDA(cudaFuncSetAttribute(k_fft_small<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  k_fft_small<M><<<(unsigned)a.ntrials, threads_for(M, 1), smem, a.st>>>(
+      a.series, a.lds, a.len, a.sums, a.Q, a.lq, a.N, a.power, a.ldp, a.psum);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
 }
-int threads_for(uint32_t L, int C) {
-  int t = (int)(L / 16) * C;
-  if (t < 32) t = 32;
-  return ((t + 31) / 32) * 32;
+
+template <int M1, int M2>
+int run_four_step(const FftArgs &a) {
+  {
+    constexpr int C = cols_for(M1);
+    const size_t smem = (size_t)M1 * sizeof(float2) * (1 + C + 1);
+    PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    dim3 grid((unsigned)(M2 / C), (unsigned)a.ntrials);
+    k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(a.series, a.lds, a.len, a.sums,
+                                                                    a.Q, a.lq, a.N, a.work);
+    PSR_CUDA(cudaGetLastError());
+  }
+  {
+    constexpr int C = cols_for(M2);
+    const size_t smem = (size_t)M2 * sizeof(float2) * (1 + C + 1);
+    PSR_CUDA(cudaFuncSetAttribute(k_fft_pass2<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    const uint32_t ng = 1 + ((uint32_t)M1 / 2 - 1 + C / 2 - 1) / (C / 2);
+    dim3 grid(ng, (unsigned)a.ntrials);
+    k_fft_pass2<M1, M2><<<grid, threads_for(M2, C), smem, a.st>>>(a.work, a.Q, a.lq, a.N, a.power,
+                                                                    a.ldp, a.psum, ng);
+    PSR_CUDA(cudaGetLastError());
+  }
+  return PSR_OK;
 }
 
 }  // namespace
 
 uint64_t FftPlan::pass2_ctas() const {
   if (m <= 12) return 1;
-  const int C = cols_for((uint32_t)M2);
-  const uint32_t H = (uint32_t)C / 2;
-  const uint32_t rest = (uint32_t)M1 / 2 - 1;
-  return 1 + (rest + H - 1) / H;
+  const uint32_t C = (uint32_t)(M2 >= 8192 ? 1 : std::min<uint64_t>(16, 8192 / M2));
+  const uint32_t H = C / 2;
+  return 1 + ((uint32_t)M1 / 2 - 1 + H - 1) / H;
 }
 
 int FftPlan::init(uint64_t series_len, cudaStream_t st) {
@@ -470,44 +535,37 @@ int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
                         uint64_t ldp, double *d_psum, cudaStream_t st) {
   int lq = 0;
   while ((1ull << lq) < p.N / 4) ++lq;
-  const float2 *Q = p.Q.as<float2>();
-  if (p.m <= 12) {
-    const int thr = threads_for((uint32_t)p.M, 1);
-    const size_t smem = (size_t)p.M * sizeof(float2) * 3;
-    PSR_CUDA(cudaFuncSetAttribute(k_fft_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    k_fft_small<<<(unsigned)ntrials, thr, smem, st>>>(d_series, lds, p.len, d_sums, Q, lq,
-                                                     (uint32_t)p.N, (uint32_t)p.M, d_power,
-                                                     ldp, d_psum);
-    PSR_CUDA(cudaGetLastError());
-    return PSR_OK;
+  FftArgs a{d_series, lds,     p.len,   d_sums, p.Q.as<float2>(), lq, (uint32_t)p.N, ntrials,
+            d_work,   d_power, ldp,     d_psum, st};
+  switch (p.m) {
+    case 1: return run_small<2>(a);
+    case 2: return run_small<4>(a);
+    case 3: return run_small<8>(a);
+    case 4: return run_small<16>(a);
+    case 5: return run_small<32>(a);
+    case 6: return run_small<64>(a);
+    case 7: return run_small<128>(a);
+    case 8: return run_small<256>(a);
+    case 9: return run_small<512>(a);
+    case 10: return run_small<1024>(a);
+    case 11: return run_small<2048>(a);
+    case 12: return run_small<4096>(a);
+    case 13: return run_four_step<128, 64>(a);
+    case 14: return run_four_step<128, 128>(a);
+    case 15: return run_four_step<256, 128>(a);
+    case 16: return run_four_step<256, 256>(a);
+    case 17: return run_four_step<512, 256>(a);
+    case 18: return run_four_step<512, 512>(a);
+    case 19: return run_four_step<1024, 512>(a);
+    case 20: return run_four_step<1024, 1024>(a);
+    case 21: return run_four_step<2048, 1024>(a);
+    case 22: return run_four_step<2048, 2048>(a);
+    case 23: return run_four_step<4096, 2048>(a);
+    case 24: return run_four_step<4096, 4096>(a);
+    default:
+      set_error("periodicity: unsupported FFT size");
+      return PSR_EINVAL;
   }
-  {
-    const int C = cols_for((uint32_t)p.M1);
-    const int thr = threads_for((uint32_t)p.M1, C);
-    const size_t smem = (size_t)p.M1 * sizeof(float2) * (1 + C + 1);
-    PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    dim3 grid((unsigned)(p.M2 / C), (unsigned)ntrials);
-    k_fft_pass1<<<grid, thr, smem, st>>>(d_series, lds, p.len, d_sums, Q, lq, (uint32_t)p.N,
-                                         (uint32_t)p.M, (uint32_t)p.M1, (uint32_t)p.M2, C,
-                                         d_work);
-    PSR_CUDA(cudaGetLastError());
-  }
-  {
-    const int C = cols_for((uint32_t)p.M2);
-    const int thr = threads_for((uint32_t)p.M2, C);
-    const size_t smem = (size_t)p.M2 * sizeof(float2) * (1 + C + 1);
-    PSR_CUDA(cudaFuncSetAttribute(k_fft_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    const uint32_t ng = (uint32_t)p.pass2_ctas();
-    dim3 grid(ng, (unsigned)ntrials);
-    k_fft_pass2<<<grid, thr, smem, st>>>(d_work, Q, lq, (uint32_t)p.N, (uint32_t)p.M,
-                                         (uint32_t)p.M1, (uint32_t)p.M2, C, d_power, ldp,
-                                         d_psum, ng);
-    PSR_CUDA(cudaGetLastError());
-  }
-  return PSR_OK;
 }
 
 }  // namespace psr
