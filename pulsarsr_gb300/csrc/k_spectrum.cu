@@ -4,8 +4,9 @@
 // Normalisation: every 64-bin block b is divided by
 //   scale_b = max(max(median(raw[lo..hi]) / ln2, floor), 1e-20),
 //   lo = max(64b-128, 1), hi = min(64b+192, len), floor = 1e-6 * mean(raw).
-// The median is exact: each 64-bin chunk is sorted once per CTA (warp bitonic
-// network; non-negative floats order like their bit patterns), elements
+// The median is exact: each 64-bin chunk is sorted once per CTA (a register
+// bitonic network per thread; non-negative floats order like their bit
+// patterns), elements
 // provably below the window's rank-(cnt/2) element are skipped with binary
 // searches, and a 5-way merge walk over the sorted chunks finds it.  Normalised power is never
 // stored: pw(i) = raw[i] / scale[i>>6], zero for i == 0 and birdie bins.
@@ -25,8 +26,9 @@
 namespace psr {
 namespace {
 
-constexpr int SC_G = 128;                // blocks per CTA (one per thread)
-constexpr int SC_CH = SC_G + 4;          // chunks staged per CTA
+constexpr int SC_NT = 128;               // threads per CTA, one chunk sort each
+constexpr int SC_CH = SC_NT;             // chunks staged per CTA
+constexpr int SC_G = SC_CH - 4;          // blocks per CTA (chunks b-2 .. b+2 each)
 constexpr float LN2F = 0.693147180559945309f;
 
 __device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
@@ -44,43 +46,11 @@ __device__ __forceinline__ int count_le64(const uint32_t *a, uint32_t key) {
   return pos;
 }
 
-// Sort 64 keys held two per lane (index lane and lane+32) ascending.
-__device__ __forceinline__ void warp_sort64(uint32_t &x0, uint32_t &x1) {
-  const int lane = threadIdx.x & 31;
-  // Element index e = lane + 32*r; bitonic network over e in [0, 64).
-  for (int k = 2; k <= 64; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      if (j == 32) {
-        // partners are x0 <-> x1 of the same lane (e and e+32)
-        const bool up = ((lane & k) == 0);  // e & k with k == 64: always 0 -> ascending
-        uint32_t a = x0, b = x1;
-        bool sw = up ? (a > b) : (a < b);
-        if (sw) {
-          x0 = b;
-          x1 = a;
-        }
-      } else {
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          uint32_t v = r ? x1 : x0;
-          const int e = lane + 32 * r;
-          uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
-          const bool up = ((e & k) == 0);
-          const bool lower = ((e & j) == 0);
-          uint32_t nv = (lower == up) ? min(v, o) : max(v, o);
-          if (r) x1 = nv;
-          else x0 = nv;
-        }
-      }
-    }
-  }
-}
-
 // Chunks are stored with a 65-word stride so that threads probing the same
 // index of different chunks hit different banks.
 constexpr int SC_STRIDE = 65;
 
-__global__ void __launch_bounds__(SC_G)
+__global__ void __launch_bounds__(SC_NT)
     k_scales(const float *__restrict__ power, uint64_t ldp, uint64_t plen,
              const double *__restrict__ psum, uint32_t npsum, float *__restrict__ scale,
              uint64_t lds, uint64_t nblocks) {
@@ -101,30 +71,53 @@ __global__ void __launch_bounds__(SC_G)
   // out-of-range chunks and bin 0 hold the sentinel 0xffffffff.
   constexpr int NV = SC_CH * 64;
   const long long e_first = c_first * 64;
-  for (int base = 0; base < NV; base += 16 * SC_G) {
+  for (int base = 0; base < NV; base += 16 * SC_NT) {
     uint32_t v[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      const int i = base + u * SC_G + (int)threadIdx.x;
+      const int i = base + u * SC_NT + (int)threadIdx.x;
       const long long e = e_first + i;
       v[u] = (i < NV && e >= 1 && e < (long long)plen) ? fbits(raw[e]) : 0xffffffffu;
     }
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      const int i = base + u * SC_G + (int)threadIdx.x;
+      const int i = base + u * SC_NT + (int)threadIdx.x;
       if (i < NV) ch[(i >> 6) * SC_STRIDE + (i & 63)] = v[u];
     }
   }
   __syncthreads();
-  for (int ci = warp; ci < SC_CH; ci += SC_G / 32) {
-    uint32_t x0 = ch[ci * SC_STRIDE + lane], x1 = ch[ci * SC_STRIDE + lane + 32];
-    warp_sort64(x0, x1);
-    ch[ci * SC_STRIDE + lane] = x0;
-    ch[ci * SC_STRIDE + lane + 32] = x1;
+  {
+    // Thread t sorts chunk t in registers (fully unrolled bitonic network of
+    // 672 compare-exchanges: no shuffles, static register indices).  The
+    // stride-65 layout makes these row reads bank-conflict free.
+    uint32_t x[64];
+    uint32_t *row = ch + threadIdx.x * SC_STRIDE;
+#pragma unroll
+    for (int i = 0; i < 64; ++i) x[i] = row[i];
+#pragma unroll
+    for (int k = 2; k <= 64; k <<= 1)
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+          const int l = i ^ j;
+          if (l > i) {
+            const uint32_t a = x[i], b = x[l];
+            if ((i & k) == 0) {
+              x[i] = min(a, b);
+              x[l] = max(a, b);
+            } else {
+              x[i] = max(a, b);
+              x[l] = min(a, b);
+            }
+          }
+        }
+#pragma unroll
+    for (int i = 0; i < 64; ++i) row[i] = x[i];
   }
   __syncthreads();
   const long long b = b0 + threadIdx.x;
-  if (b >= (long long)nblocks) return;
+  if (threadIdx.x >= SC_G || b >= (long long)nblocks) return;
   const long long center = b * 64;
   const long long lo = max(center - 128, 1ll);
   const long long hi = min(center + 192, (long long)plen);
@@ -268,8 +261,8 @@ __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64
   a.raw[trial * a.raw_cap + slot] = c;
 }
 
-constexpr int HM_NT = 512;
-constexpr int HM_KPT = 16;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
+constexpr int HM_NT = 256;
+constexpr int HM_KPT = 8;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
 constexpr int HM_BINS = HM_NT * HM_KPT;
 
 // round(RN(kf * j)) for a positive normal double kf and 1 <= j <= 16, in
@@ -347,9 +340,9 @@ __device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, c
 // max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value minus 1
 // reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and h >= 2
 // scores exist only where pw(k) >= 4.  The rare bins that pass are queued in
-// shared memory (a CTA covers 8192 bins, so the queue fills whole warps) and
+// shared memory (a CTA covers 2048 bins, so the queue fills a warp) and
 // then evaluated one bin per lane.
-__global__ void __launch_bounds__(HM_NT, 1) k_harmonic(HarmArgs a) {
+__global__ void __launch_bounds__(HM_NT, 2) k_harmonic(HarmArgs a) {
   __shared__ uint16_t q1[HM_BINS], q2[HM_BINS];
   __shared__ int n1, n2;
   const uint64_t trial = blockIdx.y;
@@ -358,7 +351,7 @@ __global__ void __launch_bounds__(HM_NT, 1) k_harmonic(HarmArgs a) {
   if (threadIdx.x == 0) n1 = n2 = 0;
   __syncthreads();
   const uint64_t kb = a.first + 1 + (uint64_t)blockIdx.x * HM_BINS;
-#pragma unroll 4
+#pragma unroll
   for (int i = 0; i < HM_KPT; ++i) {
     const uint64_t k = kb + (uint64_t)i * HM_NT + threadIdx.x;
     if (k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
@@ -602,7 +595,7 @@ int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_pow
   const uint64_t nblocks = (plen + 63) / 64;
   {
     dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
-    k_scales<<<grid, SC_G, 0, st>>>(d_power, ldp, plen, d_psum, npsum, w.scale.as<float>(),
+    k_scales<<<grid, SC_NT, 0, st>>>(d_power, ldp, plen, d_psum, npsum, w.scale.as<float>(),
                                     w.lds, nblocks);
     PSR_CUDA(cudaGetLastError());
   }
