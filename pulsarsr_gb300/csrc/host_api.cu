@@ -521,18 +521,19 @@ int dedisperse_delays(const DeviceObs &o, const uint64_t *d, int64_t length, flo
   std::vector<uint32_t> tab(o.nch);
   for (uint64_t c = 0; c < o.nch; ++c) tab[c] = (uint32_t)d[c];
   uint64_t spread = 0;
-  DevBuf dd, ser, parts, sums, err;
+  DevBuf dd, ser, parts, sums, means, err;
   PSR_TRY(dd.ensure(o.nch * 4));
   PSR_CUDA(cudaMemcpyAsync(dd.p, tab.data(), o.nch * 4, cudaMemcpyHostToDevice, st));
   const uint64_t ldo = series_ld_(n);
   PSR_TRY(ser.ensure(ldo * 4 + 256));
   PSR_TRY(parts.ensure(((n + 1023) / 1024 + 8) * 8));
   PSR_TRY(sums.ensure(8));
+  PSR_TRY(means.ensure(8));
   PSR_TRY(err.ensure(8));
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
   PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), 1, n, ser.as<float>(), ldo,
-                               parts.as<double>(), sums.as<double>(), spread, err.as<unsigned>(),
-                               st));
+                               parts.as<double>(), sums.as<double>(), means.as<float>(), spread,
+                               err.as<unsigned>(), st));
   PSR_CUDA(cudaMemcpyAsync(out, ser.p, n * 4, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
   return PSR_OK;
@@ -564,16 +565,17 @@ int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntria
     return PSR_EDEDISPERSE;
   }
   const uint64_t ldo = series_ld(length);
-  DevBuf dd, ser, parts, sums, err;
+  DevBuf dd, ser, parts, sums, means, err;
   PSR_TRY(dd.ensure(tab.size() * 4));
   PSR_CUDA(cudaMemcpyAsync(dd.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, st));
   PSR_TRY(ser.ensure(ntrials * ldo * 4 + 256));
   PSR_TRY(parts.ensure(ntrials * dedisperse_part_count(o, length) * 8 + 8));
   PSR_TRY(sums.ensure(ntrials * 8));
+  PSR_TRY(means.ensure(ntrials * 4));
   PSR_TRY(err.ensure(8));
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
   PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), ntrials, length, ser.as<float>(), ldo,
-                               parts.as<double>(), sums.as<double>(), spread,
+                               parts.as<double>(), sums.as<double>(), means.as<float>(), spread,
                                err.as<unsigned>(), st));
   PSR_CUDA(cudaMemcpy2DAsync(out, length * 4, ser.p, ldo * 4, length * 4, ntrials,
                              cudaMemcpyDeviceToHost, st));
@@ -607,8 +609,10 @@ int psr_raw_power(const float *series, uint64_t len, float *out) {
   // integer-valued and bounded-range series the search produces).
   double sum = -0.0;
   for (uint64_t i = 0; i < len; ++i) sum += (double)series[i];
-  PSR_CUDA(cudaMemcpyAsync(sums.p, &sum, 8, cudaMemcpyHostToDevice, s.s));
-  PSR_TRY(launch_raw_power_ex(p, ser.as<float>(), ldo, sums.as<double>(), 1, work.as<float2>(),
+  const float mean = (float)(sum / (double)len);
+  PSR_CUDA(cudaMemcpyAsync(sums.p, &mean, 4, cudaMemcpyHostToDevice, s.s));
+  PSR_CUDA(cudaStreamSynchronize(s.s));
+  PSR_TRY(launch_raw_power_ex(p, ser.as<float>(), ldo, sums.as<float>(), 1, work.as<float2>(),
                               power.as<float>(), ((p.M + 1 + 63) / 64) * 64, psum.as<double>(),
                               s.s));
   PSR_CUDA(cudaMemcpyAsync(out, power.p, (p.M + 1) * 4, cudaMemcpyDeviceToHost, s.s));

@@ -305,14 +305,16 @@ __global__ void __launch_bounds__(DG_NT)
   }
 }
 
-// Ordered reduction of per-tile partial sums into the series sum per trial.
+// Ordered reduction of per-tile partial sums into the series sum per trial
+// and the f32 mean the FFT subtracts (search/src/lib.rs:36-40).
 __global__ void k_reduce_parts(const double *part, uint64_t ntiles, uint64_t ntrials,
-                               double *sums) {
+                               uint64_t n, double *sums, float *means) {
   uint64_t tr = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tr >= ntrials) return;
   double s = 0.0;
   for (uint64_t i = 0; i < ntiles; ++i) s += part[tr * ntiles + i];
   sums[tr] = s;
+  means[tr] = (float)(s / (double)n);
 }
 
 }  // namespace
@@ -321,7 +323,7 @@ uint64_t series_ld(uint64_t n) { return ((n + 63) / 64) * 64; }
 
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part,
-                         double *d_sums, uint64_t max_spread, unsigned *d_err,
+                         double *d_sums, float *d_means, uint64_t max_spread, unsigned *d_err,
                          cudaStream_t st) {
   const bool packed = o.kind == SAMPLE_U8 && (double)o.nch * o.max_value() <= 65535.0;
   if (packed) {
@@ -343,7 +345,8 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
                                                cc, rowcap, d_err);
       PSR_CUDA(cudaGetLastError());
       k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles,
-                                                                         ntrials, d_sums);
+                                                                         ntrials, n, d_sums,
+                                                                         d_means);
       PSR_CUDA(cudaGetLastError());
       return PSR_OK;
     }
@@ -368,7 +371,7 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
   }
   PSR_CUDA(cudaGetLastError());
   k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles, ntrials,
-                                                                     d_sums);
+                                                                     n, d_sums, d_means);
   PSR_CUDA(cudaGetLastError());
   return PSR_OK;
 }

@@ -224,9 +224,19 @@ __device__ __forceinline__ float2 load_z(const float *__restrict__ row, uint64_t
   return make_float2(x0, x1);
 }
 
-__device__ __forceinline__ float trial_mean(const double *sums, uint64_t trial, uint64_t len) {
-  return (float)(sums[trial] / (double)len);
-}
+// Partial sums of the power spectrum for the normalisation floor: f32
+// TwoSum (error-free transformation) per thread, f64 across threads.
+struct Acc2 {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float b) {
+    const float s = __fadd_rn(hi, b);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 template <int NT>
 __device__ __forceinline__ void block_sum_store(double acc, double *dst) {
@@ -247,7 +257,7 @@ __device__ __forceinline__ void block_sum_store(double acc, double *dst) {
 template <int M>
 __global__ void __launch_bounds__(threads_for(M, 1))
     k_fft_small(const float *__restrict__ series, uint64_t lds, uint64_t len,
-                const double *__restrict__ sums, const float2 *__restrict__ Q, int lq,
+                const float *__restrict__ means, const float2 *__restrict__ Q, int lq,
                 uint32_t N, float *__restrict__ power, uint64_t ldp,
                 double *__restrict__ psum) {
   constexpr int NT = threads_for(M, 1);
@@ -256,26 +266,26 @@ __global__ void __launch_bounds__(threads_for(M, 1))
   float2 *sm = dyn + M;  // M x 2 (C = 1, S = 2)
   const uint64_t trial = blockIdx.x;
   const float *row = series + trial * lds;
-  const float mean = trial_mean(sums, trial, len);
+  const float mean = means[trial];
   build_wl<M>(Wl, N, Q, lq);
   for (int n = threadIdx.x; n < M; n += NT) sm[n * 2] = load_z(row, len, (uint64_t)n, mean);
   __syncthreads();
   subfft<M, 1, NT>(sm, Wl);
-  double acc = 0.0;
+  Acc2 acc;
   float *out = power + trial * ldp;
   for (int k = threadIdx.x; k <= M; k += NT) {
     const float p = post_power(sm[(k % M) * 2], sm[((M - k) % M) * 2], twN(Q, (uint32_t)k, lq));
     out[k] = p;
-    acc += (double)p;
+    acc.add(p);
   }
-  block_sum_store<NT>(acc, psum + trial);
+  block_sum_store<NT>(acc.value(), psum + trial);
 }
 
 // Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
 template <int M1, int M2>
 __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
     k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
-                const double *__restrict__ sums, const float2 *__restrict__ Q, int lq,
+                const float *__restrict__ means, const float2 *__restrict__ Q, int lq,
                 uint32_t N, float2 *__restrict__ work) {
   constexpr int C = cols_for(M1), S = C + 1, NT = threads_for(M1, C);
   constexpr uint32_t M = (uint32_t)M1 * M2;
@@ -285,7 +295,7 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
   const uint64_t trial = blockIdx.y;
   const uint32_t n2_0 = blockIdx.x * (uint32_t)C;
   const float *row = series + trial * lds;
-  const float mean = trial_mean(sums, trial, len);
+  const float mean = means[trial];
   build_wl<M1>(Wl, N, Q, lq);
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
   constexpr int total = M1 * C;
@@ -381,7 +391,7 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
   }
   __syncthreads();
   subfft<M2, C, NT>(sm, Wl);
-  double acc = 0.0;
+  Acc2 acc;
   if (g == 0) {
     for (uint32_t idx = threadIdx.x; idx < 2 * M2; idx += NT) {
       const uint32_t k2 = idx % M2, which = idx / M2;
@@ -395,12 +405,12 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
       }
       const float p = post_power(sm[k2 * S + which], sm[mk2 * S + which], twN(Q, k, lq));
       out[k] = p;
-      acc += (double)p;
+      acc.add(p);
     }
     if (threadIdx.x == 0) {  // k = M (Nyquist): a = Z[0], b = conj(Z[0])
       const float p = post_power(sm[0], sm[0], twN(Q, M, lq));
       out[M] = p;
-      acc += (double)p;
+      acc.add(p);
     }
   } else {
     constexpr int PB = LB / 2;  // bins per batch (two twiddles each)
@@ -430,18 +440,19 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
           const float pm = post_power(zm, zk, wm[u]);
           out[k] = pk;
           out[mk] = pm;
-          acc += (double)pk + (double)pm;
+          acc.add(pk);
+          acc.add(pm);
         }
       }
     }
   }
-  block_sum_store<NT>(acc, psum + trial * ngroups + g);
+  block_sum_store<NT>(acc.value(), psum + trial * ngroups + g);
 }
 
 struct FftArgs {
   const float *series;
   uint64_t lds, len;
-  const double *sums;
+  const float *means;
   const float2 *Q;
   int lq;
   uint32_t N;
@@ -459,7 +470,7 @@ int run_small(const FftArgs &a) {
   PSR_CUDA(cudaFuncSetAttribute(k_fft_small<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   k_fft_small<M><<<(unsigned)a.ntrials, threads_for(M, 1), smem, a.st>>>(
-      a.series, a.lds, a.len, a.sums, a.Q, a.lq, a.N, a.power, a.ldp, a.psum);
+      a.series, a.lds, a.len, a.means, a.Q, a.lq, a.N, a.power, a.ldp, a.psum);
   PSR_CUDA(cudaGetLastError());
   return PSR_OK;
 }
@@ -472,7 +483,7 @@ int run_four_step(const FftArgs &a) {
     PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     dim3 grid((unsigned)(M2 / C), (unsigned)a.ntrials);
-    k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(a.series, a.lds, a.len, a.sums,
+    k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(a.series, a.lds, a.len, a.means,
                                                                     a.Q, a.lq, a.N, a.work);
     PSR_CUDA(cudaGetLastError());
   }
@@ -531,11 +542,11 @@ int FftPlan::init(uint64_t series_len, cudaStream_t st) {
 }
 
 int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
-                        const double *d_sums, uint64_t ntrials, float2 *d_work, float *d_power,
+                        const float *d_means, uint64_t ntrials, float2 *d_work, float *d_power,
                         uint64_t ldp, double *d_psum, cudaStream_t st) {
   int lq = 0;
   while ((1ull << lq) < p.N / 4) ++lq;
-  FftArgs a{d_series, lds,     p.len,   d_sums, p.Q.as<float2>(), lq, (uint32_t)p.N, ntrials,
+  FftArgs a{d_series, lds,     p.len,   d_means, p.Q.as<float2>(), lq, (uint32_t)p.N, ntrials,
             d_work,   d_power, ldp,     d_psum, st};
   switch (p.m) {
     case 1: return run_small<2>(a);

@@ -50,124 +50,6 @@ __device__ __forceinline__ int count_le64(const uint32_t *a, uint32_t key) {
 // index of different chunks hit different banks.
 constexpr int SC_STRIDE = 65;
 
-__global__ void __launch_bounds__(SC_NT)
-    k_scales(const float *__restrict__ power, uint64_t ldp, uint64_t plen,
-             const double *__restrict__ psum, uint32_t npsum, float *__restrict__ scale,
-             uint64_t lds, uint64_t nblocks) {
-  __shared__ uint32_t ch[SC_CH * SC_STRIDE];
-  __shared__ float floor_s;
-  const uint64_t trial = blockIdx.y;
-  const float *raw = power + trial * ldp;
-  const long long b0 = (long long)blockIdx.x * SC_G;
-  const long long c_first = b0 - 2;  // chunk index of local chunk 0
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp == 0) {  // floor: mean of the raw power from the FFT's partial sums
-    double s = 0.0;
-    for (uint32_t i = lane; i < npsum; i += 32) s += psum[trial * npsum + i];
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) floor_s = (float)(s / (double)plen * 1e-6);
-  }
-  // Stage the bins of all chunks (coalesced, 16 loads in flight per thread);
-  // out-of-range chunks and bin 0 hold the sentinel 0xffffffff.
-  constexpr int NV = SC_CH * 64;
-  const long long e_first = c_first * 64;
-  for (int base = 0; base < NV; base += 16 * SC_NT) {
-    uint32_t v[16];
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int i = base + u * SC_NT + (int)threadIdx.x;
-      const long long e = e_first + i;
-      v[u] = (i < NV && e >= 1 && e < (long long)plen) ? fbits(raw[e]) : 0xffffffffu;
-    }
-#pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int i = base + u * SC_NT + (int)threadIdx.x;
-      if (i < NV) ch[(i >> 6) * SC_STRIDE + (i & 63)] = v[u];
-    }
-  }
-  __syncthreads();
-  {
-    // Thread t sorts chunk t in registers (fully unrolled bitonic network of
-    // 672 compare-exchanges: no shuffles, static register indices).  The
-    // stride-65 layout makes these row reads bank-conflict free.
-    uint32_t x[64];
-    uint32_t *row = ch + threadIdx.x * SC_STRIDE;
-#pragma unroll
-    for (int i = 0; i < 64; ++i) x[i] = row[i];
-#pragma unroll
-    for (int k = 2; k <= 64; k <<= 1)
-#pragma unroll
-      for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-        for (int i = 0; i < 64; ++i) {
-          const int l = i ^ j;
-          if (l > i) {
-            const uint32_t a = x[i], b = x[l];
-            if ((i & k) == 0) {
-              x[i] = min(a, b);
-              x[l] = max(a, b);
-            } else {
-              x[i] = max(a, b);
-              x[l] = min(a, b);
-            }
-          }
-        }
-#pragma unroll
-    for (int i = 0; i < 64; ++i) row[i] = x[i];
-  }
-  __syncthreads();
-  const long long b = b0 + threadIdx.x;
-  if (threadIdx.x >= SC_G || b >= (long long)nblocks) return;
-  const long long center = b * 64;
-  const long long lo = max(center - 128, 1ll);
-  const long long hi = min(center + 192, (long long)plen);
-  const int r = (int)(hi - lo) / 2;
-  // The window is local chunks threadIdx.x .. threadIdx.x + 4 (chunks b-2..b+2),
-  // each sorted and padded with sentinels above every value.
-  const uint32_t *w = ch + threadIdx.x * SC_STRIDE;
-  // Lower bound: y = min_i A_i[r/5].  Every chunk holds at most r/5 elements
-  // below y, so at most r elements of the window are below y and the
-  // rank-r element is >= y; those elements are skipped.
-  const int q = min(r / 5, 63);
-  uint32_t y = 0xffffffffu;
-#pragma unroll
-  for (int d = 0; d < 5; ++d) y = min(y, w[d * SC_STRIDE + q]);
-  int p[5];
-  int skipped = 0;
-#pragma unroll
-  for (int d = 0; d < 5; ++d) {
-    p[d] = y == 0u ? 0 : count_le64(w + d * SC_STRIDE, y - 1u);  // elements < y
-    skipped += p[d];
-  }
-  // 5-way merge walk over the rest: advance the smallest head r - skipped
-  // times; the smallest head is then the rank-r element.
-  uint32_t hd[5];
-#pragma unroll
-  for (int d = 0; d < 5; ++d) hd[d] = w[d * SC_STRIDE + p[d]];
-  for (int step = skipped; step < r; ++step) {
-    uint32_t m = hd[0];
-    int am = 0;
-#pragma unroll
-    for (int d = 1; d < 5; ++d)
-      if (hd[d] < m) {
-        m = hd[d];
-        am = d;
-      }
-#pragma unroll
-    for (int d = 0; d < 5; ++d)
-      if (d == am) {
-        ++p[d];
-        hd[d] = p[d] < 64 ? w[d * SC_STRIDE + p[d]] : 0xffffffffu;
-      }
-  }
-  uint32_t med_k = hd[0];
-#pragma unroll
-  for (int d = 1; d < 5; ++d) med_k = min(med_k, hd[d]);
-  const float med = __uint_as_float(med_k);
-  const float sc = fmaxf(fmaxf(__fdiv_rn(med, LN2F), floor_s), 1e-20f);
-  scale[trial * lds + b] = sc;
-}
-
 struct RawCand {
   double score;
   double freq;
@@ -261,9 +143,6 @@ __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64
   a.raw[trial * a.raw_cap + slot] = c;
 }
 
-constexpr int HM_NT = 256;
-constexpr int HM_KPT = 8;  // bins per thread; a CTA covers HM_NT * HM_KPT bins
-constexpr int HM_BINS = HM_NT * HM_KPT;
 
 // round(RN(kf * j)) for a positive normal double kf and 1 <= j <= 16, in
 // exact 64-bit integer arithmetic: kf = m * 2^E (53-bit m), the product m*j
@@ -336,41 +215,215 @@ __device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, c
   }
 }
 
-// Every bin is first tested with exact f32 gates: an h = 1 peak needs
-// max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value minus 1
-// reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and h >= 2
-// scores exist only where pw(k) >= 4.  The rare bins that pass are queued in
-// shared memory (a CTA covers 2048 bins, so the queue fills a warp) and
-// then evaluated one bin per lane.
-__global__ void __launch_bounds__(HM_NT, 2) k_harmonic(HarmArgs a) {
-  __shared__ uint16_t q1[HM_BINS], q2[HM_BINS];
-  __shared__ int n1, n2;
+// Gate queues: per trial the bins that pass the h = 1 gate (q1) and the
+// h >= 2 gate (q2); capacity qcap each, counts n1/n2.
+struct GateArgs {
+  uint32_t *q1, *q2;
+  unsigned *n1, *n2;
+  uint64_t qcap;
+};
+
+constexpr int SCG_OWN = SC_G * 64;  // bins of the CTA's own blocks
+constexpr size_t SCG_SMEM = (size_t)SC_CH * SC_STRIDE * 4 + (size_t)SCG_OWN * 4 +
+                            (size_t)(SC_G + 4) * 4 + (size_t)SCG_OWN * 2 * 2;
+
+// pw(k) from a staged raw value and its block's scale (same arithmetic as pw()).
+__device__ __forceinline__ float pw_staged(const HarmArgs &a, uint32_t bits, float scale,
+                                           uint64_t k) {
+  if (k == 0) return 0.0f;
+  const float v = __fdiv_rn(__uint_as_float(bits), scale);
+  if (a.nbirdies) {
+    const double f = (double)k * a.bin_hz;
+    for (int q = 0; q < a.nbirdies; ++q)
+      if (fabs(__dsub_rn(f, a.birdies[2 * q])) <= a.birdies[2 * q + 1]) return 0.0f;
+  }
+  return v;
+}
+
+// Normalisation scales of 124 blocks per CTA, then the exact f32 harmonic
+// gates on the CTA's own bins while they are still on chip: an h = 1 peak
+// needs max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value
+// minus 1 reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and
+// h >= 2 scores exist only where pw(k) >= 4.  The last bin of the range, whose
+// neighbour's scale belongs to the next CTA, is queued unconditionally; the
+// item kernel evaluates every queued bin exactly.
+__global__ void __launch_bounds__(SC_NT)
+    k_scales_gate(HarmArgs a, const double *__restrict__ psum, uint32_t npsum,
+                  uint64_t nblocks, float *__restrict__ scale_out, GateArgs g) {
+  extern __shared__ __align__(16) uint32_t dsm[];
+  uint32_t *ch = dsm;                                // SC_CH x SC_STRIDE (sorted chunks)
+  uint32_t *own = ch + SC_CH * SC_STRIDE;            // SCG_OWN raw bins, unsorted
+  float *scale_s = reinterpret_cast<float *>(own + SCG_OWN);
+  uint16_t *lq1 = reinterpret_cast<uint16_t *>(scale_s + SC_G + 4);
+  uint16_t *lq2 = lq1 + SCG_OWN;
+  __shared__ float floor_s;
+  __shared__ int c1, c2;
+  __shared__ unsigned base1, base2;
+  const uint64_t plen = a.plen;
+  const uint64_t trial = blockIdx.y;
+  const float *raw = a.power + trial * a.ldp;
+  const long long b0 = (long long)blockIdx.x * SC_G;
+  const long long c_first = b0 - 2;  // chunk index of local chunk 0
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {  // floor: mean of the raw power from the FFT's partial sums
+    double s = 0.0;
+    for (uint32_t i = lane; i < npsum; i += 32) s += psum[trial * npsum + i];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) floor_s = (float)(s / (double)plen * 1e-6);
+  }
+  if (threadIdx.x == 0) c1 = c2 = 0;
+  // Stage the bins of all chunks (coalesced, 16 loads in flight per thread);
+  // out-of-range chunks and bin 0 hold the sentinel 0xffffffff.
+  constexpr int NV = SC_CH * 64;
+  const long long e_first = c_first * 64;
+  for (int base = 0; base < NV; base += 16 * SC_NT) {
+    uint32_t v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int i = base + u * SC_NT + (int)threadIdx.x;
+      const long long e = e_first + i;
+      v[u] = (i < NV && e >= 1 && e < (long long)plen) ? fbits(raw[e]) : 0xffffffffu;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int i = base + u * SC_NT + (int)threadIdx.x;
+      if (i < NV) {
+        ch[(i >> 6) * SC_STRIDE + (i & 63)] = v[u];
+        if (i >= 128 && i < 128 + SCG_OWN) own[i - 128] = v[u];
+      }
+    }
+  }
+  __syncthreads();
+  {
+    // Thread t sorts chunk t in registers (fully unrolled bitonic network of
+    // 672 compare-exchanges: no shuffles, static register indices).  The
+    // stride-65 layout makes these row reads bank-conflict free.
+    uint32_t x[64];
+    uint32_t *row = ch + threadIdx.x * SC_STRIDE;
+#pragma unroll
+    for (int i = 0; i < 64; ++i) x[i] = row[i];
+#pragma unroll
+    for (int k = 2; k <= 64; k <<= 1)
+#pragma unroll
+      for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+          const int l = i ^ j;
+          if (l > i) {
+            const uint32_t p0 = x[i], p1 = x[l];
+            if ((i & k) == 0) {
+              x[i] = min(p0, p1);
+              x[l] = max(p0, p1);
+            } else {
+              x[i] = max(p0, p1);
+              x[l] = min(p0, p1);
+            }
+          }
+        }
+#pragma unroll
+    for (int i = 0; i < 64; ++i) row[i] = x[i];
+  }
+  __syncthreads();
+  const long long b = b0 + threadIdx.x;
+  if (threadIdx.x < SC_G && b < (long long)nblocks) {
+    const long long center = b * 64;
+    const long long lo = max(center - 128, 1ll);
+    const long long hi = min(center + 192, (long long)plen);
+    const int r = (int)(hi - lo) / 2;
+    // The window is local chunks threadIdx.x .. threadIdx.x + 4 (chunks
+    // b-2..b+2), each sorted and padded with sentinels above every value.
+    const uint32_t *w = ch + threadIdx.x * SC_STRIDE;
+    // Lower bound: y = min_i A_i[r/5].  Every chunk holds at most r/5
+    // elements below y, so at most r elements of the window are below y and
+    // the rank-r element is >= y; those elements are skipped.
+    const int q = min(r / 5, 63);
+    uint32_t y = 0xffffffffu;
+#pragma unroll
+    for (int d = 0; d < 5; ++d) y = min(y, w[d * SC_STRIDE + q]);
+    int p[5];
+    int skipped = 0;
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+      p[d] = y == 0u ? 0 : count_le64(w + d * SC_STRIDE, y - 1u);  // elements < y
+      skipped += p[d];
+    }
+    // 5-way merge walk over the rest: advance the smallest head r - skipped
+    // times; the smallest head is then the rank-r element.
+    uint32_t hd[5];
+#pragma unroll
+    for (int d = 0; d < 5; ++d) hd[d] = w[d * SC_STRIDE + p[d]];
+    for (int step = skipped; step < r; ++step) {
+      uint32_t m = hd[0];
+      int am = 0;
+#pragma unroll
+      for (int d = 1; d < 5; ++d)
+        if (hd[d] < m) {
+          m = hd[d];
+          am = d;
+        }
+#pragma unroll
+      for (int d = 0; d < 5; ++d)
+        if (d == am) {
+          ++p[d];
+          hd[d] = p[d] < 64 ? w[d * SC_STRIDE + p[d]] : 0xffffffffu;
+        }
+    }
+    uint32_t med_k = hd[0];
+#pragma unroll
+    for (int d = 1; d < 5; ++d) med_k = min(med_k, hd[d]);
+    const float sc = fmaxf(fmaxf(__fdiv_rn(__uint_as_float(med_k), LN2F), floor_s), 1e-20f);
+    scale_s[threadIdx.x] = sc;
+    scale_out[trial * a.lds + b] = sc;
+  }
+  __syncthreads();
+  // Gates on the CTA's own bins.
+  const uint64_t kb0 = (uint64_t)b0 * 64;
+  for (int i = threadIdx.x; i < SCG_OWN; i += SC_NT) {
+    const uint64_t k = kb0 + (uint64_t)i;
+    if (k < a.first + 1 || k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
+    const float p0 = pw_staged(a, own[i], scale_s[i >> 6], k);
+    bool pass1 = true;
+    if (i + 1 < SCG_OWN)
+      pass1 = fmaxf(p0, pw_staged(a, own[i + 1], scale_s[(i + 1) >> 6], k + 1)) >= a.t1;
+    if (pass1) lq1[atomicAdd(&c1, 1)] = (uint16_t)i;
+    if (p0 >= 4.0f) lq2[atomicAdd(&c2, 1)] = (uint16_t)i;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    base1 = atomicAdd(&g.n1[trial], (unsigned)c1);
+    base2 = atomicAdd(&g.n2[trial], (unsigned)c2);
+  }
+  __syncthreads();
+  uint32_t *q1 = g.q1 + trial * g.qcap, *q2 = g.q2 + trial * g.qcap;
+  for (int i = threadIdx.x; i < c1; i += SC_NT) q1[base1 + i] = (uint32_t)(kb0 + lq1[i]);
+  for (int i = threadIdx.x; i < c2; i += SC_NT) q2[base2 + i] = (uint32_t)(kb0 + lq2[i]);
+}
+
+// Exact evaluation of the gated bins, one bin per thread: h = 1 peaks for
+// q1 entries, all harmonic levels h >= 2 for q2 entries.
+constexpr int HI_NT = 256;
+constexpr int HI_CTAS_PER_TRIAL = 12;
+
+__global__ void __launch_bounds__(HI_NT) k_harm_items(HarmArgs a, GateArgs g) {
   const uint64_t trial = blockIdx.y;
   const float *raw = a.power + trial * a.ldp;
   const float *sc = a.scale + trial * a.lds;
-  if (threadIdx.x == 0) n1 = n2 = 0;
-  __syncthreads();
-  const uint64_t kb = a.first + 1 + (uint64_t)blockIdx.x * HM_BINS;
-#pragma unroll
-  for (int i = 0; i < HM_KPT; ++i) {
-    const uint64_t k = kb + (uint64_t)i * HM_NT + threadIdx.x;
-    if (k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
-    const float p0 = pw(a, raw, sc, k), p1 = pw(a, raw, sc, k + 1);
-    const uint16_t rel = (uint16_t)(k - kb);
-    if (fmaxf(p0, p1) >= a.t1) q1[atomicAdd(&n1, 1)] = rel;
-    if (p0 >= 4.0f) q2[atomicAdd(&n2, 1)] = rel;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n1; i += blockDim.x) {
-    const uint64_t k = kb + q1[i];
-    const double s = score_at(a, raw, sc, k, 0);
-    if (s >= a.threshold) {
-      const double sm = score_at(a, raw, sc, k - 1, 0);
-      const double sp = score_at(a, raw, sc, k + 1, 0);
-      if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
+  const unsigned n1 = g.n1[trial], n2 = g.n2[trial];
+  const uint32_t *q1 = g.q1 + trial * g.qcap, *q2 = g.q2 + trial * g.qcap;
+  for (unsigned idx = blockIdx.x * HI_NT + threadIdx.x; idx < n1 + n2;
+       idx += gridDim.x * HI_NT) {
+    if (idx < n1) {
+      const uint64_t k = q1[idx];
+      const double s = score_at(a, raw, sc, k, 0);
+      if (s >= a.threshold) {
+        const double sm = score_at(a, raw, sc, k - 1, 0);
+        const double sp = score_at(a, raw, sc, k + 1, 0);
+        if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
+      }
+    } else {
+      harm_item(a, trial, raw, sc, q2[idx - n1]);
     }
   }
-  for (int i = threadIdx.x; i < n2; i += blockDim.x) harm_item(a, trial, raw, sc, kb + q2[i]);
 }
 
 // Orderable key: score descending, then (h, k) ascending = the reference's
@@ -573,6 +626,9 @@ int spectrum_prepare(const FftPlan &p, const SpecConfig &c, uint64_t outer, uint
   PSR_TRY(w.raw.ensure(outer * w.raw_cap * sizeof(RawCand)));
   PSR_TRY(w.raw_count.ensure(outer * 4));
   PSR_TRY(w.overflow.ensure(16));
+  w.qcap = plen;
+  PSR_TRY(w.gq.ensure(2 * inner * w.qcap * 4));
+  PSR_TRY(w.gn.ensure(2 * inner * 4 + 16));
   PSR_TRY(w.birdies.ensure(std::max<size_t>(c.birdies.size(), 2) * 8));
   if (!c.birdies.empty())
     PSR_CUDA(cudaMemcpyAsync(w.birdies.p, c.birdies.data(), c.birdies.size() * 8,
@@ -593,12 +649,6 @@ int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_pow
                        uint64_t slot0, SpecWork &w, cudaStream_t st) {
   const uint64_t plen = p.M + 1;
   const uint64_t nblocks = (plen + 63) / 64;
-  {
-    dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
-    k_scales<<<grid, SC_NT, 0, st>>>(d_power, ldp, plen, d_psum, npsum, w.scale.as<float>(),
-                                    w.lds, nblocks);
-    PSR_CUDA(cudaGetLastError());
-  }
   // search/src/lib.rs:62, 73-78
   const double bin_hz = 1.0 / ((double)p.N * c.tsamp);
   HarmArgs a{};
@@ -635,10 +685,24 @@ int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_pow
       v = std::nextafter(v, INFINITY);
     a.t1 = v;
   }
+  GateArgs g{};
+  g.qcap = w.qcap;
+  g.q1 = w.gq.as<uint32_t>();
+  g.q2 = g.q1 + ntrials * w.qcap;
+  g.n1 = w.gn.as<unsigned>();
+  g.n2 = g.n1 + ntrials;
+  PSR_CUDA(cudaMemsetAsync(g.n1, 0, 2 * ntrials * 4, st));
+  {
+    PSR_CUDA(cudaFuncSetAttribute(k_scales_gate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)SCG_SMEM));
+    dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
+    k_scales_gate<<<grid, SC_NT, SCG_SMEM, st>>>(a, d_psum, npsum, nblocks, w.scale.as<float>(),
+                                                 g);
+    PSR_CUDA(cudaGetLastError());
+  }
   if (a.end[0] > first + 1) {
-    const uint64_t nk = a.end[0] - first - 1;
-    dim3 grid((unsigned)((nk + HM_NT * HM_KPT - 1) / (HM_NT * HM_KPT)), (unsigned)ntrials);
-    k_harmonic<<<grid, HM_NT, 0, st>>>(a);
+    dim3 grid(HI_CTAS_PER_TRIAL, (unsigned)ntrials);
+    k_harm_items<<<grid, HI_NT, 0, st>>>(a, g);
     PSR_CUDA(cudaGetLastError());
   }
   return PSR_OK;

@@ -147,7 +147,8 @@ struct SpecConfig {
   std::vector<double> birdies;  // pairs
 };
 struct SpecWork {
-  DevBuf scale, raw, raw_count, birdies, overflow;
+  DevBuf scale, raw, raw_count, birdies, overflow, gq, gn;
+  uint64_t qcap = 0;     // gate queue capacity per trial
   uint64_t raw_cap = 0;  // raw (pre-dedupe) candidates per trial
   uint64_t lds = 0;      // row stride of scale[]
 };
@@ -167,12 +168,14 @@ uint64_t series_ld(uint64_t n);
 // of a channel within 8 consecutive trials, and the largest delay.
 int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
                      std::vector<uint32_t> &tab, uint64_t &max_spread, uint64_t &max_delay);
+// out[trial][t] (row stride ldo); sums[trial] = f64 series sum, means[trial] =
+// (f32)(sum / n), the value search::periodicity subtracts.
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part, double *d_sums,
-                         uint64_t max_spread, unsigned *d_err, cudaStream_t st);
+                         float *d_means, uint64_t max_spread, unsigned *d_err, cudaStream_t st);
 uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
 int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
-                        const double *d_sums, uint64_t ntrials, float2 *d_work, float *d_power,
+                        const float *d_means, uint64_t ntrials, float2 *d_work, float *d_power,
                         uint64_t ldp, double *d_psum, cudaStream_t st);
 
 // ------------------------------------------------------------- fold

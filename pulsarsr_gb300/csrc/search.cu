@@ -47,6 +47,7 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   PSR_TRY(series.ensure(chunk * ldo * 4 + 256));
   PSR_TRY(parts.ensure(chunk * nparts * 8));
   PSR_TRY(sums.ensure(chunk * 8));
+  PSR_TRY(means.ensure(chunk * 4));
   PSR_TRY(work.ensure(fft.m > 12 ? inner * fft.M * 8 : 16));
   PSR_TRY(power.ensure(inner * ldp * 4));
   PSR_TRY(psum.ensure(inner * npsum * 8));
@@ -66,16 +67,21 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
   const uint64_t nt = std::min(chunk, ntrials - t0);
   PSR_TRY(record(ST_DEDISP, true, st));
   PSR_TRY(launch_dedisperse_ex(o, delays.as<uint32_t>() + t0 * o.nch, nt, n, series.as<float>(),
-                               ldo, parts.as<double>(), sums.as<double>(), max_spread,
-                               err.as<unsigned>(), st));
+                               ldo, parts.as<double>(), sums.as<double>(), means.as<float>(),
+                               max_spread, err.as<unsigned>(), st));
   PSR_TRY(record(ST_DEDISP, false, st));
-  if (!host_sums.empty())
-    PSR_CUDA(cudaMemcpyAsync(sums.p, host_sums.data() + t0, nt * 8, cudaMemcpyHostToDevice, st));
+  if (!host_sums.empty()) {
+    host_means.resize(host_sums.size());
+    for (size_t i = 0; i < host_sums.size(); ++i)
+      host_means[i] = (float)(host_sums[i] / (double)n);
+    PSR_CUDA(cudaMemcpyAsync(means.p, host_means.data() + t0, nt * 4, cudaMemcpyHostToDevice,
+                             st));
+  }
   PSR_TRY(spectrum_reset(sw, nt, st));
   for (uint64_t i0 = 0; i0 < nt; i0 += inner) {
     const uint64_t ni = std::min(inner, nt - i0);
     PSR_TRY(record(ST_FFT, true, st));
-    PSR_TRY(launch_raw_power_ex(fft, series.as<float>() + i0 * ldo, ldo, sums.as<double>() + i0,
+    PSR_TRY(launch_raw_power_ex(fft, series.as<float>() + i0 * ldo, ldo, means.as<float>() + i0,
                                 ni, work.as<float2>(), power.as<float>(), ldp,
                                 psum.as<double>(), st));
     PSR_TRY(record(ST_FFT, false, st));

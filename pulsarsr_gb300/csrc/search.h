@@ -18,6 +18,7 @@ struct SearchEngine {
   SpecConfig spec;
   SpecWork sw;
   std::vector<double> host_sums;  // series sums supplied by the caller (optional)
+  std::vector<float> host_means;
   // Optional per-stage timing: events recorded around every stage launch on
   // the engine's stream; stage_ms accumulates their elapsed times.
   enum { ST_DEDISP = 0, ST_FFT = 1, ST_SPEC = 2, ST_COUNT = 3 };
@@ -28,7 +29,7 @@ struct SearchEngine {
   int record(int stage, bool begin, cudaStream_t st);
   int harvest();  // after a sync: add elapsed times, forget the events
   ~SearchEngine();
-  DevBuf delays, trial_dm, series, parts, sums, work, power, psum, kept, kept_count, err,
+  DevBuf delays, trial_dm, series, parts, sums, means, work, power, psum, kept, kept_count, err,
       chunk_overflow;
 
   // Delay tables, FFT plan and buffers for ntrials trials of length n.
