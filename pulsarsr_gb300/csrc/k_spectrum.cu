@@ -184,7 +184,7 @@ __device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, c
 #pragma unroll
   for (int hi = 1; hi < 5; ++hi)
     if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
-  if (hmax == 0) return;
+  if (hmax == 0 || pw(a, raw, sc, k) < 4.0f) return;  // queue entries are a superset
   const double kf = __dadd_rn((double)k, offset_at(raw, k));
   const int H = 1 << hmax;
   float v[16];
@@ -224,38 +224,28 @@ struct GateArgs {
 };
 
 constexpr int SCG_OWN = SC_G * 64;  // bins of the CTA's own blocks
-constexpr size_t SCG_SMEM = (size_t)SC_CH * SC_STRIDE * 4 + (size_t)SCG_OWN * 4 +
-                            (size_t)(SC_G + 4) * 4 + (size_t)SCG_OWN * 2 * 2;
+constexpr int SCG_LQ = 1024;        // local queue slots (overflow goes to global)
+constexpr size_t SCG_SMEM = (size_t)SC_CH * SC_STRIDE * 4 + (size_t)(SC_G + 4) * 4 +
+                            (size_t)SCG_LQ * 2 * 2;
 
-// pw(k) from a staged raw value and its block's scale (same arithmetic as pw()).
-__device__ __forceinline__ float pw_staged(const HarmArgs &a, uint32_t bits, float scale,
-                                           uint64_t k) {
-  if (k == 0) return 0.0f;
-  const float v = __fdiv_rn(__uint_as_float(bits), scale);
-  if (a.nbirdies) {
-    const double f = (double)k * a.bin_hz;
-    for (int q = 0; q < a.nbirdies; ++q)
-      if (fabs(__dsub_rn(f, a.birdies[2 * q])) <= a.birdies[2 * q + 1]) return 0.0f;
-  }
-  return v;
-}
-
-// Normalisation scales of 124 blocks per CTA, then the exact f32 harmonic
-// gates on the CTA's own bins while they are still on chip: an h = 1 peak
-// needs max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value
-// minus 1 reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and
-// h >= 2 scores exist only where pw(k) >= 4.  The last bin of the range, whose
-// neighbour's scale belongs to the next CTA, is queued unconditionally; the
-// item kernel evaluates every queued bin exactly.
+// Normalisation scales of 124 blocks per CTA, then the harmonic gates on the
+// CTA's own bins while they are hot in L2.  An h = 1 peak needs
+// max(pw(k), pw(k+1)) >= t1 (t1 = the smallest float whose f64 value minus 1
+// reaches the threshold; score_1(k) is pw(k) - 1 or pw(k+1) - 1), and h >= 2
+// scores exist only where pw(k) >= 4.  The gates are conservative supersets:
+// pw is estimated as raw * (1/scale) and a bin is queued unless the estimate
+// is below the threshold by more than 4e-7 relative (the estimate is within
+// 2e-7 of the correctly rounded quotient); birdies are ignored and the last
+// bin, whose neighbour's scale belongs to the next CTA, is always queued.
+// The item kernel evaluates every queued bin exactly.
 __global__ void __launch_bounds__(SC_NT)
     k_scales_gate(HarmArgs a, const double *__restrict__ psum, uint32_t npsum,
                   uint64_t nblocks, float *__restrict__ scale_out, GateArgs g) {
   extern __shared__ __align__(16) uint32_t dsm[];
   uint32_t *ch = dsm;                                // SC_CH x SC_STRIDE (sorted chunks)
-  uint32_t *own = ch + SC_CH * SC_STRIDE;            // SCG_OWN raw bins, unsorted
-  float *scale_s = reinterpret_cast<float *>(own + SCG_OWN);
-  uint16_t *lq1 = reinterpret_cast<uint16_t *>(scale_s + SC_G + 4);
-  uint16_t *lq2 = lq1 + SCG_OWN;
+  float *inv_s = reinterpret_cast<float *>(ch + SC_CH * SC_STRIDE);  // 1/scale per block
+  uint16_t *lq1 = reinterpret_cast<uint16_t *>(inv_s + SC_G + 4);
+  uint16_t *lq2 = lq1 + SCG_LQ;
   __shared__ float floor_s;
   __shared__ int c1, c2;
   __shared__ unsigned base1, base2;
@@ -289,7 +279,6 @@ __global__ void __launch_bounds__(SC_NT)
       const int i = base + u * SC_NT + (int)threadIdx.x;
       if (i < NV) {
         ch[(i >> 6) * SC_STRIDE + (i & 63)] = v[u];
-        if (i >= 128 && i < 128 + SCG_OWN) own[i - 128] = v[u];
       }
     }
   }
@@ -372,31 +361,54 @@ __global__ void __launch_bounds__(SC_NT)
 #pragma unroll
     for (int d = 1; d < 5; ++d) med_k = min(med_k, hd[d]);
     const float sc = fmaxf(fmaxf(__fdiv_rn(__uint_as_float(med_k), LN2F), floor_s), 1e-20f);
-    scale_s[threadIdx.x] = sc;
+    inv_s[threadIdx.x] = __frcp_rn(sc);
     scale_out[trial * a.lds + b] = sc;
   }
   __syncthreads();
-  // Gates on the CTA's own bins.
+  // Gates on the CTA's own bins (raw values re-read; they are hot in L2).
   const uint64_t kb0 = (uint64_t)b0 * 64;
+  const float t1lo = a.t1 > 0.0f ? a.t1 * (1.0f - 4e-7f) : -INFINITY;
+  const float t4lo = 4.0f * (1.0f - 4e-7f);
+  uint32_t *gq1 = g.q1 + trial * g.qcap, *gq2 = g.q2 + trial * g.qcap;
   for (int i = threadIdx.x; i < SCG_OWN; i += SC_NT) {
     const uint64_t k = kb0 + (uint64_t)i;
     if (k < a.first + 1 || k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
-    const float p0 = pw_staged(a, own[i], scale_s[i >> 6], k);
+    const float e0 = raw[k] * inv_s[i >> 6];
     bool pass1 = true;
-    if (i + 1 < SCG_OWN)
-      pass1 = fmaxf(p0, pw_staged(a, own[i + 1], scale_s[(i + 1) >> 6], k + 1)) >= a.t1;
-    if (pass1) lq1[atomicAdd(&c1, 1)] = (uint16_t)i;
-    if (p0 >= 4.0f) lq2[atomicAdd(&c2, 1)] = (uint16_t)i;
+    if (i + 1 < SCG_OWN) pass1 = fmaxf(e0, raw[k + 1] * inv_s[(i + 1) >> 6]) >= t1lo;
+    if (pass1) {
+      const int slot = atomicAdd(&c1, 1);
+      if (slot < SCG_LQ) {
+        lq1[slot] = (uint16_t)i;
+      } else {
+        const unsigned gi = atomicAdd(&g.n1[trial], 1u);
+        if (gi < g.qcap) gq1[gi] = (uint32_t)k;
+        else atomicOr(a.overflow, 1u);
+      }
+    }
+    if (e0 >= t4lo) {
+      const int slot = atomicAdd(&c2, 1);
+      if (slot < SCG_LQ) {
+        lq2[slot] = (uint16_t)i;
+      } else {
+        const unsigned gi = atomicAdd(&g.n2[trial], 1u);
+        if (gi < g.qcap) gq2[gi] = (uint32_t)k;
+        else atomicOr(a.overflow, 1u);
+      }
+    }
   }
   __syncthreads();
+  const int m1 = min(c1, SCG_LQ), m2 = min(c2, SCG_LQ);
   if (threadIdx.x == 0) {
-    base1 = atomicAdd(&g.n1[trial], (unsigned)c1);
-    base2 = atomicAdd(&g.n2[trial], (unsigned)c2);
+    base1 = atomicAdd(&g.n1[trial], (unsigned)m1);
+    base2 = atomicAdd(&g.n2[trial], (unsigned)m2);
   }
   __syncthreads();
-  uint32_t *q1 = g.q1 + trial * g.qcap, *q2 = g.q2 + trial * g.qcap;
-  for (int i = threadIdx.x; i < c1; i += SC_NT) q1[base1 + i] = (uint32_t)(kb0 + lq1[i]);
-  for (int i = threadIdx.x; i < c2; i += SC_NT) q2[base2 + i] = (uint32_t)(kb0 + lq2[i]);
+  if (threadIdx.x == 0 && (base1 + m1 > g.qcap || base2 + m2 > g.qcap)) atomicOr(a.overflow, 1u);
+  for (int i = threadIdx.x; i < m1 && base1 + i < g.qcap; i += SC_NT)
+    gq1[base1 + i] = (uint32_t)(kb0 + lq1[i]);
+  for (int i = threadIdx.x; i < m2 && base2 + i < g.qcap; i += SC_NT)
+    gq2[base2 + i] = (uint32_t)(kb0 + lq2[i]);
 }
 
 // Exact evaluation of the gated bins, one bin per thread: h = 1 peaks for
@@ -408,7 +420,7 @@ __global__ void __launch_bounds__(HI_NT) k_harm_items(HarmArgs a, GateArgs g) {
   const uint64_t trial = blockIdx.y;
   const float *raw = a.power + trial * a.ldp;
   const float *sc = a.scale + trial * a.lds;
-  const unsigned n1 = g.n1[trial], n2 = g.n2[trial];
+  const unsigned n1 = min(g.n1[trial], (unsigned)g.qcap), n2 = min(g.n2[trial], (unsigned)g.qcap);
   const uint32_t *q1 = g.q1 + trial * g.qcap, *q2 = g.q2 + trial * g.qcap;
   for (unsigned idx = blockIdx.x * HI_NT + threadIdx.x; idx < n1 + n2;
        idx += gridDim.x * HI_NT) {
@@ -622,13 +634,16 @@ int spectrum_prepare(const FftPlan &p, const SpecConfig &c, uint64_t outer, uint
   const uint64_t nblocks = (plen + 63) / 64;
   w.lds = ((nblocks + 63) / 64) * 64;
   if (w.raw_cap == 0) w.raw_cap = 2048;
-  PSR_TRY(w.scale.ensure(inner * w.lds * 4));
+  PSR_TRY(w.scale.ensure(outer * w.lds * 4));
+  (void)inner;
   PSR_TRY(w.raw.ensure(outer * w.raw_cap * sizeof(RawCand)));
   PSR_TRY(w.raw_count.ensure(outer * 4));
   PSR_TRY(w.overflow.ensure(16));
-  w.qcap = plen;
-  PSR_TRY(w.gq.ensure(2 * inner * w.qcap * 4));
-  PSR_TRY(w.gn.ensure(2 * inner * 4 + 16));
+  // Gated bins are ~2% of a noise spectrum; a quarter of the bins is ample
+  // and an overflow (flagged) reruns the chunk with room for every bin.
+  w.qcap = w.queue_full ? plen : plen / 4 + 1024;
+  PSR_TRY(w.gq.ensure(2 * outer * w.qcap * 4));
+  PSR_TRY(w.gn.ensure(2 * outer * 4 + 16));
   PSR_TRY(w.birdies.ensure(std::max<size_t>(c.birdies.size(), 2) * 8));
   if (!c.birdies.empty())
     PSR_CUDA(cudaMemcpyAsync(w.birdies.p, c.birdies.data(), c.birdies.size() * 8,
@@ -639,16 +654,17 @@ int spectrum_prepare(const FftPlan &p, const SpecConfig &c, uint64_t outer, uint
 int spectrum_reset(SpecWork &w, uint64_t outer_trials, cudaStream_t st) {
   PSR_CUDA(cudaMemsetAsync(w.raw_count.p, 0, outer_trials * 4, st));
   PSR_CUDA(cudaMemsetAsync(w.overflow.p, 0, 16, st));
+  PSR_CUDA(cudaMemsetAsync(w.gn.p, 0, 2 * outer_trials * 4, st));
+  w.outer_trials = outer_trials;
   return PSR_OK;
 }
 
 // Normalisation scales and harmonic peaks of `ntrials` spectra; their raw
 // candidates go to slots [slot0, slot0 + ntrials) of the outer chunk.
-int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_power,
-                       uint64_t ldp, const double *d_psum, uint32_t npsum, uint64_t ntrials,
-                       uint64_t slot0, SpecWork &w, cudaStream_t st) {
+namespace {
+HarmArgs harm_args(const FftPlan &p, const SpecConfig &c, const float *d_power, uint64_t ldp,
+                   SpecWork &w) {
   const uint64_t plen = p.M + 1;
-  const uint64_t nblocks = (plen + 63) / 64;
   // search/src/lib.rs:62, 73-78
   const double bin_hz = 1.0 / ((double)p.N * c.tsamp);
   HarmArgs a{};
@@ -671,40 +687,57 @@ int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_pow
     const uint64_t e = std::min(last, (plen - 2) / h);
     a.end[hi] = (e <= first + 1) ? 0 : e;
   }
-  a.raw = w.raw.as<RawCand>() + slot0 * w.raw_cap;
-  a.raw_count = w.raw_count.as<unsigned>() + slot0;
+  a.raw = w.raw.as<RawCand>();
+  a.raw_count = w.raw_count.as<unsigned>();
   a.raw_cap = w.raw_cap;
   a.overflow = w.overflow.as<unsigned>();
-  {
-    // exact f32 form of the h = 1 prefilter (double)max(pw) - 1.0 >= threshold
-    float v = (float)(c.threshold + 1.0);
-    if (std::isnan(v)) v = INFINITY;
-    for (int it = 0; it < 64 && (double)v - 1.0 >= c.threshold; ++it)
-      v = std::nextafter(v, -INFINITY);
-    for (int it = 0; it < 64 && !((double)v - 1.0 >= c.threshold); ++it)
-      v = std::nextafter(v, INFINITY);
-    a.t1 = v;
-  }
+  // exact f32 form of the h = 1 prefilter (double)max(pw) - 1.0 >= threshold
+  float v = (float)(c.threshold + 1.0);
+  if (std::isnan(v)) v = INFINITY;
+  for (int it = 0; it < 64 && (double)v - 1.0 >= c.threshold; ++it)
+    v = std::nextafter(v, -INFINITY);
+  for (int it = 0; it < 64 && !((double)v - 1.0 >= c.threshold); ++it)
+    v = std::nextafter(v, INFINITY);
+  a.t1 = v;
+  return a;
+}
+GateArgs gate_args(SpecWork &w, uint64_t slot0) {
   GateArgs g{};
   g.qcap = w.qcap;
-  g.q1 = w.gq.as<uint32_t>();
-  g.q2 = g.q1 + ntrials * w.qcap;
-  g.n1 = w.gn.as<unsigned>();
-  g.n2 = g.n1 + ntrials;
-  PSR_CUDA(cudaMemsetAsync(g.n1, 0, 2 * ntrials * 4, st));
-  {
-    PSR_CUDA(cudaFuncSetAttribute(k_scales_gate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)SCG_SMEM));
-    dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
-    k_scales_gate<<<grid, SC_NT, SCG_SMEM, st>>>(a, d_psum, npsum, nblocks, w.scale.as<float>(),
-                                                 g);
-    PSR_CUDA(cudaGetLastError());
-  }
-  if (a.end[0] > first + 1) {
-    dim3 grid(HI_CTAS_PER_TRIAL, (unsigned)ntrials);
-    k_harm_items<<<grid, HI_NT, 0, st>>>(a, g);
-    PSR_CUDA(cudaGetLastError());
-  }
+  g.q1 = w.gq.as<uint32_t>() + slot0 * w.qcap;
+  g.q2 = w.gq.as<uint32_t>() + (w.outer_trials + slot0) * w.qcap;
+  g.n1 = w.gn.as<unsigned>() + slot0;
+  g.n2 = w.gn.as<unsigned>() + w.outer_trials + slot0;
+  return g;
+}
+}  // namespace
+
+// Normalisation scales and harmonic gates of the `ntrials` spectra at slots
+// [slot0, slot0 + ntrials) of the outer chunk (d_power/d_psum point at slot0).
+int spectrum_gate(const FftPlan &p, const SpecConfig &c, const float *d_power, uint64_t ldp,
+                  const double *d_psum, uint32_t npsum, uint64_t ntrials, uint64_t slot0,
+                  SpecWork &w, cudaStream_t st) {
+  const uint64_t plen = p.M + 1;
+  const uint64_t nblocks = (plen + 63) / 64;
+  HarmArgs a = harm_args(p, c, d_power, ldp, w);
+  GateArgs g = gate_args(w, slot0);
+  PSR_CUDA(cudaFuncSetAttribute(k_scales_gate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)SCG_SMEM));
+  dim3 grid((unsigned)((nblocks + SC_G - 1) / SC_G), (unsigned)ntrials);
+  k_scales_gate<<<grid, SC_NT, SCG_SMEM, st>>>(a, d_psum, npsum, nblocks,
+                                               w.scale.as<float>() + slot0 * w.lds, g);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+// Exact evaluation of every queued bin of the outer chunk's `ntrials` spectra.
+int spectrum_items(const FftPlan &p, const SpecConfig &c, const float *d_power, uint64_t ldp,
+                   uint64_t ntrials, SpecWork &w, cudaStream_t st) {
+  HarmArgs a = harm_args(p, c, d_power, ldp, w);
+  if (a.end[0] == 0) return PSR_OK;
+  dim3 grid(HI_CTAS_PER_TRIAL, (unsigned)ntrials);
+  k_harm_items<<<grid, HI_NT, 0, st>>>(a, gate_args(w, 0));
+  PSR_CUDA(cudaGetLastError());
   return PSR_OK;
 }
 

@@ -148,16 +148,20 @@ struct SpecConfig {
 };
 struct SpecWork {
   DevBuf scale, raw, raw_count, birdies, overflow, gq, gn;
-  uint64_t qcap = 0;     // gate queue capacity per trial
+  uint64_t qcap = 0;          // gate queue capacity per trial
+  bool queue_full = false;    // size the gate queues for every bin
+  uint64_t outer_trials = 0;  // trials of the chunk being processed
   uint64_t raw_cap = 0;  // raw (pre-dedupe) candidates per trial
   uint64_t lds = 0;      // row stride of scale[]
 };
 int spectrum_prepare(const FftPlan &p, const SpecConfig &c, uint64_t outer, uint64_t inner,
                      SpecWork &w, cudaStream_t st);
 int spectrum_reset(SpecWork &w, uint64_t outer_trials, cudaStream_t st);
-int spectrum_harmonics(const FftPlan &p, const SpecConfig &c, const float *d_power,
-                       uint64_t ldp, const double *d_psum, uint32_t npsum, uint64_t ntrials,
-                       uint64_t slot0, SpecWork &w, cudaStream_t st);
+int spectrum_gate(const FftPlan &p, const SpecConfig &c, const float *d_power, uint64_t ldp,
+                  const double *d_psum, uint32_t npsum, uint64_t ntrials, uint64_t slot0,
+                  SpecWork &w, cudaStream_t st);
+int spectrum_items(const FftPlan &p, const SpecConfig &c, const float *d_power, uint64_t ldp,
+                   uint64_t ntrials, SpecWork &w, cudaStream_t st);
 int spectrum_select(const FftPlan &p, const SpecConfig &c, const double *d_trial_dm,
                     uint64_t ntrials, SpecWork &w, psr_candidate *d_kept, unsigned *d_kept_count,
                     cudaStream_t st);

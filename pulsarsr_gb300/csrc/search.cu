@@ -39,7 +39,7 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   chunk = std::min(chunk, ntrials);
   if (inner == 0) {
     const uint64_t per = (fft.m > 12 ? fft.M * 8 : 0) + ldp * 4;
-    inner = std::max<uint64_t>(1, (96ull << 20) / per);
+    inner = std::max<uint64_t>(1, (64ull << 20) / per);
   }
   inner = std::min(inner, chunk);
   nparts = dedisperse_part_count(o, n);
@@ -49,8 +49,8 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   PSR_TRY(sums.ensure(chunk * 8));
   PSR_TRY(means.ensure(chunk * 4));
   PSR_TRY(work.ensure(fft.m > 12 ? inner * fft.M * 8 : 16));
-  PSR_TRY(power.ensure(inner * ldp * 4));
-  PSR_TRY(psum.ensure(inner * npsum * 8));
+  PSR_TRY(power.ensure(chunk * ldp * 4));
+  PSR_TRY(psum.ensure(chunk * npsum * 8));
   PSR_TRY(spectrum_prepare(fft, spec, chunk, inner, sw, st));
   const uint64_t maxc = std::max<uint64_t>(cfg.max_candidates, 1);
   PSR_TRY(kept.ensure(ntrials * maxc * sizeof(psr_candidate)));
@@ -82,16 +82,17 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
     const uint64_t ni = std::min(inner, nt - i0);
     PSR_TRY(record(ST_FFT, true, st));
     PSR_TRY(launch_raw_power_ex(fft, series.as<float>() + i0 * ldo, ldo, means.as<float>() + i0,
-                                ni, work.as<float2>(), power.as<float>(), ldp,
-                                psum.as<double>(), st));
+                                ni, work.as<float2>(), power.as<float>() + i0 * ldp, ldp,
+                                psum.as<double>() + i0 * npsum, st));
     PSR_TRY(record(ST_FFT, false, st));
     PSR_TRY(record(ST_SPEC, true, st));
-    PSR_TRY(spectrum_harmonics(fft, spec, power.as<float>(), ldp, psum.as<double>(), npsum, ni,
-                               i0, sw, st));
+    PSR_TRY(spectrum_gate(fft, spec, power.as<float>() + i0 * ldp, ldp,
+                          psum.as<double>() + i0 * npsum, npsum, ni, i0, sw, st));
     PSR_TRY(record(ST_SPEC, false, st));
   }
   const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
   PSR_TRY(record(ST_SPEC, true, st));
+  PSR_TRY(spectrum_items(fft, spec, power.as<float>(), ldp, nt, sw, st));
   PSR_TRY(spectrum_select(fft, spec, trial_dm.as<double>() + t0, nt, sw,
                           kept.as<psr_candidate>() + t0 * maxc, kept_count.as<unsigned>() + t0,
                           st));
@@ -158,6 +159,7 @@ int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
         return PSR_ECAPACITY;
       }
       sw.raw_cap *= 4;
+      sw.queue_full = true;
       PSR_TRY(spectrum_prepare(fft, spec, chunk, inner, sw, st));
       PSR_TRY(enqueue_chunk(o, ci, st));
       unsigned v = 0;
