@@ -8,8 +8,10 @@
 // the bit-identical value.  The fast kernel stages a tile of every channel
 // row into shared memory with TMA bulk copies (cp.async.bulk + mbarrier,
 // double buffered), and each thread accumulates 16 consecutive samples for a
-// block of trials in packed 2 x u16 lanes.  Consecutive trials whose delay
-// for a channel is unchanged reuse the unpacked lanes (warp-uniform test).
+// block of trials in packed 2 x u16 lanes (samples of <= 4 bits first in
+// 4 x u8 lanes, widened once per group of channels).  Consecutive trials whose
+// delay for a channel is unchanged reuse the aligned sample words
+// (warp-uniform test).
 //
 // Everything else (f32 samples, or integer sums that could exceed 2^16) uses
 // a kernel that adds channels in reference order in f32.
@@ -111,11 +113,16 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
   if (lane == 0) mbar_arrive(bar);
 }
 
+// BYTE_LANES: samples are at most (255 / group), so `group` channels can be
+// summed in the four 8-bit lanes of a 32-bit word with a plain IADD (no lane
+// overflows, so no carry crosses a byte); the byte lanes are widened into the
+// 16-bit lanes once per group.  Without BYTE_LANES every channel is widened.
+template <bool BYTE_LANES>
 __global__ void __launch_bounds__(DD_NT)
     k_dedisp_u8(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
                 const uint32_t *__restrict__ delays, uint64_t ntrials, uint64_t n,
                 float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
-                uint64_t ntiles, int cc, int rowcap, unsigned *err) {
+                uint64_t ntiles, int cc, int rowcap, int group, unsigned *err) {
   extern __shared__ __align__(128) uint8_t smem[];
   uint8_t *bufs[2] = {smem, smem + (size_t)cc * rowcap};
   __shared__ uint64_t bars[2];
@@ -146,6 +153,24 @@ __global__ void __launch_bounds__(DD_NT)
   for (int d = 0; d < DD_DB; ++d)
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[d][i] = 0;
+  uint32_t acc8[BYTE_LANES ? DD_DB : 1][4];
+#pragma unroll
+  for (int d = 0; d < (BYTE_LANES ? DD_DB : 1); ++d)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc8[d][i] = 0;
+  int gcount = 0;
+  auto widen = [&]() {
+    if constexpr (BYTE_LANES) {
+#pragma unroll
+      for (int d = 0; d < DD_DB; ++d)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          acc[d][2 * i] += __byte_perm(acc8[d][i], 0, 0x4140);
+          acc[d][2 * i + 1] += __byte_perm(acc8[d][i], 0, 0x4342);
+          acc8[d][i] = 0;
+        }
+    }
+  };
 
   bool alive = true;
   for (int k = 0; k < nchunks; ++k) {
@@ -162,7 +187,7 @@ __global__ void __launch_bounds__(DD_NT)
       const long long base = info[b].base[r];
       const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
       long long prev = -1;
-      uint32_t p[8];
+      uint32_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
 #pragma unroll
       for (int d = 0; d < DD_DB; ++d) {
         uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
@@ -181,19 +206,30 @@ __global__ void __launch_bounds__(DD_NT)
             w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5;
           }
           const unsigned sh = (unsigned)(o & 3) * 8u;
-          uint32_t x0 = __funnelshift_r(w0, w1, sh), x1 = __funnelshift_r(w1, w2, sh);
-          uint32_t x2 = __funnelshift_r(w2, w3, sh), x3 = __funnelshift_r(w3, w4, sh);
-          p[0] = __byte_perm(x0, 0, 0x4140);
-          p[1] = __byte_perm(x0, 0, 0x4342);
-          p[2] = __byte_perm(x1, 0, 0x4140);
-          p[3] = __byte_perm(x1, 0, 0x4342);
-          p[4] = __byte_perm(x2, 0, 0x4140);
-          p[5] = __byte_perm(x2, 0, 0x4342);
-          p[6] = __byte_perm(x3, 0, 0x4140);
-          p[7] = __byte_perm(x3, 0, 0x4342);
+          x0 = __funnelshift_r(w0, w1, sh);
+          x1 = __funnelshift_r(w1, w2, sh);
+          x2 = __funnelshift_r(w2, w3, sh);
+          x3 = __funnelshift_r(w3, w4, sh);
         }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) acc[d][i] += p[i];
+        if constexpr (BYTE_LANES) {
+          acc8[d][0] += x0;
+          acc8[d][1] += x1;
+          acc8[d][2] += x2;
+          acc8[d][3] += x3;
+        } else {
+          acc[d][0] += __byte_perm(x0, 0, 0x4140);
+          acc[d][1] += __byte_perm(x0, 0, 0x4342);
+          acc[d][2] += __byte_perm(x1, 0, 0x4140);
+          acc[d][3] += __byte_perm(x1, 0, 0x4342);
+          acc[d][4] += __byte_perm(x2, 0, 0x4140);
+          acc[d][5] += __byte_perm(x2, 0, 0x4342);
+          acc[d][6] += __byte_perm(x3, 0, 0x4140);
+          acc[d][7] += __byte_perm(x3, 0, 0x4342);
+        }
+      }
+      if (BYTE_LANES && ++gcount == group) {
+        widen();
+        gcount = 0;
       }
     }
     __syncthreads();  // every thread is done reading buffer b
@@ -203,6 +239,7 @@ __global__ void __launch_bounds__(DD_NT)
                   bufs[b], rowcap, &info[b], &bars[b]);
     }
   }
+  widen();
   if (!alive) {
     // Drain the other buffer's copy (bounded) before leaving.
     if (tl == 0) mbar_wait_bounded(&bars[0], 0, err), mbar_wait_bounded(&bars[1], 0, err);
@@ -337,12 +374,21 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
     int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, o.nch, budget / (2 * (size_t)rowcap)});
     if (cc >= 1) {
       size_t smem = 2 * (size_t)cc * rowcap;
-      PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
       dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
-      k_dedisp_u8<<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns, o.nch,
-                                               d_delays, ntrials, n, d_out, ldo, d_part, ntiles,
-                                               cc, rowcap, d_err);
+      const int group = (int)(255.0 / o.max_value());
+      if (group >= 2) {
+        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_dedisp_u8<true><<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns, o.nch,
+                                                      d_delays, ntrials, n, d_out, ldo, d_part,
+                                                      ntiles, cc, rowcap, group, d_err);
+      } else {
+        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_dedisp_u8<false><<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns,
+                                                       o.nch, d_delays, ntrials, n, d_out, ldo,
+                                                       d_part, ntiles, cc, rowcap, 1, d_err);
+      }
       PSR_CUDA(cudaGetLastError());
       k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles,
                                                                          ntrials, n, d_sums,

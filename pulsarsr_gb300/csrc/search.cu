@@ -39,7 +39,7 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   chunk = std::min(chunk, ntrials);
   if (inner == 0) {
     const uint64_t per = (fft.m > 12 ? fft.M * 8 : 0) + ldp * 4;
-    inner = std::max<uint64_t>(1, (64ull << 20) / per);
+    inner = std::max<uint64_t>(1, (96ull << 20) / per);
   }
   inner = std::min(inner, chunk);
   nparts = dedisperse_part_count(o, n);
