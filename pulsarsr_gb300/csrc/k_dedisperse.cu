@@ -27,7 +27,8 @@ namespace {
 constexpr int DD_NT = 256;              // threads per CTA
 constexpr int DD_TPT = 16;              // samples per thread
 constexpr int DD_TT = DD_NT * DD_TPT;   // samples per tile (4096)
-constexpr int DD_DB = 8;                // trials per CTA
+constexpr int DD_DB = 8;                // trials per CTA (16-bit lanes only)
+constexpr int DD_DB8 = 6;               // trials per CTA with 8-bit lanes (registers)
 constexpr int DD_MAXCC = 32;            // rows per stage (one issuing lane each)
 constexpr long long DD_SPIN_LIMIT = 1ll << 26;
 
@@ -81,6 +82,7 @@ struct StageInfo {
 
 // Issue the TMA copies of rows [c0, c0+cc) for trials [d0, d0+DB) of tile t0.
 // Run by warp 0: lane i stages row c0+i.
+template <int DB>
 __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns,
                             uint64_t nch, const uint32_t *__restrict__ delays,
                             uint64_t ntrials, uint64_t d0, uint64_t t0, uint64_t c0, int cc,
@@ -90,7 +92,7 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
   if (lane < cc && c0 + lane < nch) {
     const uint64_t c = c0 + lane;
     uint32_t dmin = 0xffffffffu, dmax = 0;
-    for (int d = 0; d < DD_DB; ++d) {
+    for (int d = 0; d < DB; ++d) {
       uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
       uint32_t v = delays[tr * nch + c];
       dmin = min(dmin, v);
@@ -117,8 +119,8 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
 // summed in the four 8-bit lanes of a 32-bit word with a plain IADD (no lane
 // overflows, so no carry crosses a byte); the byte lanes are widened into the
 // 16-bit lanes once per group.  Without BYTE_LANES every channel is widened.
-template <bool BYTE_LANES>
-__global__ void __launch_bounds__(DD_NT)
+template <bool BYTE_LANES, int DB>
+__global__ void __launch_bounds__(DD_NT, 2)
     k_dedisp_u8(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
                 const uint32_t *__restrict__ delays, uint64_t ntrials, uint64_t n,
                 float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
@@ -127,10 +129,10 @@ __global__ void __launch_bounds__(DD_NT)
   uint8_t *bufs[2] = {smem, smem + (size_t)cc * rowcap};
   __shared__ uint64_t bars[2];
   __shared__ StageInfo info[2];
-  __shared__ unsigned long long wsum[DD_NT / 32][DD_DB];
+  __shared__ unsigned long long wsum[DD_NT / 32][DB];
 
   const uint64_t t0 = (uint64_t)blockIdx.x * DD_TT;
-  const uint64_t d0 = (uint64_t)blockIdx.y * DD_DB;
+  const uint64_t d0 = (uint64_t)blockIdx.y * DB;
   const int tl = threadIdx.x;
   const int nchunks = (int)((nch + cc - 1) / cc);
 
@@ -141,28 +143,28 @@ __global__ void __launch_bounds__(DD_NT)
   }
   __syncthreads();
   if (tl < 32) {
-    issue_stage(s, ld, ns, nch, delays, ntrials, d0, t0, 0, cc, bufs[0], rowcap, &info[0],
+    issue_stage<DB>(s, ld, ns, nch, delays, ntrials, d0, t0, 0, cc, bufs[0], rowcap, &info[0],
                 &bars[0]);
     if (nchunks > 1)
-      issue_stage(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)cc, cc, bufs[1], rowcap,
+      issue_stage<DB>(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)cc, cc, bufs[1], rowcap,
                   &info[1], &bars[1]);
   }
 
-  uint32_t acc[DD_DB][8];
+  uint32_t acc[DB][8];
 #pragma unroll
-  for (int d = 0; d < DD_DB; ++d)
+  for (int d = 0; d < DB; ++d)
 #pragma unroll
     for (int i = 0; i < 8; ++i) acc[d][i] = 0;
-  uint32_t acc8[BYTE_LANES ? DD_DB : 1][4];
+  uint32_t acc8[BYTE_LANES ? DB : 1][4];
 #pragma unroll
-  for (int d = 0; d < (BYTE_LANES ? DD_DB : 1); ++d)
+  for (int d = 0; d < (BYTE_LANES ? DB : 1); ++d)
 #pragma unroll
     for (int i = 0; i < 4; ++i) acc8[d][i] = 0;
   int gcount = 0;
   auto widen = [&]() {
     if constexpr (BYTE_LANES) {
 #pragma unroll
-      for (int d = 0; d < DD_DB; ++d)
+      for (int d = 0; d < DB; ++d)
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           acc[d][2 * i] += __byte_perm(acc8[d][i], 0, 0x4140);
@@ -184,18 +186,18 @@ __global__ void __launch_bounds__(DD_NT)
     const uint8_t *buf = bufs[b];
     for (int r = 0; r < rows; ++r) {
       const uint64_t c = c0 + r;
-      const long long base = info[b].base[r];
+      const int rel0 = (int)((long long)t0 - info[b].base[r]);  // t0 - staged row start
       const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
-      long long prev = -1;
+      int prev = -1;
       uint32_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
 #pragma unroll
-      for (int d = 0; d < DD_DB; ++d) {
-        uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
-        long long off = (long long)t0 + (long long)__ldg(&delays[tr * nch + c]) - base;
+      for (int d = 0; d < DB; ++d) {
+        const uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
+        const int off = rel0 + (int)__ldg(&delays[tr * nch + c]);
         if (off != prev) {  // uniform across the CTA
           prev = off;
-          const int q = tl + (int)(off >> 4);
-          const int o = (int)(off & 15);
+          const int q = tl + (off >> 4);
+          const int o = off & 15;
           uint4 lo = row16[q], hi = row16[q + 1];
           uint32_t w0 = lo.x, w1 = lo.y, w2 = lo.z, w3 = lo.w, w4 = hi.x, w5 = hi.y, w6 = hi.z,
                    w7 = hi.w;
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(DD_NT)
     __syncthreads();  // every thread is done reading buffer b
     if (tl < 32 && k + 2 < nchunks) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue_stage(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc, cc,
+      issue_stage<DB>(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc, cc,
                   bufs[b], rowcap, &info[b], &bars[b]);
     }
   }
@@ -248,7 +250,7 @@ __global__ void __launch_bounds__(DD_NT)
 
   const uint64_t tb = t0 + (uint64_t)tl * DD_TPT;
 #pragma unroll
-  for (int d = 0; d < DD_DB; ++d) {
+  for (int d = 0; d < DB; ++d) {
     const uint64_t tr = d0 + d;
     float v[16];
     unsigned long long local = 0;
@@ -277,7 +279,7 @@ __global__ void __launch_bounds__(DD_NT)
     if ((tl & 31) == 0) wsum[tl >> 5][d] = local;
   }
   __syncthreads();
-  if (tl < DD_DB && d0 + tl < ntrials) {
+  if (tl < DB && d0 + tl < ntrials) {
     unsigned long long t = 0;
     for (int w = 0; w < DD_NT / 32; ++w) t += wsum[w][tl];
     part[(d0 + tl) * ntiles + blockIdx.x] = (double)t;
@@ -370,24 +372,28 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
     cudaGetDevice(&dev);
     int smax = 0;
     cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    size_t budget = (size_t)smax - 4096;
+    // two CTAs per SM: each gets half of the SM's shared memory
+    int smsm = 0;
+    cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    size_t budget = std::min((size_t)smax, (size_t)smsm / 2) - 4096;
     int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, o.nch, budget / (2 * (size_t)rowcap)});
     if (cc >= 1) {
       size_t smem = 2 * (size_t)cc * rowcap;
-      dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
       const int group = (int)(255.0 / o.max_value());
       if (group >= 2) {
-        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<true>,
+        dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB8 - 1) / DD_DB8));
+        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<true, DD_DB8>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_dedisp_u8<true><<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns, o.nch,
-                                                      d_delays, ntrials, n, d_out, ldo, d_part,
-                                                      ntiles, cc, rowcap, group, d_err);
+        k_dedisp_u8<true, DD_DB8><<<grid, DD_NT, smem, st>>>(
+            o.samples.as<uint8_t>(), o.ld, o.ns, o.nch, d_delays, ntrials, n, d_out, ldo, d_part,
+            ntiles, cc, rowcap, group, d_err);
       } else {
-        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false>,
+        dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
+        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false, DD_DB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_dedisp_u8<false><<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns,
-                                                       o.nch, d_delays, ntrials, n, d_out, ldo,
-                                                       d_part, ntiles, cc, rowcap, 1, d_err);
+        k_dedisp_u8<false, DD_DB><<<grid, DD_NT, smem, st>>>(
+            o.samples.as<uint8_t>(), o.ld, o.ns, o.nch, d_delays, ntrials, n, d_out, ldo, d_part,
+            ntiles, cc, rowcap, 1, d_err);
       }
       PSR_CUDA(cudaGetLastError());
       k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles,

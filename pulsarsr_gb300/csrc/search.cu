@@ -220,9 +220,10 @@ int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
     set_error("invalid dedispersion input: delay exceeds observation");
     return PSR_EDEDISPERSE;
   }
-  // Widest delay spread of any channel inside a block of 8 consecutive trials.
+  // Widest delay spread of any channel over any 8 consecutive trials (an
+  // upper bound for every trial block of at most 8, whatever its alignment).
   max_spread = 0;
-  for (uint64_t b = 0; b < ntrials; b += 8)
+  for (uint64_t b = 0; b < ntrials; ++b)
     for (uint64_t c = 0; c < o.nch; ++c) {
       uint32_t lo = 0xffffffffu, hi = 0;
       for (uint64_t i = b; i < std::min<uint64_t>(b + 8, ntrials); ++i) {
