@@ -322,26 +322,37 @@ __global__ void __launch_bounds__(SC_NT)
     // The window is local chunks threadIdx.x .. threadIdx.x + 4 (chunks
     // b-2..b+2), each sorted and padded with sentinels above every value.
     const uint32_t *w = ch + threadIdx.x * SC_STRIDE;
-    // Lower bound: y = min_i A_i[r/5].  Every chunk holds at most r/5
-    // elements below y, so at most r elements of the window are below y and
-    // the rank-r element is >= y; those elements are skipped.
-    const int q = min(r / 5, 63);
-    uint32_t y = 0xffffffffu;
+    // Rank-bound skips: with p_d elements of chunk d already known to lie
+    // below the target and rr = r - sum(p_d), let y = min_d A_d[p_d + rr/5].
+    // Each chunk has at most rr/5 unskipped elements below y, so at most rr
+    // elements below y remain and the rank-r element is >= y: skip them.
+    // Every round shrinks rr geometrically; a short merge walk finishes.
+    int p[5] = {0, 0, 0, 0, 0};
+    int rr = r;
+    for (int round = 0; round < 6; ++round) {
+      const int q = rr / 5;
+      if (q == 0) break;
+      uint32_t y = 0xffffffffu;
 #pragma unroll
-    for (int d = 0; d < 5; ++d) y = min(y, w[d * SC_STRIDE + q]);
-    int p[5];
-    int skipped = 0;
+      for (int d = 0; d < 5; ++d)
+        if (p[d] + q < 64) y = min(y, w[d * SC_STRIDE + p[d] + q]);
+      if (y == 0u) break;
+      int adv = 0;
 #pragma unroll
-    for (int d = 0; d < 5; ++d) {
-      p[d] = y == 0u ? 0 : count_le64(w + d * SC_STRIDE, y - 1u);  // elements < y
-      skipped += p[d];
+      for (int d = 0; d < 5; ++d) {
+        const int np = count_le64(w + d * SC_STRIDE, y - 1u);  // elements < y
+        adv += np - p[d];
+        p[d] = np;
+      }
+      rr -= adv;
+      if (adv == 0) break;
     }
-    // 5-way merge walk over the rest: advance the smallest head r - skipped
-    // times; the smallest head is then the rank-r element.
+    // 5-way merge walk over the rest: advance the smallest head rr times; the
+    // smallest head is then the rank-r element.
     uint32_t hd[5];
 #pragma unroll
-    for (int d = 0; d < 5; ++d) hd[d] = w[d * SC_STRIDE + p[d]];
-    for (int step = skipped; step < r; ++step) {
+    for (int d = 0; d < 5; ++d) hd[d] = p[d] < 64 ? w[d * SC_STRIDE + p[d]] : 0xffffffffu;
+    for (int step = 0; step < rr; ++step) {
       uint32_t m = hd[0];
       int am = 0;
 #pragma unroll

@@ -73,16 +73,26 @@ __device__ __forceinline__ float fkey_inv(uint32_t k) {
 
 // Block-wide exact selection of the element of rank r (ascending) among n
 // keys key(i); top_shift is the shift of the highest non-constant digit.
+// Each warp counts digits in its own histogram (hist holds 32 x 256 slots),
+// so few-valued data (4-bit samples) does not serialise on a handful of bins.
 template <class KeyFn>
 __device__ uint32_t block_select(KeyFn key, uint64_t n, uint64_t r, int top_shift,
                                  unsigned *hist, uint32_t *bcast) {
+  const int nw = (int)(blockDim.x + 31) / 32;
+  unsigned *mine = hist + (threadIdx.x >> 5) * 256;
   uint32_t prefix = 0, mask = 0;
   for (int shift = top_shift; shift >= 0; shift -= 8) {
-    for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[d] = 0;
+    for (int d = threadIdx.x; d < nw * 256; d += blockDim.x) hist[d] = 0;
     __syncthreads();
     for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
       uint32_t k = key(i);
-      if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+      if ((k & mask) == prefix) atomicAdd(&mine[(k >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+      unsigned t = 0;
+      for (int w = 0; w < nw; ++w) t += hist[w * 256 + d];
+      hist[d] = t;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -111,7 +121,7 @@ __device__ uint32_t block_select(KeyFn key, uint64_t n, uint64_t r, int top_shif
 }
 
 __global__ void k_median_f32(const float *__restrict__ v, uint64_t n, float *out) {
-  __shared__ unsigned hist[256];
+  __shared__ unsigned hist[32 * 256];
   __shared__ uint32_t bc[3];
   if (n == 0) {
     if (threadIdx.x == 0) *out = 0.0f;
@@ -125,7 +135,7 @@ __global__ void k_median_f32(const float *__restrict__ v, uint64_t n, float *out
 template <class T>
 __global__ void k_chan_median(const T *__restrict__ s, uint64_t ns, uint64_t ld,
                               float *__restrict__ med) {
-  __shared__ unsigned hist[256];
+  __shared__ unsigned hist[32 * 256];
   __shared__ uint32_t bc[3];
   const T *row = s + (uint64_t)blockIdx.x * ld;
   uint32_t k;
@@ -285,7 +295,7 @@ __global__ void k_channel_decide(const float *means, const float *vars, uint64_t
                                  float threshold, float *scratch, unsigned char *f1,
                                  unsigned char *f2, unsigned char *chbad,
                                  unsigned long long *active) {
-  __shared__ unsigned hist[256];
+  __shared__ unsigned hist[32 * 256];
   __shared__ uint32_t bc[3];
   block_outliers(means, nch, threshold, scratch, f1, hist, bc);
   block_outliers(vars, nch, threshold, scratch, f2, hist, bc);
@@ -316,7 +326,7 @@ __global__ void k_block_means(const float *bsum, const unsigned char *chbad, uin
 
 __global__ void k_block_decide(const float *bmeans, uint64_t blocks_n, float threshold,
                                float *scratch, unsigned char *blkbad) {
-  __shared__ unsigned hist[256];
+  __shared__ unsigned hist[32 * 256];
   __shared__ uint32_t bc[3];
   block_outliers(bmeans, blocks_n, threshold, scratch, blkbad, hist, bc);
 }
