@@ -15,9 +15,9 @@
 //   Sub-FFT of size L: Stockham autosort stages with radices
 //   [16]*(q/4) + [2|4|8]; DFT_8 = 2x4 and DFT_16 = 4x4 four-step with the
 //   internal twiddles W_R^(n2*k1).
-// A CTA transforms C columns held in shared memory as [position][C+1]
-// (padding keeps both the row-wise global loads and the Stockham accesses
-// free of bank conflicts).  Every size is a template parameter, so all index
+// A CTA transforms C columns held in shared memory position-major with one
+// padding slot every 16 (free of bank conflicts for the row-wise global
+// loads, every Stockham access and the drains).  Every size is a template parameter, so all index
 // arithmetic reduces to shifts and masks; each thread owns exactly one
 // radix-16 butterfly per stage.  Stages are in place: every thread loads its
 // inputs, the block synchronises, then stores.
@@ -39,6 +39,19 @@ __host__ __device__ constexpr int cols_for(int L) {
 }
 __host__ __device__ constexpr int threads_for(int L, int C) {
   return ((L / 16) * C < 32 ? 32 : (L / 16) * C);
+}
+
+// Shared-memory slot of (position, column) for C columns: the linear index
+// e = pos*C + col padded by one slot every 16 (conflict-free for the fill,
+// every Stockham load/store pattern and the drains of both passes).
+template <int C>
+__device__ __forceinline__ int lay(int pos, int col) {
+  const int e = pos * C + col;
+  return e + (e >> 4);
+}
+template <int L, int C>
+__host__ __device__ constexpr int lay_slots() {
+  return L * C + (L * C) / 16 + 1;
 }
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
@@ -140,7 +153,6 @@ __device__ __forceinline__ void dftR(float2 *v, const float2 *Wl) {
 // C columns of length L; NT threads, each owning 16/R butterflies.
 template <int R, int L, int C, int NT, int Ns>
 __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
-  constexpr int S = C + 1;
   constexpr int nb = L / R;
   constexpr int total = nb * C;
   constexpr int BPT = (total + NT - 1) / NT;
@@ -151,7 +163,7 @@ __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
     if (total % NT == 0 || w < total) {
       const int col = w % C, j = w / C;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[i][r] = sm[(j + r * nb) * S + col];
+      for (int r = 0; r < R; ++r) v[i][r] = sm[lay<C>(j + r * nb, col)];
       if constexpr (Ns > 1) {
         const int k = j % Ns;
         if (k != 0) {
@@ -170,7 +182,7 @@ __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
       const int col = w % C, j = w / C;
       const int base = (j / Ns) * Ns * R + j % Ns;
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[(base + r * Ns) * S + col] = v[i][r];
+      for (int r = 0; r < R; ++r) sm[lay<C>(base + r * Ns, col)] = v[i][r];
     }
   }
   __syncthreads();
@@ -235,20 +247,26 @@ struct Acc2 {
     hi = s;
     lo = __fadd_rn(lo, err);
   }
-  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
+// Block total of the per-thread (hi, lo) pairs: TwoSum merges across the
+// warp in f32, f64 only for the final per-warp pairs (thread 0).
 template <int NT>
-__device__ __forceinline__ void block_sum_store(double acc, double *dst) {
-  __shared__ double red[NT / 32 > 0 ? NT / 32 : 1];
+__device__ __forceinline__ void block_sum_store(Acc2 acc, double *dst) {
+  __shared__ float2 red[NT / 32 > 0 ? NT / 32 : 1];
 #pragma unroll
-  for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  for (int o = 16; o; o >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, acc.hi, o);
+    const float ol = __shfl_down_sync(0xffffffffu, acc.lo, o);
+    acc.add(oh);
+    acc.lo = __fadd_rn(acc.lo, ol);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_float2(acc.hi, acc.lo);
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
 #pragma unroll
-    for (int w = 0; w < NT / 32; ++w) t += red[w];
+    for (int w = 0; w < NT / 32; ++w) t += (double)red[w].x + (double)red[w].y;
     *dst = t;
   }
 }
@@ -263,22 +281,23 @@ __global__ void __launch_bounds__(threads_for(M, 1))
   constexpr int NT = threads_for(M, 1);
   extern __shared__ float2 dyn[];
   float2 *Wl = dyn;      // M entries
-  float2 *sm = dyn + M;  // M x 2 (C = 1, S = 2)
+  float2 *sm = dyn + M;  // lay_slots<M, 1>() entries
   const uint64_t trial = blockIdx.x;
   const float *row = series + trial * lds;
   const float mean = means[trial];
   build_wl<M>(Wl, N, Q, lq);
-  for (int n = threadIdx.x; n < M; n += NT) sm[n * 2] = load_z(row, len, (uint64_t)n, mean);
+  for (int n = threadIdx.x; n < M; n += NT) sm[lay<1>(n, 0)] = load_z(row, len, (uint64_t)n, mean);
   __syncthreads();
   subfft<M, 1, NT>(sm, Wl);
   Acc2 acc;
   float *out = power + trial * ldp;
   for (int k = threadIdx.x; k <= M; k += NT) {
-    const float p = post_power(sm[(k % M) * 2], sm[((M - k) % M) * 2], twN(Q, (uint32_t)k, lq));
+    const float p =
+        post_power(sm[lay<1>(k % M, 0)], sm[lay<1>((M - k) % M, 0)], twN(Q, (uint32_t)k, lq));
     out[k] = p;
     acc.add(p);
   }
-  block_sum_store<NT>(acc.value(), psum + trial);
+  block_sum_store<NT>(acc, psum + trial);
 }
 
 // Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
@@ -286,12 +305,12 @@ template <int M1, int M2>
 __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
     k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
                 const float *__restrict__ means, const float2 *__restrict__ Q, int lq,
-                uint32_t N, float2 *__restrict__ work) {
-  constexpr int C = cols_for(M1), S = C + 1, NT = threads_for(M1, C);
+                uint32_t N, const float2 *__restrict__ tw1, float2 *__restrict__ work) {
+  constexpr int C = cols_for(M1), NT = threads_for(M1, C);
   constexpr uint32_t M = (uint32_t)M1 * M2;
   extern __shared__ float2 dyn[];
   float2 *Wl = dyn;       // M1 entries
-  float2 *sm = dyn + M1;  // M1 x (C+1)
+  float2 *sm = dyn + M1;  // lay_slots<M1, C>() entries
   const uint64_t trial = blockIdx.y;
   const uint32_t n2_0 = blockIdx.x * (uint32_t)C;
   const float *row = series + trial * lds;
@@ -312,21 +331,22 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
       const int idx = base + u * NT + (int)threadIdx.x;
-      if (idx < total) sm[(idx / C) * S + (idx % C)] = v[u];
+      if (idx < total) sm[lay<C>(idx / C, idx % C)] = v[u];
     }
   }
   __syncthreads();
   subfft<M1, C, NT>(sm, Wl);
   float2 *out = work + trial * (uint64_t)M;
-  // Twiddle loads for LB outputs are issued before any is consumed.
+  // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 + n2]
+  // (values identical to the quarter-table lookup), so these reads coalesce.
 #pragma unroll 1
   for (int base = 0; base < total; base += LB * NT) {
     float2 w[LB];
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
       const int idx = base + u * NT + (int)threadIdx.x;
-      const uint32_t e = (n2_0 + (uint32_t)(idx % C)) * (uint32_t)(idx / C);
-      w[u] = (idx < total && e != 0) ? twN(Q, 2u * e, lq) : make_float2(1.0f, 0.0f);
+      w[u] = idx < total ? __ldg(&tw1[(uint64_t)(idx / C) * M2 + n2_0 + (idx % C)])
+                         : make_float2(1.0f, 0.0f);
     }
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
@@ -334,7 +354,7 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
       if (idx < total) {
         const int col = idx % C, k1 = idx / C;
         const uint32_t n2 = n2_0 + (uint32_t)col;
-        float2 v = sm[k1 * S + col];
+        float2 v = sm[lay<C>(k1, col)];
         if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
         out[(uint64_t)k1 * M2 + n2] = v;
       }
@@ -351,11 +371,11 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
     k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q, int lq,
                 uint32_t N, float *__restrict__ power, uint64_t ldp, double *__restrict__ psum,
                 uint32_t ngroups) {
-  constexpr int C = cols_for(M2), S = C + 1, NT = threads_for(M2, C), H = C / 2;
+  constexpr int C = cols_for(M2), NT = threads_for(M2, C), H = C / 2;
   constexpr uint32_t M = (uint32_t)M1 * M2;
   extern __shared__ float2 dyn[];
   float2 *Wl = dyn;       // M2 entries
-  float2 *sm = dyn + M2;  // M2 x (C+1)
+  float2 *sm = dyn + M2;  // lay_slots<M2, C>() entries
   const uint64_t trial = blockIdx.y;
   const uint32_t g = blockIdx.x;
   const float2 *in = work + trial * (uint64_t)M;
@@ -386,7 +406,7 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
 #pragma unroll
     for (int u = 0; u < LB; ++u) {
       const int idx = base + u * NT + (int)threadIdx.x;
-      if (idx < total) sm[(idx % M2) * S + idx / M2] = v[u];
+      if (idx < total) sm[lay<C>(idx % M2, idx / M2)] = v[u];
     }
   }
   __syncthreads();
@@ -403,12 +423,12 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
         k = M1 / 2 + M1 * k2;
         mk2 = M2 - 1 - k2;
       }
-      const float p = post_power(sm[k2 * S + which], sm[mk2 * S + which], twN(Q, k, lq));
+      const float p = post_power(sm[lay<C>(k2, which)], sm[lay<C>(mk2, which)], twN(Q, k, lq));
       out[k] = p;
       acc.add(p);
     }
     if (threadIdx.x == 0) {  // k = M (Nyquist): a = Z[0], b = conj(Z[0])
-      const float p = post_power(sm[0], sm[0], twN(Q, M, lq));
+      const float p = post_power(sm[lay<C>(0, 0)], sm[lay<C>(0, 0)], twN(Q, M, lq));
       out[M] = p;
       acc.add(p);
     }
@@ -434,8 +454,8 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
           const uint32_t k2 = (uint32_t)(idx / h);
           const uint32_t k = kb + (uint32_t)p + M1 * k2;
           const uint32_t mk = M - k;
-          const float2 zk = sm[k2 * S + p];
-          const float2 zm = sm[(M2 - 1 - k2) * S + h + p];
+          const float2 zk = sm[lay<C>(k2, p)];
+          const float2 zm = sm[lay<C>(M2 - 1 - k2, h + p)];
           const float pk = post_power(zk, zm, wk[u]);
           const float pm = post_power(zm, zk, wm[u]);
           out[k] = pk;
@@ -446,7 +466,7 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
       }
     }
   }
-  block_sum_store<NT>(acc.value(), psum + trial * ngroups + g);
+  block_sum_store<NT>(acc, psum + trial * ngroups + g);
 }
 
 struct FftArgs {
@@ -456,6 +476,7 @@ struct FftArgs {
   const float2 *Q;
   int lq;
   uint32_t N;
+  const float2 *tw1;
   uint64_t ntrials;
   float2 *work;
   float *power;
@@ -466,7 +487,7 @@ struct FftArgs {
 
 template <int M>
 int run_small(const FftArgs &a) {
-  const size_t smem = (size_t)M * sizeof(float2) * 3;
+  const size_t smem = (size_t)(M + lay_slots<M, 1>()) * sizeof(float2);
   PSR_CUDA(cudaFuncSetAttribute(k_fft_small<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   k_fft_small<M><<<(unsigned)a.ntrials, threads_for(M, 1), smem, a.st>>>(
@@ -479,17 +500,17 @@ template <int M1, int M2>
 int run_four_step(const FftArgs &a) {
   {
     constexpr int C = cols_for(M1);
-    const size_t smem = (size_t)M1 * sizeof(float2) * (1 + C + 1);
+    const size_t smem = (size_t)(M1 + lay_slots<M1, C>()) * sizeof(float2);
     PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     dim3 grid((unsigned)(M2 / C), (unsigned)a.ntrials);
     k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(a.series, a.lds, a.len, a.means,
-                                                                    a.Q, a.lq, a.N, a.work);
+                                                                    a.Q, a.lq, a.N, a.tw1, a.work);
     PSR_CUDA(cudaGetLastError());
   }
   {
     constexpr int C = cols_for(M2);
-    const size_t smem = (size_t)M2 * sizeof(float2) * (1 + C + 1);
+    const size_t smem = (size_t)(M2 + lay_slots<M2, C>()) * sizeof(float2);
     PSR_CUDA(cudaFuncSetAttribute(k_fft_pass2<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     const uint32_t ng = 1 + ((uint32_t)M1 / 2 - 1 + C / 2 - 1) / (C / 2);
@@ -537,6 +558,27 @@ int FftPlan::init(uint64_t series_len, cudaStream_t st) {
   for (uint64_t r = n8 + 1; r <= n4; ++r) q[r] = make_float2(q[n4 - r].y, q[n4 - r].x);
   PSR_TRY(Q.ensure(q.size() * sizeof(float2)));
   PSR_CUDA(cudaMemcpyAsync(Q.p, q.data(), q.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+  if (m > 12) {
+    // Tw1[k1*M2 + n2] = W_N^(2*n2*k1) = W_M^(n2*k1), from the same quarter table
+    // and quadrant rule as the device lookup.
+    std::vector<float2> t((size_t)M);
+    for (uint64_t k1 = 0; k1 < M1; ++k1)
+      for (uint64_t n2 = 0; n2 < M2; ++n2) {
+        const uint64_t x = 2 * n2 * k1, qd = x / n4, r = x % n4;
+        const float2 v = q[r];
+        float2 w;
+        switch (qd & 3) {
+          case 0: w = make_float2(v.x, -v.y); break;
+          case 1: w = make_float2(-v.y, -v.x); break;
+          case 2: w = make_float2(-v.x, v.y); break;
+          default: w = make_float2(v.y, v.x); break;
+        }
+        t[k1 * M2 + n2] = w;
+      }
+    PSR_TRY(tw1.ensure(t.size() * sizeof(float2)));
+    PSR_CUDA(cudaMemcpyAsync(tw1.p, t.data(), t.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                             st));
+  }
   PSR_CUDA(cudaStreamSynchronize(st));
   return PSR_OK;
 }
@@ -546,8 +588,8 @@ int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
                         uint64_t ldp, double *d_psum, cudaStream_t st) {
   int lq = 0;
   while ((1ull << lq) < p.N / 4) ++lq;
-  FftArgs a{d_series, lds,     p.len,   d_means, p.Q.as<float2>(), lq, (uint32_t)p.N, ntrials,
-            d_work,   d_power, ldp,     d_psum, st};
+  FftArgs a{d_series, lds,          p.len,   d_means, p.Q.as<float2>(), lq, (uint32_t)p.N,
+            p.tw1.as<float2>(), ntrials, d_work, d_power, ldp, d_psum, st};
   switch (p.m) {
     case 1: return run_small<2>(a);
     case 2: return run_small<4>(a);

@@ -135,6 +135,7 @@ struct FftPlan {
   int m = 0;          // log2 M
   uint64_t M1 = 0, M2 = 0;
   DevBuf Q;           // quarter twiddle table, N/4 + 1 float2
+  DevBuf tw1;         // pass-1 twiddles W_M^(n2*k1) laid out [k1][n2]
   int init(uint64_t series_len, cudaStream_t st);
   uint64_t bins() const { return M + 1; }
   uint64_t pass2_ctas() const;
