@@ -143,6 +143,32 @@ int psr_dedisperse_trials(const psr_fb *fb, const double *trials,
  * mean removal, zero padding to N = 2*next_pow2(len), real FFT, |X|^2.
  * out holds N/2 + 1 floats. */
 int psr_raw_power(const float *series, uint64_t len, float *out);
+/* psr_raw_power without any device allocation.  No counterpart in the
+ * reference (a CPU program has no device memory to allocate).
+ *
+ * For callers that must not allocate device memory while they run: a process
+ * whose device memory is handed out up front to another pool (a framework's
+ * caching allocator, an MPS client under a memory limit), or a real-time
+ * caller that cannot take the device-wide synchronisation of cudaFree while
+ * other streams are busy.  psr_raw_power allocates and frees its buffers on
+ * every call; this entry point computes the same spectrum, bit for bit, with
+ * the same kernels, using one fixed device array of about 28 MiB reserved
+ * when the library's module is loaded on a device.
+ *
+ *   - len must be at most PSR_RAW_POWER_NOALLOC_MAX_LEN samples; longer
+ *     series return PSR_ECAPACITY (use psr_raw_power for them).
+ *   - series and out are host buffers as in psr_raw_power (out: N/2 + 1
+ *     floats); stream is a cudaStream_t (NULL: the default stream).  The call
+ *     returns after synchronising that stream.
+ *   - The first call on a device (the one current on the calling thread)
+ *     looks up the array's address with cudaGetSymbolAddress; make that first
+ *     call before any stream capture on the device.
+ *   - Every call on a device shares the one array (series, work, spectrum and
+ *     twiddle tables, which are kept between calls of the same FFT size), so
+ *     calls that overlap in time on one device, from several threads or
+ *     streams, race and corrupt each other's results: serialise them. */
+#define PSR_RAW_POWER_NOALLOC_MAX_LEN (1u << 20)
+int psr_raw_power_noalloc(const float *series, uint64_t len, float *out, void *stream);
 /* search::periodicity (search/src/lib.rs:33-145) on one host series. */
 int psr_periodicity(const float *series, uint64_t len, double tsamp, double dm,
                     const psr_search_config *cfg, psr_candidate *out,

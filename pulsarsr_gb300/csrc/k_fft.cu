@@ -621,4 +621,41 @@ int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
   }
 }
 
+int launch_raw_power_tables(uint64_t len, uint64_t N, const float2 *d_Q, const float2 *d_tw1,
+                            const float *d_series, uint64_t lds, const float *d_means,
+                            uint64_t ntrials, float2 *d_work, float *d_power, uint64_t ldp,
+                            double *d_psum, cudaStream_t st) {
+  int lq = 0;
+  while ((1ull << lq) < N / 4) ++lq;
+  int m = 0;
+  while ((1ull << m) < N / 2) ++m;
+  FftArgs a{d_series, lds, len, d_means, d_Q, lq, (uint32_t)N, d_tw1, ntrials, d_work, d_power,
+            ldp, d_psum, st};
+  switch (m) {
+    case 1: return run_small<2>(a);
+    case 2: return run_small<4>(a);
+    case 3: return run_small<8>(a);
+    case 4: return run_small<16>(a);
+    case 5: return run_small<32>(a);
+    case 6: return run_small<64>(a);
+    case 7: return run_small<128>(a);
+    case 8: return run_small<256>(a);
+    case 9: return run_small<512>(a);
+    case 10: return run_small<1024>(a);
+    case 11: return run_small<2048>(a);
+    case 12: return run_small<4096>(a);
+    case 13: return run_four_step<128, 64>(a);
+    case 14: return run_four_step<128, 128>(a);
+    case 15: return run_four_step<256, 128>(a);
+    case 16: return run_four_step<256, 256>(a);
+    case 17: return run_four_step<512, 256>(a);
+    case 18: return run_four_step<512, 512>(a);
+    case 19: return run_four_step<1024, 512>(a);
+    case 20: return run_four_step<1024, 1024>(a);
+    default:
+      set_error("periodicity: unsupported FFT size");
+      return PSR_EINVAL;
+  }
+}
+
 }  // namespace psr

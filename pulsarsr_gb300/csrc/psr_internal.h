@@ -182,6 +182,12 @@ uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
 int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
                         const float *d_means, uint64_t ntrials, float2 *d_work, float *d_power,
                         uint64_t ldp, double *d_psum, cudaStream_t st);
+// The same kernels with caller-owned twiddle tables (FftPlan's Q and tw1
+// layouts for real FFT size N = 2 * next_pow2(len)); N <= 2^21.
+int launch_raw_power_tables(uint64_t len, uint64_t N, const float2 *d_Q, const float2 *d_tw1,
+                            const float *d_series, uint64_t lds, const float *d_means,
+                            uint64_t ntrials, float2 *d_work, float *d_power, uint64_t ldp,
+                            double *d_psum, cudaStream_t st);
 
 // ------------------------------------------------------------- fold
 // Host statistics of a folded profile (fold/src/lib.rs:39-79).
