@@ -199,6 +199,93 @@ int psr_measure(const float *x, uint64_t n, uint64_t offset, double tsamp,
                 double period, uint64_t start_bin, uint64_t width_bins,
                 uint64_t bins, psr_measurement *out);
 
+/* ------------------------------------------------------ confirmation */
+/* confirmation::Rules (search/src/confirmation.rs:17-40); the version string
+ * is always "split-confirm-v1". */
+typedef struct {
+  double minimum_validation_snr;
+  double minimum_part_snr;
+  uint64_t minimum_time_parts;
+  uint64_t minimum_subbands;
+  double minimum_dm_contrast;
+  double minimum_dispersion_widths;
+  double maximum_zero_dm_spectral_ratio;
+} psr_rules;
+/* Rules::default() (confirmation.rs:27-39). */
+void psr_rules_default(psr_rules *out);
+
+/* confirmation::Window (confirmation.rs:41-46). */
+typedef struct {
+  uint64_t start_bin;
+  uint64_t width_bins;
+  uint64_t bins;
+} psr_window;
+
+/* confirmation::group (confirmation.rs:177-199), host: candidates sorted by
+ * score (stable, descending) and assigned to harmonic families.  order[k] is
+ * the input index of the k-th candidate in score order and family[k] its
+ * family (-1 when it started no family because `limit` families exist);
+ * the leader of family f is the first k with family[k] == f. */
+int psr_group(const psr_candidate *in, uint64_t n, double resolution_hz,
+              uint64_t limit, uint64_t *order, int64_t *family,
+              uint64_t *nfamilies);
+
+/* Scalar fields of confirmation::ConfirmedCandidate (confirmation.rs:70-91).
+ * rejection_mask bit i is set for reason i in the order the reference checks
+ * them: 0 held-out SNR, 1 time segments, 2 subbands, 3 zero-DM control,
+ * 4 dispersion sweep, 5 zero-DM spectral ratio. */
+typedef struct {
+  psr_candidate candidate;
+  double refined_dm;
+  psr_profile_stats profile;
+  psr_window window;
+  psr_measurement validation;
+  psr_measurement zero_dm_validation;
+  double zero_dm_period_s;
+  psr_window zero_dm_window;
+  double dm_contrast;
+  double dispersion_widths;
+  double zero_dm_related_spectral_ratio;
+  psr_measurement time_parts[4];
+  psr_measurement subbands[4];
+  uint64_t harmonic_members;
+  int32_t accepted;
+  uint32_t rejection_mask;
+} psr_confirmed;
+
+/* confirmation::Outcome (confirmation.rs:93-101), owned by the library. */
+typedef struct psr_outcome psr_outcome;
+typedef struct {
+  uint64_t discovery_samples;
+  uint64_t validation_start_sample;
+  uint64_t validation_samples;
+  uint64_t common_samples;
+  uint64_t trial_count;
+  uint64_t candidates;
+} psr_outcome_info;
+
+/* confirmation::analyze (confirmation.rs:203-496) on a device filterbank
+ * (after psr_rfi_mask where the CLI masks): the zero-DM control search,
+ * harmonic families, and for each family the frequency refinement, the
+ * half-step DM grid, the held-out validation, the zero-DM control, time
+ * parts, subbands, per-channel discovery profiles and the DM response, all
+ * computed on the device.  rules NULL means Rules::default().  Errors are the
+ * reference's dedisperse::Error texts (PSR_EDEDISPERSE). */
+int psr_analyze(const psr_fb *fb, const double *trials, uint64_t ntrials,
+                const psr_candidate *generated, uint64_t ngenerated,
+                uint64_t limit, uint64_t bins, const psr_rules *rules,
+                psr_outcome **out);
+int psr_outcome_info_get(const psr_outcome *o, psr_outcome_info *out);
+/* Candidate i; profile_bins/profile_counts (bins entries) may be NULL. */
+int psr_outcome_candidate(const psr_outcome *o, uint64_t i, psr_confirmed *out,
+                          float *profile_bins, uint64_t *profile_counts);
+/* The Outcome as serde_json writes it (field order and number format of the
+ * reference), compact or pretty.  Copies at most len bytes including the
+ * NUL; returns the full length without the NUL. */
+uint64_t psr_outcome_json(const psr_outcome *o, int pretty, char *buf,
+                          uint64_t len);
+void psr_outcome_free(psr_outcome *o);
+
 /* ----------------------------------------------------------- session */
 /* A whole search of one observation shape kept resident on the device:
  * packed payload -> unpack -> RFI mask -> trial loop -> per-trial candidate
@@ -230,6 +317,10 @@ int psr_session_mask(psr_session *s, uint64_t *channels, uint64_t *nchannels_bad
  * runs since the last reset. */
 int psr_session_set_profiling(psr_session *s, int enable);
 int psr_session_stage_times(psr_session *s, double *ms, uint64_t *launches, int reset);
+/* confirmation::analyze over the last run's candidates (the psr search
+ * command, cli/src/main.rs:474-478), on the session's masked observation. */
+int psr_session_analyze(psr_session *s, uint64_t limit, uint64_t bins,
+                        const psr_rules *rules, psr_outcome **out);
 /* Device copy of the packed payload buffer (for device-resident timing). */
 void *psr_session_payload_device(psr_session *s);
 /* The session's CUDA stream (cudaStream_t), for event timing. */

@@ -65,6 +65,7 @@ def lib() -> C.CDLL:
         _lib.orc_last_error.restype = C.c_char_p
         _lib.orc_median.restype = C.c_float
         _lib.orc_psr_search_json.restype = C.c_void_p
+        _lib.orc_analyze_json.restype = C.c_void_p
     return _lib
 
 
@@ -287,6 +288,27 @@ def psr_search(data: bytes, dm_min=0.0, dm_max=500.0, dm_step=None, min_hz=15.0,
         C.c_int(1 if no_rfi else 0), _ptr(b, C.c_double) if b.size else None,
         C.c_uint64(b.size // 2), C.c_int64(-1 if max_samples is None else max_samples),
         C.c_int(threads))
+    if not ptr:
+        raise OracleError(lib().orc_last_error().decode())
+    try:
+        text = C.string_at(ptr).decode()
+    finally:
+        lib().orc_free(C.c_void_p(ptr))
+    return json.loads(text)
+
+
+def analyze(data: np.ndarray, freqs, tsamp: float, trials, generated, limit: int = 5,
+            bins: int = 64) -> dict:
+    """confirmation::analyze on masked channel-major data; the parsed Outcome."""
+    x = _f32(data)
+    nch, ns = x.shape
+    f = np.ascontiguousarray(freqs, dtype=np.float64)
+    t = np.ascontiguousarray(trials, dtype=np.float64)
+    g = np.ascontiguousarray(np.asarray(generated, dtype=CAND_DTYPE))
+    ptr = lib().orc_analyze_json(_ptr(x, C.c_float), C.c_uint64(nch), C.c_uint64(ns),
+                                 _ptr(f, C.c_double), C.c_double(tsamp), _ptr(t, C.c_double),
+                                 C.c_uint64(t.size), g.ctypes.data_as(C.c_void_p),
+                                 C.c_uint64(g.size), C.c_uint64(limit), C.c_uint64(bins))
     if not ptr:
         raise OracleError(lib().orc_last_error().decode())
     try:

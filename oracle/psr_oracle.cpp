@@ -1614,6 +1614,24 @@ char *orc_psr_search_json(const uint8_t *bytes, uint64_t len, double dm_min,
   return res;
 }
 
+// confirmation::analyze (confirmation.rs:203-496) alone, on already masked
+// channel-major data and a given candidate list; the Outcome JSON.
+char *orc_analyze_json(const float *data, uint64_t nchans, uint64_t nsamples,
+                       const double *freqs, double tsamp, const double *trials,
+                       uint64_t ntrials, const orc_candidate *generated, uint64_t ngenerated,
+                       uint64_t limit, uint64_t bins) {
+  std::vector<double> f(freqs, freqs + nchans), t(trials, trials + ntrials);
+  std::vector<Cand> gen(ngenerated);
+  for (uint64_t i = 0; i < ngenerated; ++i)
+    gen[i] = Cand{generated[i].frequency_hz, generated[i].period_s, generated[i].dm,
+                  generated[i].harmonics, generated[i].score};
+  Json j;
+  if (!analyze(data, nsamples, f, tsamp, t, gen, limit, bins, j)) return nullptr;
+  char *res = (char *)std::malloc(j.s.size() + 1);
+  std::memcpy(res, j.s.c_str(), j.s.size() + 1);
+  return res;
+}
+
 void orc_free(void *p) { std::free(p); }
 
 }  // extern "C"

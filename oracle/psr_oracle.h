@@ -129,6 +129,13 @@ int orc_search_trials(const float *data, uint64_t nchans, uint64_t nsamples,
                       const orc_config *cfg, int threads, uint64_t *counts,
                       orc_candidate *out, uint64_t cap, uint64_t *n_total);
 
+/* confirmation::analyze (search/src/confirmation.rs:203-496) on masked
+ * channel-major data and a candidate list; malloc'd Outcome JSON (orc_free). */
+char *orc_analyze_json(const float *data, uint64_t nchans, uint64_t nsamples,
+                       const double *freqs, double tsamp, const double *trials,
+                       uint64_t ntrials, const orc_candidate *generated,
+                       uint64_t ngenerated, uint64_t limit, uint64_t bins);
+
 /* Whole `psr search` (minus plots, hashing and file output) on the bytes of a
  * SIGPROC file; returns a malloc'd JSON document (free with orc_free). */
 char *orc_psr_search_json(const uint8_t *bytes, uint64_t len, double dm_min,

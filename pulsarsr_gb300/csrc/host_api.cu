@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "analyze.h"
 #include "psr_internal.h"
 #include "search.h"
 
@@ -294,6 +295,7 @@ struct psr_session {
   uint64_t rfi_block = 0;
   float rfi_threshold = 8.0f;
   SearchEngine eng;
+  std::vector<double> trials;
   DevBuf errbuf;
   bool have_run = false;
   // unpack / rfi timing (the engine times its own stages)
@@ -661,6 +663,22 @@ int psr_search_trials(const psr_fb *fb, const double *trials, uint64_t ntrials,
   return e.collect(st, counts, out, cap, n_total);
 }
 
+int psr_analyze(const psr_fb *fb, const double *trials, uint64_t ntrials,
+                const psr_candidate *generated, uint64_t ngenerated, uint64_t limit,
+                uint64_t bins, const psr_rules *rules, psr_outcome **out) {
+  if (!fb || !out || (!generated && ngenerated)) {
+    set_error("analyze: null argument");
+    return PSR_EINVAL;
+  }
+  psr_rules r;
+  psr_rules_default(&r);
+  std::unique_ptr<psr_outcome> o(new psr_outcome());
+  PSR_TRY(analyze_obs(fb->o, trials, ntrials, generated, ngenerated, limit, bins,
+                      rules ? *rules : r, o->o, fb->stream.s));
+  *out = o.release();
+  return PSR_OK;
+}
+
 // search::sift (search/src/lib.rs:147-176).
 int psr_sift(const psr_candidate *in, uint64_t n, double res, uint64_t limit,
              int reject_dm_zero, psr_candidate *out, uint64_t *n_out) {
@@ -785,6 +803,7 @@ int psr_session_create(const psr_header *header, uint64_t nsamples, const double
   PSR_TRY(o.alloc());
   s->rfi_block = rfi_block_samples;
   s->rfi_threshold = rfi_threshold;
+  s->trials.assign(trials, trials + ntrials);
   PSR_TRY(s->eng.prepare(o, trials, ntrials, discovery, to_spec(cfg, header->tsamp),
                          s->stream.s));
   PSR_TRY(s->errbuf.ensure(8));
@@ -909,6 +928,30 @@ int psr_session_mask(psr_session *s, uint64_t *channels, uint64_t *nchannels_bad
 
 void *psr_session_payload_device(psr_session *s) { return s ? s->o.payload.p : nullptr; }
 void *psr_session_stream(psr_session *s) { return s ? (void *)s->stream.s : nullptr; }
+int psr_session_analyze(psr_session *s, uint64_t limit, uint64_t bins, const psr_rules *rules,
+                        psr_outcome **out) {
+  if (!s || !out) {
+    set_error("session_analyze: null argument");
+    return PSR_EINVAL;
+  }
+  if (!s->have_run) {
+    set_error("session_analyze: nothing has been run");
+    return PSR_EINVAL;
+  }
+  PSR_TRY(psr_session_sync(s));
+  uint64_t total = 0;
+  PSR_TRY(s->eng.collect(s->stream.s, nullptr, nullptr, 0, &total));
+  std::vector<psr_candidate> all(total);
+  PSR_TRY(s->eng.collect(s->stream.s, nullptr, all.data(), all.size(), &total));
+  psr_rules r;
+  psr_rules_default(&r);
+  std::unique_ptr<psr_outcome> o(new psr_outcome());
+  PSR_TRY(analyze_obs(s->o, s->trials.data(), s->trials.size(), all.data(), all.size(), limit,
+                      bins, rules ? *rules : r, o->o, s->stream.s));
+  *out = o.release();
+  return PSR_OK;
+}
+
 void psr_session_free(psr_session *s) { delete s; }
 
 }  // extern "C"

@@ -22,7 +22,7 @@ constexpr int FOLD_NT = 256;
 constexpr int FOLD_MAXBINS = 1024;
 
 __global__ void __launch_bounds__(FOLD_NT)
-    k_fold(const float *__restrict__ x, uint64_t n, double tsamp,
+    k_fold(const float *__restrict__ x, uint64_t xstride, uint64_t n, double tsamp,
            const double *__restrict__ periods, uint64_t bins, uint64_t offset,
            uint64_t per_cta, double *__restrict__ psums, unsigned long long *__restrict__ pcounts) {
   extern __shared__ unsigned char sm_raw[];
@@ -30,6 +30,7 @@ __global__ void __launch_bounds__(FOLD_NT)
   unsigned *c = reinterpret_cast<unsigned *>(s + bins);
   const uint64_t per = blockIdx.y;
   const double period = periods[per];
+  x += per * xstride;
   for (uint64_t b = threadIdx.x; b < bins; b += blockDim.x) {
     s[b] = 0.0;
     c[b] = 0;
@@ -71,10 +72,14 @@ __global__ void k_fold_reduce(const double *__restrict__ psums,
   counts[id] = cnt;
 }
 
-// Series mean and variance in f64 (fold/src/lib.rs:63-68).
-__global__ void k_series_moments(const float *__restrict__ x, uint64_t n, double *out) {
+// Series mean and variance in f64 (fold/src/lib.rs:63-68); one CTA per
+// series at x + blockIdx.x * xstride.
+__global__ void k_series_moments(const float *__restrict__ x, uint64_t xstride, uint64_t n,
+                                 double *out) {
   __shared__ double red[32];
   __shared__ double mean_s;
+  x += blockIdx.x * xstride;
+  out += 2 * blockIdx.x;
   double a = 0.0;
   for (uint64_t t = threadIdx.x; t < n; t += blockDim.x) a += (double)x[t];
   for (int o = 16; o; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
@@ -195,11 +200,20 @@ void profile_stats(const double *sums, const unsigned long long *cnts, uint64_t 
     for (uint64_t b = 0; b < bins; ++b) counts[b] = cnts[b];
 }
 
-// Fold one device series at nper periods; stats/values/counts are arrays of
-// nper entries (values/counts nper*bins).
 int fold_profiles(const float *d_x, uint64_t n, double tsamp, const double *periods,
                   uint64_t nper, uint64_t bins, uint64_t offset, psr_profile_stats *stats,
                   float *values, uint64_t *counts, cudaStream_t st) {
+  return fold_profiles_ex(d_x, 0, n, tsamp, periods, nper, bins, offset, stats, values, counts,
+                          st);
+}
+
+// Fold nper (series, period) pairs: series p starts at d_x + p * xstride
+// (xstride 0: one series at every period); stats/values/counts are arrays of
+// nper entries (values/counts nper*bins).
+int fold_profiles_ex(const float *d_x, uint64_t xstride, uint64_t n, double tsamp,
+                     const double *periods, uint64_t nper, uint64_t bins, uint64_t offset,
+                     psr_profile_stats *stats, float *values, uint64_t *counts,
+                     cudaStream_t st) {
   if (bins < 4 || bins > FOLD_MAXBINS || n == 0) {
     set_error("profile_at: 4 <= bins <= 1024 and a non-empty series are required");
     return PSR_EINVAL;
@@ -212,30 +226,34 @@ int fold_profiles(const float *d_x, uint64_t n, double tsamp, const double *peri
   PSR_TRY(pcounts.ensure(nper * nparts * bins * 8));
   PSR_TRY(sums.ensure(nper * bins * 8));
   PSR_TRY(cnts.ensure(nper * bins * 8));
-  PSR_TRY(mom.ensure(16));
+  const uint64_t nser = xstride ? nper : 1;
+  PSR_TRY(mom.ensure(16 * nser));
   PSR_CUDA(cudaMemcpyAsync(dper.p, periods, nper * 8, cudaMemcpyHostToDevice, st));
   const size_t smem = bins * (8 + 4);
   dim3 grid((unsigned)nparts, (unsigned)nper);
-  k_fold<<<grid, FOLD_NT, smem, st>>>(d_x, n, tsamp, dper.as<double>(), bins, offset, per_cta,
-                                      psums.as<double>(), pcounts.as<unsigned long long>());
+  k_fold<<<grid, FOLD_NT, smem, st>>>(d_x, xstride, n, tsamp, dper.as<double>(), bins, offset,
+                                      per_cta, psums.as<double>(),
+                                      pcounts.as<unsigned long long>());
   PSR_CUDA(cudaGetLastError());
   k_fold_reduce<<<(unsigned)((nper * bins + 255) / 256), 256, 0, st>>>(
       psums.as<double>(), pcounts.as<unsigned long long>(), nparts, bins, nper,
       sums.as<double>(), cnts.as<unsigned long long>());
-  k_series_moments<<<1, 1024, 0, st>>>(d_x, n, mom.as<double>());
+  k_series_moments<<<(unsigned)nser, 1024, 0, st>>>(d_x, xstride, n, mom.as<double>());
   PSR_CUDA(cudaGetLastError());
-  std::vector<double> hs(nper * bins), hm(2);
+  std::vector<double> hs(nper * bins), hm(2 * nser);
   std::vector<unsigned long long> hc(nper * bins);
   PSR_CUDA(cudaMemcpyAsync(hs.data(), sums.p, nper * bins * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaMemcpyAsync(hc.data(), cnts.p, nper * bins * 8, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaMemcpyAsync(hm.data(), mom.p, 16, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hm.data(), mom.p, 16 * nser, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
-  const double smean = hm[0] / (double)n;
-  const double svar = hm[1] / (double)n;
-  for (uint64_t p = 0; p < nper; ++p)
+  for (uint64_t p = 0; p < nper; ++p) {
+    const uint64_t m = xstride ? p : 0;
+    const double smean = hm[2 * m] / (double)n;
+    const double svar = hm[2 * m + 1] / (double)n;
     profile_stats(hs.data() + p * bins, hc.data() + p * bins, bins, smean, svar, periods[p],
                   &stats[p], values ? values + p * bins : nullptr,
                   counts ? counts + p * bins : nullptr);
+  }
   return PSR_OK;
 }
 
@@ -276,6 +294,158 @@ int measure_device(const float *d_x, uint64_t n, uint64_t offset, double tsamp, 
   out->snr = err > 1e-10 ? diff / err : 0.0;
   out->mean_difference = diff;
   out->standard_error = err;
+  return PSR_OK;
+}
+
+}  // namespace psr
+
+// ---------------------------------------------------------------------------
+// Per-channel discovery profiles and the DM response of
+// confirmation::analyze (search/src/confirmation.rs:391-433).
+namespace psr {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ double sample_as_f64(const T *row, uint64_t t) {
+  return (double)(float)row[t];
+}
+
+// fold::profile of every channel row over samples [0, n) at one period:
+// CTA (part, channel) accumulates its part of the row into shared bins.
+template <typename T>
+__global__ void __launch_bounds__(FOLD_NT)
+    k_fold_rows(const T *__restrict__ samples, uint64_t ld, uint64_t n, double tsamp,
+                double period, uint64_t bins, uint64_t per_cta, double *__restrict__ psums,
+                unsigned long long *__restrict__ pcounts) {
+  extern __shared__ unsigned char sm_raw[];
+  double *s = reinterpret_cast<double *>(sm_raw);
+  unsigned *c = reinterpret_cast<unsigned *>(s + bins);
+  const uint64_t ch = blockIdx.y;
+  const T *row = samples + ch * ld;
+  for (uint64_t b = threadIdx.x; b < bins; b += blockDim.x) {
+    s[b] = 0.0;
+    c[b] = 0;
+  }
+  __syncthreads();
+  const uint64_t t0 = (uint64_t)blockIdx.x * per_cta;
+  const uint64_t t1 = min(t0 + per_cta, n);
+  const double dbins = (double)bins;
+  for (uint64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    const double q = __ddiv_rn(__dmul_rn((double)t, tsamp), period);
+    uint64_t b = (uint64_t)__dmul_rn(__dsub_rn(q, trunc(q)), dbins);
+    if (b > bins - 1) b = bins - 1;
+    atomicAdd(&s[b], sample_as_f64(row, t));
+    atomicAdd(&c[b], 1u);
+  }
+  __syncthreads();
+  const uint64_t slot = (ch * gridDim.x + blockIdx.x) * bins;
+  for (uint64_t b = threadIdx.x; b < bins; b += blockDim.x) {
+    psums[slot + b] = s[b];
+    pcounts[slot + b] = c[b];
+  }
+}
+
+// comb[trial][b] = sum over channels (in channel order) of the linearly
+// interpolated, mean-removed channel profile shifted by delay*tsamp/period
+// bins; the f64 operations and their order follow confirmation.rs:403-413.
+// One CTA per trial; the channel shifts are computed once into shared memory.
+__global__ void k_dm_response(const float *__restrict__ chp, const double *__restrict__ chmean,
+                              const uint32_t *__restrict__ delays, uint64_t nch, uint64_t bins,
+                              double tsamp, double period, double *__restrict__ comb) {
+  extern __shared__ double shift[];
+  const uint64_t trial = blockIdx.x;
+  const double dbins = (double)bins;
+  for (uint64_t c = threadIdx.x; c < nch; c += blockDim.x) {
+    const double d = (double)delays[trial * nch + c];
+    shift[c] = __dmul_rn(__ddiv_rn(__dmul_rn(d, tsamp), period), dbins);
+  }
+  __syncthreads();
+  for (uint64_t b = threadIdx.x; b < bins; b += blockDim.x) {
+    double out = 0.0;
+    for (uint64_t c = 0; c < nch; ++c) {
+      double pos = fmod(__dadd_rn((double)b, shift[c]), dbins);
+      if (pos < 0.0) pos = __dadd_rn(pos, dbins);
+      const double fl = floor(pos);
+      uint64_t index = (uint64_t)fl;
+      if (index > bins - 1) index = bins - 1;
+      const double fraction = __dsub_rn(pos, (double)index);
+      const double m = chmean[c];
+      const double a = __dmul_rn(__dsub_rn((double)chp[c * bins + index], m),
+                                 __dsub_rn(1.0, fraction));
+      const double e = __dmul_rn(__dsub_rn((double)chp[c * bins + (index + 1) % bins], m),
+                                 fraction);
+      out = __dadd_rn(out, __dadd_rn(a, e));
+    }
+    comb[trial * bins + b] = out;
+  }
+}
+
+}  // namespace
+
+int fold_channels(const DeviceObs &o, uint64_t n, double tsamp, double period, uint64_t bins,
+                  std::vector<float> &values, cudaStream_t st) {
+  if (bins < 4 || bins > FOLD_MAXBINS || n == 0 || n > o.ns) {
+    set_error("profile: 4 <= bins <= 1024 and 0 < n <= nsamples are required");
+    return PSR_EINVAL;
+  }
+  const uint64_t per_cta = 8192;
+  const uint64_t nparts = (n + per_cta - 1) / per_cta;
+  DevBuf psums, pcounts, sums, cnts;
+  PSR_TRY(psums.ensure(o.nch * nparts * bins * 8));
+  PSR_TRY(pcounts.ensure(o.nch * nparts * bins * 8));
+  PSR_TRY(sums.ensure(o.nch * bins * 8));
+  PSR_TRY(cnts.ensure(o.nch * bins * 8));
+  const size_t smem = bins * (8 + 4);
+  dim3 grid((unsigned)nparts, (unsigned)o.nch);
+  switch (o.kind) {
+    case SAMPLE_U8:
+      k_fold_rows<unsigned char><<<grid, FOLD_NT, smem, st>>>(
+          o.samples.as<unsigned char>(), o.ld, n, tsamp, period, bins, per_cta,
+          psums.as<double>(), pcounts.as<unsigned long long>());
+      break;
+    case SAMPLE_U16:
+      k_fold_rows<uint16_t><<<grid, FOLD_NT, smem, st>>>(
+          o.samples.as<uint16_t>(), o.ld, n, tsamp, period, bins, per_cta, psums.as<double>(),
+          pcounts.as<unsigned long long>());
+      break;
+    default:
+      k_fold_rows<float><<<grid, FOLD_NT, smem, st>>>(o.samples.as<float>(), o.ld, n, tsamp,
+                                                       period, bins, per_cta, psums.as<double>(),
+                                                       pcounts.as<unsigned long long>());
+      break;
+  }
+  PSR_CUDA(cudaGetLastError());
+  k_fold_reduce<<<(unsigned)((o.nch * bins + 255) / 256), 256, 0, st>>>(
+      psums.as<double>(), pcounts.as<unsigned long long>(), nparts, bins, o.nch,
+      sums.as<double>(), cnts.as<unsigned long long>());
+  PSR_CUDA(cudaGetLastError());
+  std::vector<double> hs(o.nch * bins);
+  std::vector<unsigned long long> hc(o.nch * bins);
+  PSR_CUDA(cudaMemcpyAsync(hs.data(), sums.p, hs.size() * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hc.data(), cnts.p, hc.size() * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  values.resize(o.nch * bins);
+  for (uint64_t i = 0; i < o.nch * bins; ++i)
+    values[i] = hc[i] > 0 ? (float)(hs[i] / (double)hc[i]) : 0.0f;
+  return PSR_OK;
+}
+
+int dm_response(const std::vector<float> &chp, const std::vector<double> &chmean,
+                const uint32_t *d_delays, uint64_t ntrials, uint64_t nch, uint64_t bins,
+                double tsamp, double period, std::vector<double> &comb, cudaStream_t st) {
+  DevBuf dp, dm, dc;
+  PSR_TRY(dp.ensure(chp.size() * 4));
+  PSR_TRY(dm.ensure(chmean.size() * 8));
+  PSR_TRY(dc.ensure(ntrials * bins * 8));
+  PSR_CUDA(cudaMemcpyAsync(dp.p, chp.data(), chp.size() * 4, cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(dm.p, chmean.data(), chmean.size() * 8, cudaMemcpyHostToDevice, st));
+  k_dm_response<<<(unsigned)ntrials, 128, nch * 8, st>>>(dp.as<float>(), dm.as<double>(),
+                                                         d_delays, nch, bins, tsamp, period,
+                                                         dc.as<double>());
+  PSR_CUDA(cudaGetLastError());
+  comb.resize(ntrials * bins);
+  PSR_CUDA(cudaMemcpyAsync(comb.data(), dc.p, comb.size() * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
   return PSR_OK;
 }
 

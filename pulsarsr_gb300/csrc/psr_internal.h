@@ -202,5 +202,18 @@ int fold_profiles(const float *d_series, uint64_t n, double tsamp,
                   const double *periods, uint64_t nper, uint64_t bins,
                   uint64_t sample_offset, psr_profile_stats *stats,
                   float *values, uint64_t *counts, cudaStream_t st);
+// nper (series, period) pairs, series p at d_series + p * xstride.
+int fold_profiles_ex(const float *d_series, uint64_t xstride, uint64_t n, double tsamp,
+                     const double *periods, uint64_t nper, uint64_t bins,
+                     uint64_t sample_offset, psr_profile_stats *stats, float *values,
+                     uint64_t *counts, cudaStream_t st);
+// fold::profile of every channel row of o over samples [0, n): values[c*bins+b].
+int fold_channels(const DeviceObs &o, uint64_t n, double tsamp, double period, uint64_t bins,
+                  std::vector<float> &values, cudaStream_t st);
+// Combined shifted channel profiles per trial (confirmation.rs:397-413):
+// comb[trial*bins + b]; d_delays is the [ntrials][nch] u32 delay table.
+int dm_response(const std::vector<float> &chp, const std::vector<double> &chmean,
+                const uint32_t *d_delays, uint64_t ntrials, uint64_t nch, uint64_t bins,
+                double tsamp, double period, std::vector<double> &comb, cudaStream_t st);
 
 }  // namespace psr
