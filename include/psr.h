@@ -96,6 +96,12 @@ uint64_t psr_last_error(char *buf, uint64_t len);
 /* ------------------------------------------------------------- fbank */
 /* fbank::parse_header (fbank/src/lib.rs:72-147), host. */
 int psr_parse_header(const uint8_t *bytes, uint64_t len, psr_header *out);
+/* The parsed fbank::Header as serde_json writes it (psr header, header.json):
+ * the sorted keyword map "fields", then nchans, nbits, tsamp, fch1, foff,
+ * data_offset.  *needed receives the length without the NUL; at most cap
+ * bytes including the NUL are copied to buf (which may be NULL). */
+int psr_header_json(const uint8_t *bytes, uint64_t len, int pretty, char *buf,
+                    uint64_t cap, uint64_t *needed);
 
 /* Device-resident filterbank: the decoded samples live in HBM, channel-major,
  * stored in their integer width (u8 for nbits <= 8, u16, or f32). */

@@ -53,7 +53,15 @@ bool rd_string(const uint8_t *b, uint64_t len, uint64_t &pos, std::string &out, 
 }  // namespace
 
 // fbank::parse_header (fbank/src/lib.rs:72-147): strict keyword table.
+int parse_header_fields(const uint8_t *b, uint64_t len, psr_header &h,
+                        psrjson::Value *fields_json);
+
 int parse_header(const uint8_t *b, uint64_t len, psr_header &h) {
+  return parse_header_fields(b, len, h, nullptr);
+}
+
+int parse_header_fields(const uint8_t *b, uint64_t len, psr_header &h,
+                        psrjson::Value *fields_json) {
   static const char *kInts[] = {"machine_id", "telescope_id", "data_type", "barycentric",
                                 "pulsarcentric", "nbits", "nsamples", "nchans", "nifs",
                                 "nbeams", "ibeam", "signed"};
@@ -63,6 +71,7 @@ int parse_header(const uint8_t *b, uint64_t len, psr_header &h) {
     int kind;
     int32_t i;
     double f;
+    std::string t;
   };
   uint64_t pos = 0;
   int code = PSR_OK;
@@ -79,8 +88,7 @@ int parse_header(const uint8_t *b, uint64_t len, psr_header &h) {
     if (key == "HEADER_END") break;
     V v{};
     if (key == "rawdatafile" || key == "source_name") {
-      std::string t;
-      if (!rd_string(b, len, pos, t, code)) return code;
+      if (!rd_string(b, len, pos, v.t, code)) return code;
       v.kind = 2;
     } else if (std::any_of(std::begin(kInts), std::end(kInts),
                            [&](const char *k) { return key == k; })) {
@@ -167,6 +175,26 @@ int parse_header(const uint8_t *b, uint64_t len, psr_header &h) {
   h.fch1 = fch1;
   h.foff = foff;
   h.data_offset = (int64_t)pos;
+  if (fields_json) {
+    // fbank::Header as serde writes it: the BTreeMap of keywords (sorted),
+    // untagged values, then the parsed scalars (fbank/src/lib.rs:29-38).
+    psrjson::Value fm = psrjson::Value::object();
+    for (const auto &kv : f) {
+      const V &v = kv.second;
+      fm.set(kv.first, v.kind == 0   ? psrjson::Value::i64(v.i)
+                       : v.kind == 1 ? psrjson::Value::num(v.f)
+                                     : psrjson::Value::str(v.t));
+    }
+    psrjson::Value hv = psrjson::Value::object();
+    hv.set("fields", std::move(fm));
+    hv.set("nchans", psrjson::Value::u64((uint64_t)nchans));
+    hv.set("nbits", psrjson::Value::u64((uint64_t)nbits));
+    hv.set("tsamp", psrjson::Value::num(tsamp));
+    hv.set("fch1", psrjson::Value::num(fch1));
+    hv.set("foff", psrjson::Value::num(foff));
+    hv.set("data_offset", psrjson::Value::u64(pos));
+    *fields_json = std::move(hv);
+  }
   return PSR_OK;
 }
 
@@ -355,6 +383,25 @@ uint64_t psr_last_error(char *buf, uint64_t len) {
     buf[n] = 0;
   }
   return e.size();
+}
+
+int psr_header_json(const uint8_t *bytes, uint64_t len, int pretty, char *buf, uint64_t cap,
+                    uint64_t *needed) {
+  if (!bytes || !needed) {
+    set_error("header_json: null argument");
+    return PSR_EINVAL;
+  }
+  psr_header h;
+  psrjson::Value v;
+  PSR_TRY(parse_header_fields(bytes, len, h, &v));
+  const std::string s = psrjson::dump(v, pretty != 0);
+  *needed = s.size();
+  if (buf && cap) {
+    const uint64_t n = std::min<uint64_t>(cap - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+  }
+  return PSR_OK;
 }
 
 int psr_parse_header(const uint8_t *bytes, uint64_t len, psr_header *out) {

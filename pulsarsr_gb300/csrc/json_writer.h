@@ -167,4 +167,96 @@ inline std::string dump(const Value &v, bool pretty) {
   return o;
 }
 
+// Reads JSON text written by dump(): scalars keep their text, so a document
+// read and dumped again is unchanged.  Returns false on malformed input.
+struct Reader {
+  const std::string &s;
+  size_t i = 0;
+  explicit Reader(const std::string &text) : s(text) {}
+  void ws() {
+    while (i < s.size() && (s[i] == ' ' || s[i] == '\n' || s[i] == '\r' || s[i] == '\t')) ++i;
+  }
+  bool str(std::string &out) {
+    if (i >= s.size() || s[i] != '"') return false;
+    const size_t a = i++;
+    while (i < s.size() && s[i] != '"') i += s[i] == '\\' ? 2 : 1;
+    if (i >= s.size()) return false;
+    out = s.substr(a, ++i - a);
+    return true;
+  }
+  bool value(Value &v) {
+    ws();
+    if (i >= s.size()) return false;
+    const char c = s[i];
+    if (c == '{') {
+      v = Value::object();
+      ++i;
+      ws();
+      if (i < s.size() && s[i] == '}') return ++i, true;
+      for (;;) {
+        ws();
+        std::string k;
+        if (!str(k)) return false;
+        ws();
+        if (i >= s.size() || s[i++] != ':') return false;
+        Value x;
+        if (!value(x)) return false;
+        v.set(k.substr(1, k.size() - 2), std::move(x));
+        ws();
+        if (i < s.size() && s[i] == ',') {
+          ++i;
+          continue;
+        }
+        if (i < s.size() && s[i] == '}') return ++i, true;
+        return false;
+      }
+    }
+    if (c == '[') {
+      v = Value::array();
+      ++i;
+      ws();
+      if (i < s.size() && s[i] == ']') return ++i, true;
+      for (;;) {
+        Value x;
+        if (!value(x)) return false;
+        v.push(std::move(x));
+        ws();
+        if (i < s.size() && s[i] == ',') {
+          ++i;
+          continue;
+        }
+        if (i < s.size() && s[i] == ']') return ++i, true;
+        return false;
+      }
+    }
+    if (c == '"') {
+      std::string t;
+      if (!str(t)) return false;
+      v = Value::raw(t);
+      return true;
+    }
+    const size_t a = i;
+    while (i < s.size() && s[i] != ',' && s[i] != ']' && s[i] != '}' && s[i] != ' ' &&
+           s[i] != '\n')
+      ++i;
+    if (i == a) return false;
+    v = Value::raw(s.substr(a, i - a));
+    return true;
+  }
+};
+
+inline bool parse(const std::string &text, Value &out) {
+  Reader r(text);
+  if (!r.value(out)) return false;
+  r.ws();
+  return r.i == text.size();
+}
+
+// Field lookup in an object value (nullptr when absent).
+inline const Value *field(const Value &v, const std::string &k) {
+  for (const auto &f : v.fields)
+    if (f.first == k) return &f.second;
+  return nullptr;
+}
+
 }  // namespace psrjson
