@@ -78,6 +78,14 @@ typedef struct {
   double reduced_chi_square;
 } psr_profile_stats;
 
+/* Spin and dispersion parameters of a refinement: period (s), period
+ * derivative (s/s) and DM (pc cm^-3). */
+typedef struct {
+  double period_s;
+  double pdot;
+  double dm;
+} psr_timing;
+
 /* confirmation::Measurement (search/src/confirmation.rs:52-59). */
 typedef struct {
   double snr;
@@ -204,6 +212,51 @@ int psr_refine(const float *series, uint64_t n, double tsamp, double frequency,
 int psr_measure(const float *x, uint64_t n, uint64_t offset, double tsamp,
                 double period, uint64_t start_bin, uint64_t width_bins,
                 uint64_t bins, psr_measurement *out);
+
+/* ------------------------------------------------ gradient refinement */
+/* Refinement of (P, Pdot, DM) by gradient ascent on a differentiable fold
+ * objective.  No counterpart in the reference, whose refinement is the grid of
+ * fold::refine (fold/src/lib.rs:81-97) plus the half-step DM grid of
+ * confirmation::analyze (confirmation.rs:295-310); psr_refine_grid runs that
+ * grid, and this is offered beside it.
+ *
+ * Objective on samples t in [0, n) of a device filterbank:
+ *   y(t)  = sum_c (1-a_c) x[c][t+m_c] + a_c x[c][t+m_c+1]  with
+ *           m_c + a_c = 4148.808 DM (f_c^-2 - f_max^-2) / tsamp  (fractional,
+ *           linear-interpolated delays);
+ *   phase = nu T + nudot T^2 / 2, T = t tsamp, nu = 1/P, nudot = -Pdot/P^2;
+ *   each sample is split between its two nearest of `bins` phase bins
+ *   (weights 1-w, w) and folded into `subints` equal time parts;
+ *   J = sum_b (p_b - mean p)^2 / (n v), p_b summed over subints, v the
+ *   variance of y (at the starting point for psr_refine_gradient).
+ * The gradient comes from a hand-written adjoint; one objective + gradient
+ * evaluation reads the filterbank once. */
+typedef struct {
+  uint64_t bins;       /* phase bins (default 128) */
+  uint64_t subints;    /* time subintegrations (default 64) */
+  uint64_t max_evals;  /* objective evaluations per candidate (default 40) */
+  double tol_bins;     /* stop when a step moves < tol_bins phase bins (1e-3) */
+} psr_refine_options;
+void psr_refine_options_default(psr_refine_options *out);
+/* J and dJ/d(P, Pdot, DM) at theta.  variance <= 0 uses the variance of y at
+ * theta.  profile (bins values) and subint_profiles (subints*bins) may be
+ * NULL. */
+int psr_refine_objective(const psr_fb *fb, uint64_t n, const psr_timing *theta,
+                         const psr_refine_options *opt, double variance, double *J,
+                         double *grad, double *profile, double *subint_profiles);
+/* Gradient refinement (quasi-Newton ascent) of ncand starting points. */
+int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start,
+                        uint64_t ncand, const psr_refine_options *opt,
+                        psr_timing *out, double *J, uint64_t *evals);
+/* The reference's grid refinement on the device, for each starting point:
+ * integer-delay dedispersion at the start DM, fold::refine over 41
+ * frequencies within +-resolution_hz of 1/P, then 21 DMs at half dm_step
+ * around the start (clamped to [dm_lo, dm_hi]) folded at the refined period;
+ * the best reduced chi-square wins.  Pdot is passed through unchanged. */
+int psr_refine_grid(const psr_fb *fb, uint64_t n, const psr_timing *start,
+                    uint64_t ncand, double resolution_hz, double dm_step, double dm_lo,
+                    double dm_hi, uint64_t bins, psr_timing *out,
+                    double *reduced_chi_square);
 
 /* ------------------------------------------------------ confirmation */
 /* confirmation::Rules (search/src/confirmation.rs:17-40); the version string

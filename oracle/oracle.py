@@ -316,3 +316,23 @@ def analyze(data: np.ndarray, freqs, tsamp: float, trials, generated, limit: int
     finally:
         lib().orc_free(C.c_void_p(ptr))
     return json.loads(text)
+
+
+def refine_objective(data: np.ndarray, freqs, tsamp: float, n: int, period: float, pdot: float,
+                     dm: float, bins: int = 128, subints: int = 64, variance: float = 0.0):
+    """FP64 objective J and gradient (dJ/dP, dJ/dPdot, dJ/dDM) of the
+    gradient-refinement model, and its profile."""
+    x = _f32(data)
+    nch, ns = x.shape
+    f = np.ascontiguousarray(freqs, dtype=np.float64)
+    J = C.c_double()
+    grad = np.zeros(3)
+    prof = np.zeros(bins)
+    rc = lib().orc_refine_objective(_ptr(x, C.c_float), C.c_uint64(nch), C.c_uint64(ns),
+                                    _ptr(f, C.c_double), C.c_double(tsamp), C.c_uint64(n),
+                                    C.c_double(period), C.c_double(pdot), C.c_double(dm),
+                                    C.c_uint64(bins), C.c_uint64(subints),
+                                    C.c_double(variance), C.byref(J), _ptr(grad, C.c_double),
+                                    _ptr(prof, C.c_double))
+    _check(rc)
+    return J.value, grad, prof

@@ -1632,6 +1632,100 @@ char *orc_analyze_json(const float *data, uint64_t nchans, uint64_t nsamples,
   return res;
 }
 
+// FP64 reference of the gradient-refinement objective and its gradient (a
+// model this project defines; the reference has no counterpart).  Every
+// quantity is f64: fractional delays a_c, the interpolated series y and
+// z = dy/dDM, cloud-in-cell folding, J = sum_b (p_b - mean)^2 / (n v), and the
+// analytic derivatives d/dP, d/dPdot, d/dDM of J with v held fixed.
+int orc_refine_objective(const float *data, uint64_t nch, uint64_t ns, const double *freqs,
+                         double tsamp, uint64_t n, double P, double Pdot, double DM,
+                         uint64_t bins, uint64_t subints, double variance, double *J,
+                         double *grad, double *profile) {
+  if (n + 2 > ns || bins < 4 || subints < 1 || !(P > 0.0) || !(DM >= 0.0)) {
+    g_err = "refine_objective: invalid arguments";
+    return 1;
+  }
+  double fmax = 0.0;
+  for (uint64_t c = 0; c < nch; ++c) fmax = std::fmax(fmax, freqs[c]);
+  std::vector<double> a(nch), k(nch);
+  std::vector<uint64_t> m(nch);
+  for (uint64_t c = 0; c < nch; ++c) {
+    k[c] = 4148.808 * (1.0 / (freqs[c] * freqs[c]) - 1.0 / (fmax * fmax)) / tsamp;
+    const double tau = k[c] * DM;
+    m[c] = (uint64_t)std::floor(tau);
+    a[c] = tau - std::floor(tau);
+    if (m[c] + n + 1 > ns) {
+      g_err = "refine_objective: delays leave fewer than n + 1 samples";
+      return 1;
+    }
+  }
+  std::vector<double> y(n, 0.0), z(n, 0.0);
+  for (uint64_t c = 0; c < nch; ++c) {
+    const float *row = data + c * ns + m[c];
+    for (uint64_t t = 0; t < n; ++t) {
+      const double v0 = row[t], v1 = row[t + 1];
+      y[t] += (1.0 - a[c]) * v0 + a[c] * v1;
+      z[t] += k[c] * (v1 - v0);
+    }
+  }
+  double mean = 0.0, sq = 0.0;
+  for (double v : y) {
+    mean += v;
+    sq += v * v;
+  }
+  mean /= (double)n;
+  const double v = variance > 0.0 ? variance : std::fmax(sq / (double)n - mean * mean, 1e-300);
+  const double nu = 1.0 / P, nudot = -Pdot / (P * P);
+  const double B = (double)bins;
+  std::vector<double> p(bins, 0.0);
+  std::vector<uint64_t> b0s(n), b1s(n);
+  std::vector<double> ws(n);
+  for (uint64_t t = 0; t < n; ++t) {
+    const double T = (double)t * tsamp;
+    const double ph = nu * T + 0.5 * nudot * T * T;
+    const double u = (ph - std::floor(ph)) * B;
+    double fb = std::floor(u);
+    uint64_t b0 = (uint64_t)fb;
+    double w = u - fb;
+    if (b0 >= bins) {
+      b0 = 0;
+      w = 0.0;
+    }
+    const uint64_t b1 = b0 + 1 == bins ? 0 : b0 + 1;
+    b0s[t] = b0;
+    b1s[t] = b1;
+    ws[t] = w;
+    p[b0] += (1.0 - w) * y[t];
+    p[b1] += w * y[t];
+  }
+  double pm = 0.0;
+  for (double x : p) pm += x;
+  pm /= B;
+  double j = 0.0;
+  std::vector<double> g(bins);
+  for (uint64_t b = 0; b < bins; ++b) {
+    const double d = p[b] - pm;
+    j += d * d;
+    g[b] = 2.0 * d / ((double)n * v);
+  }
+  *J = j / ((double)n * v);
+  double dnu = 0.0, dnudot = 0.0, ddm = 0.0;
+  for (uint64_t t = 0; t < n; ++t) {
+    const double T = (double)t * tsamp;
+    const double du = y[t] * (g[b1s[t]] - g[b0s[t]]);
+    dnu += du * B * T;
+    dnudot += du * B * 0.5 * T * T;
+    ddm += ((1.0 - ws[t]) * g[b0s[t]] + ws[t] * g[b1s[t]]) * z[t];
+  }
+  if (grad) {
+    grad[0] = dnu * (-1.0 / (P * P)) + dnudot * (2.0 * Pdot / (P * P * P));
+    grad[1] = dnudot * (-1.0 / (P * P));
+    grad[2] = ddm;
+  }
+  if (profile) std::copy(p.begin(), p.end(), profile);
+  return 0;
+}
+
 void orc_free(void *p) { std::free(p); }
 
 }  // extern "C"

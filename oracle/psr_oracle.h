@@ -136,6 +136,13 @@ char *orc_analyze_json(const float *data, uint64_t nchans, uint64_t nsamples,
                        uint64_t ntrials, const orc_candidate *generated,
                        uint64_t ngenerated, uint64_t limit, uint64_t bins);
 
+/* FP64 reference of the gradient-refinement objective J and dJ/d(P, Pdot, DM)
+ * (the model this project defines; no reference counterpart). */
+int orc_refine_objective(const float *data, uint64_t nch, uint64_t ns,
+                         const double *freqs, double tsamp, uint64_t n, double P,
+                         double Pdot, double DM, uint64_t bins, uint64_t subints,
+                         double variance, double *J, double *grad, double *profile);
+
 /* Whole `psr search` (minus plots, hashing and file output) on the bytes of a
  * SIGPROC file; returns a malloc'd JSON document (free with orc_free). */
 char *orc_psr_search_json(const uint8_t *bytes, uint64_t len, double dm_min,

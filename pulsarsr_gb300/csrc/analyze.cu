@@ -173,6 +173,49 @@ int measure_dev(const float *d_x, uint64_t n, uint64_t offset, double tsamp, dou
 
 }  // namespace
 
+int grid_refine_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
+                    double resolution, double dm_step, double dm_lo, double dm_hi,
+                    uint64_t bins, psr_timing &out, double &rcs, cudaStream_t st) {
+  std::vector<double> freqs(o.nch);
+  for (uint64_t c = 0; c < o.nch; ++c) freqs[c] = o.h.fch1 + (double)c * o.h.foff;
+  const double tsamp = o.h.tsamp;
+  std::vector<uint64_t> d;
+  PSR_TRY(delays_for(freqs, tsamp, start.dm, d));
+  Dedisperser initial;
+  PSR_TRY(initial.run(o, d, 1, n, st));
+  FoldedProfile best;
+  PSR_TRY(refine_dev(initial.row(0), n, tsamp, 1.0 / start.period_s, resolution, 40, bins,
+                     best, st));
+  double best_dm = start.dm;
+  const double period = best.st.period_s;
+  std::vector<double> dms(21);
+  std::vector<uint64_t> grid;
+  for (int i = -10; i <= 10; ++i) {
+    const double dm = std::fmin(std::fmax(start.dm + (double)i * dm_step / 2.0, dm_lo), dm_hi);
+    dms[(size_t)(i + 10)] = dm;
+    PSR_TRY(delays_for(freqs, tsamp, dm, d));
+    grid.insert(grid.end(), d.begin(), d.end());
+  }
+  Dedisperser g;
+  PSR_TRY(g.run(o, grid, 21, n, st));
+  std::vector<double> periods(21, period);
+  std::vector<psr_profile_stats> sts(21);
+  std::vector<float> vals(21 * bins);
+  std::vector<uint64_t> cnts(21 * bins);
+  PSR_TRY(fold_profiles_ex(g.row(0), g.ldo, n, tsamp, periods.data(), 21, bins, 0, sts.data(),
+                           vals.data(), cnts.data(), st));
+  for (size_t i = 0; i < 21; ++i)
+    if (sts[i].reduced_chi_square > best.st.reduced_chi_square) {
+      best.st = sts[i];
+      best_dm = dms[i];
+    }
+  out.period_s = period;
+  out.pdot = start.pdot;
+  out.dm = best_dm;
+  rcs = best.st.reduced_chi_square;
+  return PSR_OK;
+}
+
 std::vector<Family> group_candidates(const psr_candidate *c, uint64_t n, double resolution,
                                      uint64_t limit, std::vector<uint64_t> *order,
                                      std::vector<int64_t> *family) {

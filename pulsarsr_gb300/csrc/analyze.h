@@ -56,6 +56,12 @@ int analyze_obs(const DeviceObs &o, const double *trials, uint64_t ntrials,
                 const psr_candidate *generated, uint64_t ngenerated, uint64_t limit,
                 uint64_t bins, const psr_rules &rules, Outcome &out, cudaStream_t st);
 
+// The reference's grid refinement (fold::refine over 41 frequencies, then 21
+// half-step DMs) at one starting point, on the device.
+int grid_refine_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
+                    double resolution, double dm_step, double dm_lo, double dm_hi,
+                    uint64_t bins, psr_timing &out, double &rcs, cudaStream_t st);
+
 psrjson::Value candidate_json(const psr_candidate &c);
 psrjson::Value outcome_json(const Outcome &o);
 

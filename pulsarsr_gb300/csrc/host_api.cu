@@ -13,6 +13,7 @@
 
 #include "analyze.h"
 #include "psr_internal.h"
+#include "refine.h"
 #include "search.h"
 
 namespace psr {
@@ -723,6 +724,98 @@ int psr_analyze(const psr_fb *fb, const double *trials, uint64_t ntrials,
   PSR_TRY(analyze_obs(fb->o, trials, ntrials, generated, ngenerated, limit, bins,
                       rules ? *rules : r, o->o, fb->stream.s));
   *out = o.release();
+  return PSR_OK;
+}
+
+// ------------------------------------------------ gradient refinement
+namespace {
+int refine_options(const psr_refine_options *o, RefineOptions &r) {
+  if (o) {
+    r.bins = o->bins;
+    r.subints = o->subints;
+    r.max_evals = o->max_evals;
+    r.tol = o->tol_bins;
+  }
+  if (r.bins < 4 || r.subints < 1 || r.max_evals < 1 || !(r.tol > 0.0)) {
+    set_error("refine: bins >= 4, subints >= 1, max_evals >= 1 and tol_bins > 0 required");
+    return PSR_EINVAL;
+  }
+  return PSR_OK;
+}
+int refine_length(const psr_fb *fb, uint64_t n) {
+  if (!fb || n < 16 || n + 2 > fb->o.ns) {
+    set_error("refine: 16 <= n <= nsamples - 2 required");
+    return PSR_EINVAL;
+  }
+  return PSR_OK;
+}
+}  // namespace
+
+int psr_refine_objective(const psr_fb *fb, uint64_t n, const psr_timing *theta,
+                         const psr_refine_options *opt, double variance, double *J, double *grad,
+                         double *profile, double *subint_profiles) {
+  PSR_TRY(refine_length(fb, n));
+  RefineOptions ro;
+  PSR_TRY(refine_options(opt, ro));
+  if (!theta || !J) {
+    set_error("refine: null argument");
+    return PSR_EINVAL;
+  }
+  RefineWork w;
+  RefineEval ev;
+  PSR_TRY(w.evaluate(fb->o, n, *theta, ro, 1.0, ev, fb->stream.s));
+  const double v = variance > 0.0 ? variance : (ev.var_y > 0.0 ? ev.var_y : 1.0);
+  *J = ev.J / v;
+  if (grad) {
+    grad[0] = ev.dP / v;
+    grad[1] = ev.dPdot / v;
+    grad[2] = ev.dDM / v;
+  }
+  if (profile) std::copy(ev.profile.begin(), ev.profile.end(), profile);
+  if (subint_profiles) std::copy(ev.cells.begin(), ev.cells.end(), subint_profiles);
+  return PSR_OK;
+}
+
+int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start, uint64_t ncand,
+                        const psr_refine_options *opt, psr_timing *out, double *J,
+                        uint64_t *evals) {
+  PSR_TRY(refine_length(fb, n));
+  RefineOptions ro;
+  PSR_TRY(refine_options(opt, ro));
+  if ((!start || !out) && ncand) {
+    set_error("refine: null argument");
+    return PSR_EINVAL;
+  }
+  RefineWork w;
+  for (uint64_t i = 0; i < ncand; ++i) {
+    double j = 0.0;
+    uint64_t e = 0;
+    PSR_TRY(refine_gradient_one(fb->o, n, start[i], ro, w, out[i], j, e, fb->stream.s));
+    if (J) J[i] = j;
+    if (evals) evals[i] = e;
+  }
+  return PSR_OK;
+}
+
+int psr_refine_grid(const psr_fb *fb, uint64_t n, const psr_timing *start, uint64_t ncand,
+                    double resolution_hz, double dm_step, double dm_lo, double dm_hi,
+                    uint64_t bins, psr_timing *out, double *rcs) {
+  PSR_TRY(refine_length(fb, n));
+  if ((!start || !out) && ncand) {
+    set_error("refine: null argument");
+    return PSR_EINVAL;
+  }
+  if (!(resolution_hz >= 0.0) || !(dm_step > 0.0) || !(dm_lo >= 0.0) || !(dm_hi >= dm_lo) ||
+      bins < 4) {
+    set_error("refine_grid: resolution >= 0, dm_step > 0, 0 <= dm_lo <= dm_hi, bins >= 4");
+    return PSR_EINVAL;
+  }
+  for (uint64_t i = 0; i < ncand; ++i) {
+    double r = 0.0;
+    PSR_TRY(grid_refine_one(fb->o, n, start[i], resolution_hz, dm_step, dm_lo, dm_hi, bins,
+                            out[i], r, fb->stream.s));
+    if (rcs) rcs[i] = r;
+  }
   return PSR_OK;
 }
 

@@ -1,0 +1,41 @@
+// Gradient refinement internals (k_refine.cu).
+#pragma once
+#include <vector>
+
+#include "psr_internal.h"
+
+namespace psr {
+
+struct RefineOptions {
+  uint64_t bins = 128;
+  uint64_t subints = 64;
+  uint64_t max_evals = 40;
+  double tol = 1e-3;  // stop when a step moves every parameter by < tol phase bins
+};
+
+struct RefineEval {
+  double J = 0.0;                        // objective
+  double dP = 0.0, dPdot = 0.0, dDM = 0.0;  // gradient
+  double dnu = 0.0, dnudot = 0.0;           // gradient in (1/P, -Pdot/P^2)
+  double mean_y = 0.0, var_y = 0.0;      // of the dedispersed series
+  std::vector<double> profile;           // B bins (sum over subints)
+  std::vector<double> cells;             // S x B cloud-in-cell fold
+};
+
+// Device buffers reused across evaluations of one filterbank.
+struct RefineWork {
+  DevBuf dm_, dalpha_, dk_, y_, z_, parts_, cells_, g_, adj_;
+  // Objective and adjoint gradient at th; v_fixed > 0 normalises J.
+  int evaluate(const DeviceObs &o, uint64_t n, const psr_timing &th, const RefineOptions &opt,
+               double v_fixed, RefineEval &ev, cudaStream_t st);
+};
+
+// Largest DM whose delays keep n + 1 samples inside the observation.
+double max_dm_for(const DeviceObs &o, uint64_t n);
+
+// Quasi-Newton ascent from `start`; returns the refined parameters.
+int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
+                        const RefineOptions &opt, RefineWork &w, psr_timing &out, double &J,
+                        uint64_t &evals, cudaStream_t st);
+
+}  // namespace psr

@@ -57,3 +57,71 @@ def measure(x, offset: int, tsamp: float, period: float, start_bin: int, width_b
                             C.c_uint64(start_bin), C.c_uint64(width_bins), C.c_uint64(bins),
                             C.byref(m)))
     return {k: getattr(m, k) for k, _ in Measurement._fields_}
+
+
+# ------------------------------------------------ gradient refinement
+class Timing(C.Structure):
+    """(P, Pdot, DM) of a refinement (psr_timing)."""
+    _fields_ = [("period_s", C.c_double), ("pdot", C.c_double), ("dm", C.c_double)]
+
+
+class RefineOptions(C.Structure):
+    _fields_ = [("bins", C.c_uint64), ("subints", C.c_uint64), ("max_evals", C.c_uint64),
+                ("tol_bins", C.c_double)]
+
+    @staticmethod
+    def make(bins=128, subints=64, max_evals=40, tol_bins=1e-3) -> "RefineOptions":
+        return RefineOptions(bins, subints, max_evals, tol_bins)
+
+
+TIMING_DTYPE = np.dtype([("period_s", "<f8"), ("pdot", "<f8"), ("dm", "<f8")])
+
+
+def refine_objective(fb, n: int, period: float, pdot: float, dm: float, bins: int = 128,
+                     subints: int = 64, variance: float = 0.0):
+    """The gradient-refinement objective J, dJ/d(P, Pdot, DM), the profile and
+    the (subints x bins) folded cells, computed on the device."""
+    th = Timing(period, pdot, dm)
+    opt = RefineOptions.make(bins, subints)
+    J = C.c_double()
+    grad = np.zeros(3)
+    prof = np.zeros(bins)
+    cells = np.zeros(bins * subints)
+    check(lib().psr_refine_objective(fb.handle, C.c_uint64(n), C.byref(th), C.byref(opt),
+                                     C.c_double(variance), C.byref(J),
+                                     grad.ctypes.data_as(C.POINTER(C.c_double)),
+                                     prof.ctypes.data_as(C.POINTER(C.c_double)),
+                                     cells.ctypes.data_as(C.POINTER(C.c_double))))
+    return J.value, grad, prof, cells.reshape(subints, bins)
+
+
+def refine_gradient(fb, n: int, starts, bins: int = 128, subints: int = 64,
+                    max_evals: int = 40, tol_bins: float = 1e-3):
+    """Gradient refinement of every starting point (a TIMING_DTYPE array or
+    (P, Pdot, DM) tuples); returns (refined, J, evaluations)."""
+    s = np.ascontiguousarray(np.array([tuple(x) for x in starts], dtype=TIMING_DTYPE))
+    out = np.zeros_like(s)
+    J = np.zeros(s.size)
+    ev = np.zeros(s.size, dtype=np.uint64)
+    opt = RefineOptions.make(bins, subints, max_evals, tol_bins)
+    check(lib().psr_refine_gradient(fb.handle, C.c_uint64(n), s.ctypes.data_as(C.c_void_p),
+                                    C.c_uint64(s.size), C.byref(opt),
+                                    out.ctypes.data_as(C.c_void_p),
+                                    J.ctypes.data_as(C.POINTER(C.c_double)),
+                                    ev.ctypes.data_as(C.POINTER(C.c_uint64))))
+    return out, J, ev
+
+
+def refine_grid(fb, n: int, starts, resolution_hz: float, dm_step: float, dm_lo: float,
+                dm_hi: float, bins: int = 64):
+    """The reference's grid refinement (41 frequencies, then 21 half-step DMs)
+    of every starting point, on the device; returns (refined, reduced chi2)."""
+    s = np.ascontiguousarray(np.array([tuple(x) for x in starts], dtype=TIMING_DTYPE))
+    out = np.zeros_like(s)
+    r = np.zeros(s.size)
+    check(lib().psr_refine_grid(fb.handle, C.c_uint64(n), s.ctypes.data_as(C.c_void_p),
+                                C.c_uint64(s.size), C.c_double(resolution_hz),
+                                C.c_double(dm_step), C.c_double(dm_lo), C.c_double(dm_hi),
+                                C.c_uint64(bins), out.ctypes.data_as(C.c_void_p),
+                                r.ctypes.data_as(C.POINTER(C.c_double))))
+    return out, r

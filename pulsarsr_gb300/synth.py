@@ -65,6 +65,7 @@ class Pulsar:
     duty: float          # FWHM as a fraction of the period
     amplitude: float     # peak, in units of the noise sigma
     phase: float = 0.25
+    pdot: float = 0.0    # period derivative (s/s); phase = t/P - pdot t^2 / (2 P^2)
 
 
 @dataclass
@@ -113,7 +114,9 @@ class Observation:
             x = rng.standard_normal(ns) + zero_dm
             for p in self.pulsars:
                 delay = K_DM * p.dm * (freqs[c] ** -2 - ref ** -2)
-                ph = np.mod((t - delay) / p.period_s - p.phase, 1.0)
+                td = t - delay
+                ph = np.mod(td / p.period_s - 0.5 * p.pdot * td * td / p.period_s ** 2
+                            - p.phase, 1.0)
                 dist = np.minimum(ph, 1.0 - ph)
                 x += p.amplitude * np.exp(-0.5 * (dist / (p.duty / 2.355)) ** 2)
             v = self.noise_mean + self.noise_sigma * gains[c] * x

@@ -1,0 +1,132 @@
+"""Gradient refinement of (P, Pdot, DM): the adjoint against finite
+differences and the FP64 oracle gradient, and the refined parameters against
+the injected truth and the reference's grid refinement."""
+import numpy as np
+import pytest
+
+# A 64-channel f32 filterbank, 1100-1500 MHz, 64 us, 2^17 samples (8.4 s),
+# with one 23.7 ms pulsar at DM 71.3.
+NCH, NS, TSAMP, FCH1, FOFF = 64, 1 << 17, 64e-6, 1500.0, -400.0 / 64
+TRUE_P, TRUE_DM, TRUE_PDOT = 0.0237, 71.3, 0.0
+N = NS - 4096
+
+
+def observation(seed=4, amplitude=0.6):
+    from pulsarsr_gb300 import synth
+    return synth.Observation(nchans=NCH, nbits=32, nsamples=NS, tsamp=TSAMP, fch1=FCH1,
+                             foff=FOFF, seed=seed, noise_mean=0.0, noise_sigma=1.0,
+                             pulsars=[synth.Pulsar(TRUE_P, TRUE_DM, 0.05, amplitude)],
+                             name="refine test")
+
+
+@pytest.fixture(scope="module")
+def obs_data():
+    o = observation()
+    x = o.samples()  # (ns, nch) f32
+    return o, np.ascontiguousarray(x.T)
+
+
+def central(f, x, h):
+    return (f(x + h) - f(x - h)) / (2 * h)
+
+
+# Finite-difference steps.  DM: 1e-6 relative.  P and Pdot: steps that move
+# the last sample's phase by ~1e-5 bins.  The cloud-in-cell objective is
+# piecewise quadratic, with a kink wherever a sample crosses a bin edge; a
+# 1e-6 relative step in P moves the last sample by 0.04 bins here (0.1-0.4
+# cycles at 2^23 samples), so its secant is not the derivative.
+H_P, H_PDOT, H_DM = 1e-10, 1e-12, 1e-6
+
+
+def test_oracle_gradient_matches_finite_differences(obs_data, oracle):
+    """The FP64 adjoint formulas against central differences."""
+    o, data = obs_data
+    freqs = o.frequencies()
+    P, D = TRUE_P * (1 + 3e-6), TRUE_DM + 0.4
+
+    def J(p, pd, d):
+        return oracle.refine_objective(data, freqs, TSAMP, N, p, pd, d, 128, 64,
+                                       variance=vfix)[0]
+    # hold the variance fixed at the evaluation point, as the model does
+    vfix = float(np.var(_y64(data, freqs, D)))
+    J0, g, _ = oracle.refine_objective(data, freqs, TSAMP, N, P, 0.0, D, 128, 64, variance=vfix)
+    fd_p = central(lambda x: J(x, 0.0, D), P, P * H_P)
+    fd_d = central(lambda x: J(P, 0.0, x), D, D * H_DM)
+    fd_pd = central(lambda x: J(P, x, D), 0.0, H_PDOT)
+    assert np.isclose(g[0], fd_p, rtol=1e-4), (g[0], fd_p)
+    assert np.isclose(g[2], fd_d, rtol=1e-4), (g[2], fd_d)
+    assert np.isclose(g[1], fd_pd, rtol=1e-3), (g[1], fd_pd)
+
+
+def _y64(data, freqs, dm):
+    k = 4148.808 * (1 / freqs ** 2 - 1 / freqs.max() ** 2) / TSAMP
+    tau = k * dm
+    m = np.floor(tau).astype(int)
+    a = tau - m
+    y = np.zeros(N)
+    for c in range(len(freqs)):
+        row = data[c].astype(np.float64)
+        y += (1 - a[c]) * row[m[c]:m[c] + N] + a[c] * row[m[c] + 1:m[c] + 1 + N]
+    return y
+
+
+@pytest.mark.gpu
+def test_device_objective_and_adjoint_match_fp64(gpu, oracle, obs_data):
+    from pulsarsr_gb300 import fbank, fold
+    o, data = obs_data
+    fb = fbank.decode(o.to_bytes())
+    freqs = o.frequencies()
+    for P, D, PD in ((TRUE_P, TRUE_DM, 0.0), (TRUE_P * (1 + 4e-6), TRUE_DM - 0.7, 1e-9),
+                     (TRUE_P * (1 - 2e-6), TRUE_DM + 1.1, -3e-10)):
+        vfix = float(np.var(_y64(data, freqs, D)))
+        Jd, gd, pd, cells = fold.refine_objective(fb, N, P, PD, D, 128, 64, variance=vfix)
+        Jo, go, po = oracle.refine_objective(data, freqs, TSAMP, N, P, PD, D, 128, 64,
+                                             variance=vfix)
+        # f32 sums over 64 channels against f64: relative 1e-5 per sample.
+        assert np.isclose(Jd, Jo, rtol=1e-4), (Jd, Jo)
+        assert np.allclose(pd, po, rtol=1e-4, atol=1e-3 * np.abs(po).max())
+        assert np.allclose(cells.sum(axis=0), pd, rtol=1e-9, atol=1e-6)
+        assert np.allclose(gd, go, rtol=2e-3, atol=1e-3 * np.abs(go).max()), (gd, go)
+
+
+@pytest.mark.gpu
+def test_device_adjoint_matches_finite_differences(gpu, obs_data):
+    from pulsarsr_gb300 import fbank, fold
+    o, data = obs_data
+    fb = fbank.decode(o.to_bytes())
+    P, D = TRUE_P * (1 + 3e-6), TRUE_DM + 0.4
+    vfix = 1.0
+
+    def J(p, pd, d):
+        return fold.refine_objective(fb, N, p, pd, d, 128, 64, variance=vfix)[0]
+    _, g, _, _ = fold.refine_objective(fb, N, P, 0.0, D, 128, 64, variance=vfix)
+    assert np.isclose(g[0], central(lambda x: J(x, 0.0, D), P, P * H_P), rtol=1e-3)
+    assert np.isclose(g[2], central(lambda x: J(P, 0.0, x), D, D * H_DM), rtol=5e-3)
+    assert np.isclose(g[1], central(lambda x: J(P, x, D), 0.0, H_PDOT), rtol=1e-3)
+
+
+@pytest.mark.gpu
+def test_gradient_refinement_reaches_truth_and_grid(gpu, obs_data):
+    from pulsarsr_gb300 import dedisperse, fbank, fold
+    o, data = obs_data
+    fb = fbank.decode(o.to_bytes())
+    freqs = o.frequencies()
+    T = N * TSAMP
+    resolution = 1.0 / T
+    step = dedisperse.dm_step(freqs, TSAMP)
+    rng = np.random.default_rng(7)
+    starts = []
+    for _ in range(8):
+        # Up to +-2 steps of the grid: frequency steps of resolution/20,
+        # DM steps of half the plan step.
+        f = 1 / TRUE_P + rng.uniform(-2, 2) * resolution / 20
+        starts.append((1 / f, 0.0, TRUE_DM + rng.uniform(-2, 2) * step / 2))
+    out, J, ev = fold.refine_gradient(fb, N, starts, 128, 64)
+    grid, rcs = fold.refine_grid(fb, N, starts, resolution, step, 0.0, 150.0, 128)
+    for i in range(len(starts)):
+        # Both land on the injected signal; the gradient result is no farther
+        # from the truth than the grid's (whose steps quantise it).
+        assert abs(out[i]["dm"] - TRUE_DM) <= max(abs(grid[i]["dm"] - TRUE_DM), step / 4) + 0.02
+        assert abs(out[i]["period_s"] - TRUE_P) <= \
+            max(abs(grid[i]["period_s"] - TRUE_P), TRUE_P ** 2 * resolution / 40) + 1e-9
+        assert ev[i] <= 40
