@@ -119,6 +119,35 @@ typedef struct psr_fb psr_fb;
 int psr_fb_decode(const uint8_t *bytes, uint64_t len, int64_t limit /* <0: none */,
                   psr_fb **out);
 int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples);
+/* A seeded synthetic filterbank generated directly on the device (the psr
+ * synth command, synth/src/lib.rs:37-88, and large test shapes).  Same signal
+ * model as the reference (Gaussian noise plus dispersed Gaussian pulses with
+ * fractional delays), but the noise stream is a counter-based hash of
+ * (seed, channel, sample), not the reference's ChaCha8 stream.  Integer bit
+ * depths are rounded and clamped. */
+typedef struct {
+  double period_s;
+  double pdot;
+  double dm;
+  double duty;       /* Gaussian FWHM as a fraction of the period, (0, 0.5) */
+  double amplitude;  /* peak in units of the noise sigma */
+  double phase;      /* pulse phase offset (cycles); the reference uses 0.25 */
+} psr_synth_pulsar;
+typedef struct {
+  int64_t nchans;
+  int64_t nbits;     /* 1, 2, 4, 8, 16 or 32 (f32) */
+  uint64_t nsamples;
+  double tsamp;
+  double fch1;
+  double foff;
+  uint64_t seed;
+  double noise_mean;
+  double noise_sigma;
+  double gain_spread;  /* per-channel gains uniform in 1 +- gain_spread */
+  const psr_synth_pulsar *pulsars;
+  uint64_t npulsars;   /* at most 64 */
+} psr_synth_config;
+int psr_fb_synth(const psr_synth_config *cfg, psr_fb **out);
 /* Filterbank.data as f32, channel-major (nchans * nsamples values). */
 int psr_fb_download(const psr_fb *fb, float *out);
 void psr_fb_free(psr_fb *fb);
@@ -236,6 +265,12 @@ typedef struct {
   uint64_t subints;    /* time subintegrations (default 64) */
   uint64_t max_evals;  /* objective evaluations per candidate (default 40) */
   double tol_bins;     /* stop when a step moves < tol_bins phase bins (1e-3) */
+  int32_t exact;       /* 0 (default): fold once per group of nearby starting
+                          points into a channels x subints x bins cube at a
+                          reference (P, Pdot, DM) and optimise on it, each
+                          (channel, subint) profile shifted by its phase change
+                          at the subint centre; 1: every evaluation runs the
+                          objective above on the filterbank */
 } psr_refine_options;
 void psr_refine_options_default(psr_refine_options *out);
 /* J and dJ/d(P, Pdot, DM) at theta.  variance <= 0 uses the variance of y at

@@ -426,6 +426,17 @@ int psr_fb_decode(const uint8_t *bytes, uint64_t len, int64_t limit, psr_fb **ou
   return PSR_OK;
 }
 
+int psr_fb_synth(const psr_synth_config *cfg, psr_fb **out) {
+  if (!cfg || !out) {
+    set_error("invalid synthetic configuration");
+    return PSR_EINVAL;
+  }
+  std::unique_ptr<psr_fb> fb(new psr_fb());
+  PSR_TRY(synth_obs(*cfg, fb->o, fb->stream.s));
+  *out = fb.release();
+  return PSR_OK;
+}
+
 int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples) {
   if (!fb) {
     set_error("fb_info: null handle");
@@ -735,6 +746,7 @@ int refine_options(const psr_refine_options *o, RefineOptions &r) {
     r.subints = o->subints;
     r.max_evals = o->max_evals;
     r.tol = o->tol_bins;
+    r.exact = o->exact != 0;
   }
   if (r.bins < 4 || r.subints < 1 || r.max_evals < 1 || !(r.tol > 0.0)) {
     set_error("refine: bins >= 4, subints >= 1, max_evals >= 1 and tol_bins > 0 required");
@@ -786,13 +798,66 @@ int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start, u
     set_error("refine: null argument");
     return PSR_EINVAL;
   }
-  RefineWork w;
-  for (uint64_t i = 0; i < ncand; ++i) {
-    double j = 0.0;
-    uint64_t e = 0;
-    PSR_TRY(refine_gradient_one(fb->o, n, start[i], ro, w, out[i], j, e, fb->stream.s));
-    if (J) J[i] = j;
-    if (evals) evals[i] = e;
+  if (ro.exact) {
+    RefineWork w;
+    for (uint64_t i = 0; i < ncand; ++i) {
+      double j = 0.0;
+      uint64_t e = 0;
+      PSR_TRY(refine_gradient_one(fb->o, n, start[i], ro, w, out[i], j, e, fb->stream.s));
+      if (J) J[i] = j;
+      if (evals) evals[i] = e;
+    }
+    return PSR_OK;
+  }
+  for (uint64_t i = 0; i < ncand; ++i)
+    if (!(start[i].period_s > 0.0) || !std::isfinite(start[i].period_s) ||
+        !std::isfinite(start[i].pdot) || !(start[i].dm >= 0.0)) {
+      set_error("refine: finite positive period, finite pdot and nonnegative DM required");
+      return PSR_EINVAL;
+    }
+  // Group nearby starting points (sorted by DM, then frequency): at most 16
+  // per cube, within half a cycle of frequency drift over the observation and
+  // a quarter cycle of DM smear across the band of the group's first member.
+  const DeviceObs &o = fb->o;
+  double fmax = 0.0, fmin = 1e300;
+  for (uint64_t c = 0; c < o.nch; ++c) {
+    const double f = o.h.fch1 + (double)c * o.h.foff;
+    fmax = std::fmax(fmax, f);
+    fmin = std::fmin(fmin, f);
+  }
+  const double kspan = 4148.808 * (1.0 / (fmin * fmin) - 1.0 / (fmax * fmax));
+  const double T = (double)n * o.h.tsamp;
+  std::vector<uint64_t> idx(ncand);
+  for (uint64_t i = 0; i < ncand; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](uint64_t a, uint64_t b) {
+    if (start[a].dm != start[b].dm) return start[a].dm < start[b].dm;
+    return start[a].period_s > start[b].period_s;
+  });
+  std::vector<uint64_t> pending = idx;
+  while (!pending.empty()) {
+    const uint64_t lead = pending.front();
+    const double nu0 = 1.0 / start[lead].period_s;
+    std::vector<uint64_t> group, rest;
+    for (uint64_t k : pending) {
+      const double nu = 1.0 / start[k].period_s;
+      const bool near = std::fabs(nu - nu0) * T <= 0.5 &&
+                        std::fabs(start[k].dm - start[lead].dm) * kspan * nu0 <= 0.25 &&
+                        std::fabs(start[k].pdot - start[lead].pdot) * nu0 * nu0 * T * T <= 1.0;
+      if (near && group.size() < 16) group.push_back(k);
+      else rest.push_back(k);
+    }
+    std::vector<psr_timing> gs(group.size()), go(group.size());
+    std::vector<double> gj(group.size());
+    std::vector<uint64_t> ge(group.size());
+    for (size_t i = 0; i < group.size(); ++i) gs[i] = start[group[i]];
+    PSR_TRY(refine_cube_group(o, n, gs.data(), group.size(), ro, go.data(), gj.data(),
+                              ge.data(), fb->stream.s));
+    for (size_t i = 0; i < group.size(); ++i) {
+      out[group[i]] = go[i];
+      if (J) J[group[i]] = gj[i];
+      if (evals) evals[group[i]] = ge[i];
+    }
+    pending.swap(rest);
   }
   return PSR_OK;
 }

@@ -319,13 +319,15 @@ int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
   const double kspan = K_DM_R * (1.0 / (fmin * fmin) - 1.0 / (fmax * fmax));  // s per DM
   const double nu0 = 1.0 / start.period_s;
   const double nudot0 = -start.pdot / (start.period_s * start.period_s);
-  // Scaled coordinates: one unit moves the phase of the last sample (nu, nudot)
-  // or of the lowest channel (DM) by one profile bin.
-  const double s1 = 1.0 / (B * T), s2 = 2.0 / (B * T * T);
+  // Scaled coordinates (one unit = one profile bin), orthogonal over the
+  // span: with x = 2T/T_end - 1 the phase change is q1 x / B + q2 (x^2 - 1/3) / B,
+  // i.e. dnu = (2 q1 - 4 q2) / (B T_end), dnudot = 8 q2 / (B T_end^2); q3 moves
+  // the lowest channel's phase by q3 bins through DM.
   const double s3 = kspan > 0.0 ? start.period_s / (B * kspan) : 1.0;
   const double dm_hi = max_dm_for(o, n);
   auto theta = [&](const double q[3]) {
-    const double nu = nu0 + q[0] * s1, nudot = nudot0 + q[1] * s2;
+    const double nu = nu0 + (2.0 * q[0] - 4.0 * q[1]) / (B * T);
+    const double nudot = nudot0 + 8.0 * q[1] / (B * T * T);
     psr_timing t;
     t.period_s = 1.0 / nu;
     t.pdot = -nudot / (nu * nu);
@@ -339,8 +341,8 @@ int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
   ++evals;
   const double v = ev.var_y > 0.0 ? ev.var_y : 1.0;
   auto grad_q = [&](const RefineEval &e, double g[3]) {
-    g[0] = e.dnu * s1;
-    g[1] = e.dnudot * s2;
+    g[0] = e.dnu * 2.0 / (B * T);
+    g[1] = e.dnu * (-4.0 / (B * T)) + e.dnudot * 8.0 / (B * T * T);
     g[2] = e.dDM * s3;
   };
   double Jc = ev.J / v, g[3];
@@ -409,5 +411,5 @@ int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
 
 // ------------------------------------------------------------------ C ABI
 extern "C" void psr_refine_options_default(psr_refine_options *out) {
-  if (out) *out = psr_refine_options{128, 64, 40, 1e-3};
+  if (out) *out = psr_refine_options{128, 64, 40, 1e-3, 0};
 }

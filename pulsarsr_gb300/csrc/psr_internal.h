@@ -97,6 +97,9 @@ struct DeviceObs {
   }
 };
 
+// Seeded synthetic observation generated on the device (k_synth.cu).
+int synth_obs(const psr_synth_config &cfg, DeviceObs &o, cudaStream_t st);
+
 // Host-side restatements that stay on the host (FP64 tables, small sorts).
 bool host_delays(const double *f, size_t n, double tsamp, double dm,
                  std::vector<uint64_t> &out);

@@ -11,6 +11,7 @@ struct RefineOptions {
   uint64_t subints = 64;
   uint64_t max_evals = 40;
   double tol = 1e-3;  // stop when a step moves every parameter by < tol phase bins
+  bool exact = false;  // optimise the filterbank objective itself (no cube)
 };
 
 struct RefineEval {
@@ -37,5 +38,10 @@ double max_dm_for(const DeviceObs &o, uint64_t n);
 int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
                         const RefineOptions &opt, RefineWork &w, psr_timing &out, double &J,
                         uint64_t &evals, cudaStream_t st);
+
+// Cube-based refinement of K nearby starting points (k_refine_cube.cu).
+int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, uint64_t K,
+                      const RefineOptions &opt, psr_timing *out, double *J, uint64_t *evals,
+                      cudaStream_t st);
 
 }  // namespace psr

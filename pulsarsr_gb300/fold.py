@@ -67,11 +67,11 @@ class Timing(C.Structure):
 
 class RefineOptions(C.Structure):
     _fields_ = [("bins", C.c_uint64), ("subints", C.c_uint64), ("max_evals", C.c_uint64),
-                ("tol_bins", C.c_double)]
+                ("tol_bins", C.c_double), ("exact", C.c_int32)]
 
     @staticmethod
-    def make(bins=128, subints=64, max_evals=40, tol_bins=1e-3) -> "RefineOptions":
-        return RefineOptions(bins, subints, max_evals, tol_bins)
+    def make(bins=128, subints=64, max_evals=40, tol_bins=1e-3, exact=False) -> "RefineOptions":
+        return RefineOptions(bins, subints, max_evals, tol_bins, 1 if exact else 0)
 
 
 TIMING_DTYPE = np.dtype([("period_s", "<f8"), ("pdot", "<f8"), ("dm", "<f8")])
@@ -96,14 +96,16 @@ def refine_objective(fb, n: int, period: float, pdot: float, dm: float, bins: in
 
 
 def refine_gradient(fb, n: int, starts, bins: int = 128, subints: int = 64,
-                    max_evals: int = 40, tol_bins: float = 1e-3):
+                    max_evals: int = 40, tol_bins: float = 1e-3, exact: bool = False):
     """Gradient refinement of every starting point (a TIMING_DTYPE array or
-    (P, Pdot, DM) tuples); returns (refined, J, evaluations)."""
+    (P, Pdot, DM) tuples); returns (refined, J, evaluations).  exact=False
+    optimises on a folded cube per group of nearby starts, exact=True on the
+    filterbank objective at every evaluation."""
     s = np.ascontiguousarray(np.array([tuple(x) for x in starts], dtype=TIMING_DTYPE))
     out = np.zeros_like(s)
     J = np.zeros(s.size)
     ev = np.zeros(s.size, dtype=np.uint64)
-    opt = RefineOptions.make(bins, subints, max_evals, tol_bins)
+    opt = RefineOptions.make(bins, subints, max_evals, tol_bins, exact)
     check(lib().psr_refine_gradient(fb.handle, C.c_uint64(n), s.ctypes.data_as(C.c_void_p),
                                     C.c_uint64(s.size), C.byref(opt),
                                     out.ctypes.data_as(C.c_void_p),

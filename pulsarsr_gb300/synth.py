@@ -153,3 +153,34 @@ def config_c2(seed: int = 2) -> Observation:
                        pulsars=[Pulsar(0.0046214, 62.4, 0.03, 0.04)], tone_hz=28.76,
                        tone_amplitude=0.05, bursts=5, burst_amplitude=1.0,
                        name="config2 GBT-shaped synthetic")
+
+
+# ----------------------------------------------------------- on the device
+def device(nchans: int, nbits: int, nsamples: int, tsamp: float, fch1: float, foff: float,
+           seed: int, noise_mean: float = 0.0, noise_sigma: float = 1.0,
+           gain_spread: float = 0.0, pulsars=()):
+    """A seeded synthetic filterbank generated directly in HBM (psr_fb_synth);
+    pulsars are Pulsar values.  Returns an fbank.Filterbank."""
+    import ctypes as C
+
+    from ._lib import check, lib
+    from .fbank import Filterbank
+
+    class _P(C.Structure):
+        _fields_ = [("period_s", C.c_double), ("pdot", C.c_double), ("dm", C.c_double),
+                    ("duty", C.c_double), ("amplitude", C.c_double), ("phase", C.c_double)]
+
+    class _Cfg(C.Structure):
+        _fields_ = [("nchans", C.c_int64), ("nbits", C.c_int64), ("nsamples", C.c_uint64),
+                    ("tsamp", C.c_double), ("fch1", C.c_double), ("foff", C.c_double),
+                    ("seed", C.c_uint64), ("noise_mean", C.c_double),
+                    ("noise_sigma", C.c_double), ("gain_spread", C.c_double),
+                    ("pulsars", C.POINTER(_P)), ("npulsars", C.c_uint64)]
+
+    arr = (_P * max(len(pulsars), 1))(*[_P(p.period_s, p.pdot, p.dm, p.duty, p.amplitude,
+                                            p.phase) for p in pulsars])
+    cfg = _Cfg(nchans, nbits, nsamples, tsamp, fch1, foff, seed, noise_mean, noise_sigma,
+               gain_spread, arr if pulsars else None, len(pulsars))
+    h = C.c_void_p()
+    check(lib().psr_fb_synth(C.byref(cfg), C.byref(h)))
+    return Filterbank(h.value)

@@ -26,6 +26,14 @@ def obs_data():
     return o, np.ascontiguousarray(x.T)
 
 
+def mid_epoch(t, T):
+    """Period at the middle of a span of T seconds (P and Pdot at the start are
+    nearly degenerate over short spans; the mid-span period is not)."""
+    t = t.copy()
+    t["period_s"] = t["period_s"] + t["pdot"] * T / 2
+    return t
+
+
 def central(f, x, h):
     return (f(x + h) - f(x - h)) / (2 * h)
 
@@ -121,12 +129,64 @@ def test_gradient_refinement_reaches_truth_and_grid(gpu, obs_data):
         # DM steps of half the plan step.
         f = 1 / TRUE_P + rng.uniform(-2, 2) * resolution / 20
         starts.append((1 / f, 0.0, TRUE_DM + rng.uniform(-2, 2) * step / 2))
-    out, J, ev = fold.refine_gradient(fb, N, starts, 128, 64)
     grid, rcs = fold.refine_grid(fb, N, starts, resolution, step, 0.0, 150.0, 128)
-    for i in range(len(starts)):
-        # Both land on the injected signal; the gradient result is no farther
-        # from the truth than the grid's (whose steps quantise it).
-        assert abs(out[i]["dm"] - TRUE_DM) <= max(abs(grid[i]["dm"] - TRUE_DM), step / 4) + 0.02
-        assert abs(out[i]["period_s"] - TRUE_P) <= \
-            max(abs(grid[i]["period_s"] - TRUE_P), TRUE_P ** 2 * resolution / 40) + 1e-9
-        assert ev[i] <= 40
+    for exact in (True, False):
+        out, J, ev = fold.refine_gradient(fb, N, starts, 128, 64, exact=exact)
+        out = mid_epoch(out, T)
+        for i in range(len(starts)):
+            # Both land on the injected signal; the gradient result is no
+            # farther from the truth than the grid's (whose steps quantise it).
+            assert abs(out[i]["dm"] - TRUE_DM) <= \
+                max(abs(grid[i]["dm"] - TRUE_DM), step / 4) + 0.02, (exact, out[i], grid[i])
+            assert abs(out[i]["period_s"] - TRUE_P) <= \
+                max(abs(grid[i]["period_s"] - TRUE_P), TRUE_P ** 2 * resolution / 40) + 1e-9, \
+                (exact, out[i], grid[i])
+            assert ev[i] <= 40
+
+
+@pytest.mark.gpu
+def test_device_synth_statistics_and_determinism(gpu):
+    from pulsarsr_gb300 import synth
+    a = synth.device(16, 32, 1 << 16, 64e-6, 1500.0, -10.0, seed=9, noise_mean=3.0,
+                     noise_sigma=2.0)
+    b = synth.device(16, 32, 1 << 16, 64e-6, 1500.0, -10.0, seed=9, noise_mean=3.0,
+                     noise_sigma=2.0)
+    c = synth.device(16, 8, 1 << 16, 64e-6, 1500.0, -10.0, seed=9, noise_mean=100.0,
+                     noise_sigma=10.0)
+    x, y, z = a.data, b.data, c.data
+    assert x.tobytes() == y.tobytes()
+    assert abs(x.mean() - 3.0) < 0.02 and abs(x.std() - 2.0) < 0.02
+    assert abs(z.mean() - 100.0) < 0.2 and z.min() >= 0 and z.max() <= 255
+    assert np.all(z == np.rint(z))
+    # neighbouring samples and channels are uncorrelated
+    r = np.corrcoef(x[:, :-1].ravel(), x[:, 1:].ravel())[0, 1]
+    assert abs(r) < 0.01
+
+
+@pytest.mark.gpu
+def test_refinement_on_device_synthesised_pulsar(gpu):
+    """A 256-channel 2^20-sample f32 observation made on the device with one
+    pulsar (P 8.7 ms, DM 213.4); the gradient and grid refinements from offset
+    starts both recover it."""
+    from pulsarsr_gb300 import dedisperse, fold, synth
+    P, PD, DM = 0.0087341, 0.0, 213.4
+    fb = synth.device(256, 32, 1 << 20, 64e-6, 1500.0, -400.0 / 256, seed=11,
+                      pulsars=[synth.Pulsar(P, DM, 0.04, 0.08, phase=0.3, pdot=PD)])
+    freqs = fb.header.frequencies()
+    n = fb.nsamples - int(dedisperse.delays(freqs, 64e-6, 400.0).max()) - 4
+    T = n * 64e-6
+    resolution = 1.0 / T
+    step = dedisperse.dm_step(freqs, 64e-6)
+    rng = np.random.default_rng(3)
+    starts = [(1 / (1 / P + rng.uniform(-2, 2) * resolution / 20), 0.0,
+               DM + rng.uniform(-2, 2) * step / 2) for _ in range(16)]
+    out, J, ev = fold.refine_gradient(fb, n, starts, 128, 64)
+    out = mid_epoch(out, T)
+    grid, _ = fold.refine_grid(fb, n, starts, resolution, step, 0.0, 400.0, 128)
+    dp_grad = np.abs(out["period_s"] - P)
+    dp_grid = np.abs(grid["period_s"] - P)
+    dd_grad = np.abs(out["dm"] - DM)
+    dd_grid = np.abs(grid["dm"] - DM)
+    assert np.median(dp_grad) <= np.median(dp_grid) + P * P * resolution / 40
+    assert np.median(dd_grad) <= np.median(dd_grid) + step / 8
+    assert np.all(dp_grad < P * P * resolution / 4) and np.all(dd_grad < step)
