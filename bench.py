@@ -382,13 +382,102 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------ refinement
+def refine_workload(seed=4):
+    """1024 ch f32, 2^23 samples at 64 us, 1100-1500 MHz, generated on the
+    device: N(0,1) noise plus 16 seeded pulsars (P 5-500 ms log-uniform, DM
+    10-300, duty 3-5%); 16 starting points per pulsar offset uniformly by up
+    to +-2 grid steps in frequency (resolution / 20) and DM (half the plan
+    step)."""
+    from pulsarsr_gb300 import dedisperse, synth
+    rng = np.random.default_rng(seed)
+    nch, ns, tsamp, fch1, foff = 1024, 1 << 23, 64e-6, 1500.0, -400.0 / 1024
+    pulsars = []
+    for _ in range(16):
+        P = float(np.exp(rng.uniform(np.log(0.005), np.log(0.5))))
+        pulsars.append(synth.Pulsar(P, float(rng.uniform(10, 300)), float(rng.uniform(0.03, 0.05)),
+                                    float(rng.uniform(0.002, 0.005)),
+                                    phase=float(rng.uniform(0, 1))))
+    fb = synth.device(nch, 32, ns, tsamp, fch1, foff, seed=seed, pulsars=pulsars)
+    freqs = fb.header.frequencies()
+    n = ns - int(dedisperse.delays(freqs, tsamp, 400.0).max()) - 4
+    resolution = 1.0 / (n * tsamp)
+    step = dedisperse.dm_step(freqs, tsamp)
+    starts, truth = [], []
+    for p in pulsars:
+        for _ in range(16):
+            f = 1 / p.period_s + rng.uniform(-2, 2) * resolution / 20
+            starts.append((1 / f, 0.0, p.dm + rng.uniform(-2, 2) * step / 2))
+            truth.append((p.period_s, 0.0, p.dm))
+    return fb, n, starts, np.array(truth), resolution, step, tsamp
+
+
+def run_refine(args):
+    from pulsarsr_gb300 import fold
+    rt = cudart()
+    t0 = time.perf_counter()
+    fb, n, starts, truth, resolution, step, tsamp = refine_workload()
+    rt.cudaDeviceSynchronize()
+    t_synth = time.perf_counter() - t0
+    T = n * tsamp
+    # warm-up on a few candidates (module loads, allocations)
+    # The gradient's DM is kept inside the window the grid searches (10 half steps).
+    window = 10 * step / 2
+    fold.refine_gradient(fb, n, starts[:16], dm_window=window)
+    fold.refine_grid(fb, n, starts[:2], resolution, step, 0.0, 400.0, 128)
+    rt.cudaDeviceSynchronize()
+    t0 = time.perf_counter()
+    g, J, ev = fold.refine_gradient(fb, n, starts, dm_window=window)
+    rt.cudaDeviceSynchronize()
+    t_grad = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    q, rcs = fold.refine_grid(fb, n, starts, resolution, step, 0.0, 400.0, 128)
+    rt.cudaDeviceSynchronize()
+    t_grid = time.perf_counter() - t0
+    pm_grad = g["period_s"] + g["pdot"] * T / 2  # period at mid-span
+    dp_grad = np.abs(pm_grad - truth[:, 0])
+    dp_grid = np.abs(q["period_s"] - truth[:, 0])
+    dd_grad = np.abs(g["dm"] - truth[:, 2])
+    dd_grid = np.abs(q["dm"] - truth[:, 2])
+    gg_p = np.abs(pm_grad - q["period_s"])
+    gg_d = np.abs(g["dm"] - q["dm"])
+    ncand = len(starts)
+    line = {
+        "metric": "refine s/candidate (gradient vs grid, 256 candidates)",
+        "value": round(t_grad / ncand, 6), "unit": "s/candidate", "n_gpus": 1,
+        "higher_is_better": False, "dtype": "f32 data, f64 phases",
+        "data": "synthetic, generated on the device (seed 4)",
+        "config": {"workload": "1024 ch f32 x 2^23 samples, 64 us, 1100-1500 MHz, 16 pulsars, "
+                               "256 starts offset <= 2 grid steps; 128 bins x 64 subints",
+                   "n": int(n), "candidates": ncand},
+        "grid_s_per_candidate": round(t_grid / ncand, 6),
+        "speedup_vs_grid": round(t_grid / t_grad, 2),
+        "synth_seconds": round(t_synth, 3),
+        "evaluations_median": int(np.median(ev)),
+        "period_error_s": {"gradient_median": float(np.median(dp_grad)),
+                           "gradient_p90": float(np.percentile(dp_grad, 90)),
+                           "grid_median": float(np.median(dp_grid)),
+                           "grid_p90": float(np.percentile(dp_grid, 90))},
+        "dm_error": {"gradient_median": float(np.median(dd_grad)),
+                     "gradient_p90": float(np.percentile(dd_grad, 90)),
+                     "grid_median": float(np.median(dd_grid)),
+                     "grid_p90": float(np.percentile(dd_grid, 90))},
+        "gradient_vs_grid": {"within_1e-9s": float(np.mean(gg_p <= 1e-9)),
+                             "within_0.01dm": float(np.mean(gg_d <= 0.01)),
+                             "period_median_s": float(np.median(gg_p)),
+                             "dm_median": float(np.median(gg_d))},
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c4"],
+                    help="c1/c2: searches; c4: gradient vs grid refinement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--trials", type=int, default=0,
                     help="search only the first N trial DMs (small profiling case)")
@@ -398,7 +487,10 @@ def main():
     else:
         from pulsarsr_gb300 import build
         build.build()
-        run_ours(args)
+        if args.config == "c4":
+            run_refine(args)
+        else:
+            run_ours(args)
 
 
 if __name__ == "__main__":

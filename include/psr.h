@@ -271,6 +271,8 @@ typedef struct {
                           (channel, subint) profile shifted by its phase change
                           at the subint centre; 1: every evaluation runs the
                           objective above on the filterbank */
+  double dm_window;    /* > 0: keep DM within start +- dm_window (the grid
+                          searches +-10 half steps); 0: unbounded */
 } psr_refine_options;
 void psr_refine_options_default(psr_refine_options *out);
 /* J and dJ/d(P, Pdot, DM) at theta.  variance <= 0 uses the variance of y at

@@ -747,6 +747,7 @@ int refine_options(const psr_refine_options *o, RefineOptions &r) {
     r.max_evals = o->max_evals;
     r.tol = o->tol_bins;
     r.exact = o->exact != 0;
+    r.dm_window = o->dm_window;
   }
   if (r.bins < 4 || r.subints < 1 || r.max_evals < 1 || !(r.tol > 0.0)) {
     set_error("refine: bins >= 4, subints >= 1, max_evals >= 1 and tol_bins > 0 required");

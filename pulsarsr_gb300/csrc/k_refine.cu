@@ -331,7 +331,10 @@ int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
     psr_timing t;
     t.period_s = 1.0 / nu;
     t.pdot = -nudot / (nu * nu);
-    t.dm = std::fmin(std::fmax(start.dm + q[2] * s3, 0.0), dm_hi);
+    double dm = start.dm + q[2] * s3;
+    if (opt.dm_window > 0.0)
+      dm = std::fmin(std::fmax(dm, start.dm - opt.dm_window), start.dm + opt.dm_window);
+    t.dm = std::fmin(std::fmax(dm, 0.0), dm_hi);
     return t;
   };
   RefineEval ev;
@@ -411,5 +414,5 @@ int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
 
 // ------------------------------------------------------------------ C ABI
 extern "C" void psr_refine_options_default(psr_refine_options *out) {
-  if (out) *out = psr_refine_options{128, 64, 40, 1e-3, 0};
+  if (out) *out = psr_refine_options{128, 64, 40, 1e-3, 0, 0.0};
 }

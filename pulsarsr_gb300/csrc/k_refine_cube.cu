@@ -34,50 +34,82 @@ constexpr double K_DM_C = 4148.808;  // dedisperse/src/lib.rs:3
 constexpr int CB_NT = 256;
 constexpr int CB_MAXB = 1024;
 
-// Fold subint s of channel c (one CTA) into C[c][s][*] and the channel's
-// sum / sum of squares.  Thread j takes samples j, j + 256, ...; its phase is
-// anchored in f64 at its first sample and advanced in f32 by 256 samples.
+// Fold subint s of channel c (one CTA) into C[c][s][*] (the row's mean
+// removed, which leaves every shifted profile's deviations unchanged and keeps
+// f32 sums accurate) and the channel's sum / sum of squares.  Tiles of
+// CB_NT x CB_RUN samples are loaded coalesced into shared memory (one pad word
+// per CB_RUN so that per-thread runs are free of bank conflicts); thread j
+// then folds the run [j*CB_RUN, (j+1)*CB_RUN) of the tile, its phase anchored
+// in f64 at the run's first sample and advanced in f32, summing consecutive
+// samples of the same bin in registers and issuing shared-memory atomics only
+// when the bin changes (slow pulsars stay in one bin for many samples).
+constexpr int CB_RUN = 32;
+constexpr int CB_TILE = CB_NT * CB_RUN;
+
 template <class T>
 __global__ void __launch_bounds__(CB_NT)
     k_cube_fold(const T *__restrict__ x, uint64_t ld, uint64_t n, int S, int B, double tsamp,
                 double nu, double nudot, const double *__restrict__ tau,
                 float *__restrict__ cube, double *__restrict__ chsum) {
   __shared__ float bins[CB_MAXB];
+  __shared__ float tile[CB_TILE + CB_TILE / CB_RUN];
   __shared__ double red[2][CB_NT / 32];
+  __shared__ float mean_s;
   const int s = blockIdx.x;
   const uint64_t c = blockIdx.y;
   for (int b = threadIdx.x; b < B; b += blockDim.x) bins[b] = 0.0f;
-  __syncthreads();
   const uint64_t t0 = (n * (uint64_t)s) / (uint64_t)S, t1 = (n * (uint64_t)(s + 1)) / (uint64_t)S;
   const T *row = x + c * ld;
   const double tc = tau[c];
+  const float fB = (float)B;
   double sum = 0.0, sq = 0.0;
-  const uint64_t first = t0 + threadIdx.x;
-  if (first < t1) {
-    const double td = (double)first * tsamp - tc;
-    const double ph = nu * td + 0.5 * nudot * td * td;
-    float u = (float)((ph - floor(ph)) * (double)B);
-    const float step =
-        (float)(((nu + nudot * td) * tsamp * (double)CB_NT - floor((nu + nudot * td) * tsamp *
-                                                                    (double)CB_NT)) *
-                (double)B);
-    const float fB = (float)B;
-    for (uint64_t t = first; t < t1; t += CB_NT) {
-      const float v = (float)row[t];
+  for (uint64_t base = t0; base < t1; base += CB_TILE) {
+    const int len = (int)min((uint64_t)CB_TILE, t1 - base);
+    __syncthreads();  // previous tile consumed (and bins zeroed on entry)
+    for (int i = threadIdx.x; i < len; i += CB_NT) {
+      const float v = (float)row[base + i];
+      tile[i + i / CB_RUN] = v;
       sum += (double)v;
       sq += (double)v * (double)v;
-      float fl = floorf(u);
-      int b0 = (int)fl;
-      float w = u - fl;
-      if (b0 >= B) {
-        b0 = 0;
-        w = 0.0f;
+    }
+    __syncthreads();
+    const int r0 = threadIdx.x * CB_RUN;
+    if (r0 < len) {
+      const int r1 = min(r0 + CB_RUN, len);
+      const double td = (double)(base + r0) * tsamp - tc;
+      const double ph = nu * td + 0.5 * nudot * td * td;
+      float u = (float)((ph - floor(ph)) * (double)B);
+      const double dps = (nu + nudot * td) * tsamp;  // cycles per sample
+      const float du = (float)((dps - floor(dps)) * (double)B);
+      int cur = -1;
+      float a0 = 0.0f, a1 = 0.0f;
+      const float *run = tile + threadIdx.x * (CB_RUN + 1);
+      for (int i = r0; i < r1; ++i) {
+        const float v = run[i - r0];
+        float fl = floorf(u);
+        int b0 = (int)fl;
+        float w = u - fl;
+        if (b0 >= B) {
+          b0 = 0;
+          w = 0.0f;
+        }
+        if (b0 != cur) {
+          if (cur >= 0) {
+            atomicAdd(&bins[cur], a0);
+            atomicAdd(&bins[cur + 1 == B ? 0 : cur + 1], a1);
+          }
+          cur = b0;
+          a0 = a1 = 0.0f;
+        }
+        a0 += (1.0f - w) * v;
+        a1 += w * v;
+        u += du;
+        if (u >= fB) u -= fB;
       }
-      const int b1 = b0 + 1 == B ? 0 : b0 + 1;
-      atomicAdd(&bins[b0], (1.0f - w) * v);
-      atomicAdd(&bins[b1], w * v);
-      u += step;
-      if (u >= fB) u -= fB;
+      if (cur >= 0) {
+        atomicAdd(&bins[cur], a0);
+        atomicAdd(&bins[cur + 1 == B ? 0 : cur + 1], a1);
+      }
     }
   }
   for (int o = 16; o; o >>= 1) {
@@ -89,13 +121,15 @@ __global__ void __launch_bounds__(CB_NT)
     red[1][threadIdx.x >> 5] = sq;
   }
   __syncthreads();
-  float *dst = cube + (c * (uint64_t)S + (uint64_t)s) * (uint64_t)B;
-  for (int b = threadIdx.x; b < B; b += blockDim.x) dst[b] = bins[b];
   if (threadIdx.x < 2) {
     double a = 0.0;
     for (int w2 = 0; w2 < CB_NT / 32; ++w2) a += red[threadIdx.x][w2];
     chsum[(c * (uint64_t)S + (uint64_t)s) * 2 + threadIdx.x] = a;
+    if (threadIdx.x == 0) mean_s = (float)(a / (double)B);
   }
+  __syncthreads();
+  float *dst = cube + (c * (uint64_t)S + (uint64_t)s) * (uint64_t)B;
+  for (int b = threadIdx.x; b < B; b += blockDim.x) dst[b] = bins[b] - mean_s;
 }
 
 struct CandDev {
@@ -113,79 +147,95 @@ __device__ __forceinline__ double cube_shift(const CandDev &q, double nu_r, doub
   return (phq - phr) * B;
 }
 
-// Profiles of every candidate: CTA (chunk of (c, s) rows, candidate) adds
-// its rows' shifted, interpolated bins into a shared profile, then into
-// prof[cand][b] (double atomics; order-dependent in the last bits only).
+// Shift of row r = (c, s) for a candidate, in bins: integer part mod B and
+// fraction, plus T_s - tau_c(candidate DM) for the gradient.
+__device__ __forceinline__ void row_shift(const CandDev &q, double nu_r, double nudot_r,
+                                          double dm_r, double Tsub, const double *kc, int S,
+                                          int B, uint64_t r, int &kk, float &f, double &tdq,
+                                          double &kcc) {
+  const uint64_t c = r / (uint64_t)S;
+  const int s = (int)(r % (uint64_t)S);
+  const double Ts = ((double)s + 0.5) * Tsub;
+  kcc = kc[c];
+  const double d = cube_shift(q, nu_r, nudot_r, dm_r, Ts, kcc, (double)B, tdq);
+  const double fl = floor(d);
+  f = (float)(d - fl);
+  long long k = (long long)fl % B;
+  if (k < 0) k += B;
+  kk = (int)k;
+}
+
+// Profiles of every candidate: CTA (chunk of rows, candidate) adds its rows'
+// shifted, linearly interpolated bins into a shared f32 profile, then into
+// prof[cand][b] (f64 atomics).
+constexpr int CB_ROWS = 64;
 __global__ void __launch_bounds__(CB_NT)
     k_cube_profile(const float *__restrict__ cube, uint64_t rows, int S, int B,
                    const double *__restrict__ kc, double Tsub, double nu_r, double nudot_r,
-                   double dm_r, const CandDev *__restrict__ cands, int rows_per_cta,
-                   double *__restrict__ prof) {
-  __shared__ double acc[CB_MAXB];
+                   double dm_r, const CandDev *__restrict__ cands, double *__restrict__ prof) {
+  __shared__ float acc[CB_MAXB];
+  __shared__ int ks[CB_ROWS];
+  __shared__ float fs[CB_ROWS];
   const int k = blockIdx.y;
   const CandDev q = cands[k];
-  for (int b = threadIdx.x; b < B; b += blockDim.x) acc[b] = 0.0;
-  __syncthreads();
-  const uint64_t r0 = (uint64_t)blockIdx.x * rows_per_cta;
-  const uint64_t r1 = min(r0 + (uint64_t)rows_per_cta, rows);
-  for (uint64_t r = r0; r < r1; ++r) {
-    const uint64_t c = r / (uint64_t)S;
-    const int s = (int)(r % (uint64_t)S);
-    const double Ts = ((double)s + 0.5) * Tsub;
-    double tdq;
-    const double d = cube_shift(q, nu_r, nudot_r, dm_r, Ts, kc[c], (double)B, tdq);
-    const double fl = floor(d);
-    const double f = d - fl;
-    long long kk = (long long)fl % B;
-    if (kk < 0) kk += B;
-    const float *row = cube + r * (uint64_t)B;
-    for (int b = threadIdx.x; b < B; b += blockDim.x) {
-      int i0 = b - (int)kk;
-      if (i0 < 0) i0 += B;
-      const int i1 = i0 == 0 ? B - 1 : i0 - 1;
-      acc[b] += (1.0 - f) * (double)row[i0] + f * (double)row[i1];
-    }
+  const uint64_t r0 = (uint64_t)blockIdx.x * CB_ROWS;
+  const int nr = (int)min((uint64_t)CB_ROWS, rows - r0);
+  for (int b = threadIdx.x; b < B; b += blockDim.x) acc[b] = 0.0f;
+  if (threadIdx.x < nr) {
+    double tdq, kcc;
+    row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r0 + threadIdx.x, ks[threadIdx.x],
+              fs[threadIdx.x], tdq, kcc);
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < B; b += blockDim.x) atomicAdd(&prof[(uint64_t)k * B + b], acc[b]);
+  for (int b = threadIdx.x; b < B; b += blockDim.x) {
+    float a = 0.0f;
+    for (int i = 0; i < nr; ++i) {
+      const float *row = cube + (r0 + i) * (uint64_t)B;
+      int i0 = b - ks[i];
+      if (i0 < 0) i0 += B;
+      const int i1 = i0 == 0 ? B - 1 : i0 - 1;
+      const float f = fs[i];
+      a += (1.0f - f) * row[i0] + f * row[i1];
+    }
+    acc[b] = a;
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < B; b += blockDim.x)
+    atomicAdd(&prof[(uint64_t)k * B + b], (double)acc[b]);
 }
 
 // Gradient: each warp takes rows; lanes split the bins of a row.
 __global__ void __launch_bounds__(CB_NT)
     k_cube_grad(const float *__restrict__ cube, uint64_t rows, int S, int B,
                 const double *__restrict__ kc, double Tsub, double nu_r, double nudot_r,
-                double dm_r, const CandDev *__restrict__ cands, const double *__restrict__ g,
+                double dm_r, const CandDev *__restrict__ cands, const float *__restrict__ g,
                 double *__restrict__ grad) {
   __shared__ double red[3][CB_NT / 32];
   const int k = blockIdx.y;
   const CandDev q = cands[k];
-  const double *gk = g + (uint64_t)k * B;
+  const float *gk = g + (uint64_t)k * B;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = (int)(gridDim.x * (CB_NT / 32));
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   for (uint64_t r = (uint64_t)blockIdx.x * (CB_NT / 32) + warp; r < rows; r += nwarps) {
-    const uint64_t c = r / (uint64_t)S;
-    const int s = (int)(r % (uint64_t)S);
-    const double Ts = ((double)s + 0.5) * Tsub;
-    double tdq;
-    const double d = cube_shift(q, nu_r, nudot_r, dm_r, Ts, kc[c], (double)B, tdq);
-    const double fl = floor(d);
-    long long kk = (long long)fl % B;
-    if (kk < 0) kk += B;
+    int kk;
+    float f;
+    double tdq, kcc;
+    row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r, kk, f, tdq, kcc);
     const float *row = cube + r * (uint64_t)B;
-    double dd = 0.0;
+    float dd = 0.0f;
     for (int b = lane; b < B; b += 32) {
-      int i0 = b - (int)kk;
+      int i0 = b - kk;
       if (i0 < 0) i0 += B;
       const int i1 = i0 == 0 ? B - 1 : i0 - 1;
-      dd += gk[b] * ((double)row[i1] - (double)row[i0]);
+      dd += gk[b] * (row[i1] - row[i0]);
     }
     for (int o = 16; o; o >>= 1) dd += __shfl_down_sync(0xffffffffu, dd, o);
     if (lane == 0) {
-      const double Bd = (double)B;
-      a0 += dd * Bd * tdq;
-      a1 += dd * Bd * 0.5 * tdq * tdq;
-      a2 += dd * (-Bd * (q.nu + q.nudot * tdq) * kc[c]);
+      const double Bd = (double)B, ddd = (double)dd;
+      a0 += ddd * Bd * tdq;
+      a1 += ddd * Bd * 0.5 * tdq * tdq;
+      a2 += ddd * (-Bd * (q.nu + q.nudot * tdq) * kcc);
     }
   }
   if (lane == 0) {
@@ -276,13 +326,13 @@ int eval_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu_r, double 
                            st));
   PSR_CUDA(cudaMemsetAsync(w.prof.p, 0, (size_t)K * B * 8, st));
   PSR_CUDA(cudaMemsetAsync(w.grad.p, 0, (size_t)K * 3 * 8, st));
-  const int rows_per_cta = 64;
-  dim3 gp((unsigned)((w.rows + rows_per_cta - 1) / rows_per_cta), (unsigned)K);
+  dim3 gp((unsigned)((w.rows + CB_ROWS - 1) / CB_ROWS), (unsigned)K);
   k_cube_profile<<<gp, CB_NT, 0, st>>>(w.cube.as<float>(), w.rows, S, B, w.kc.as<double>(), Tsub,
-                                       nu_r, nudot_r, dm_r, w.cands.as<CandDev>(), rows_per_cta,
+                                       nu_r, nudot_r, dm_r, w.cands.as<CandDev>(),
                                        w.prof.as<double>());
   PSR_CUDA(cudaGetLastError());
-  std::vector<double> p((size_t)K * B), g((size_t)K * B);
+  std::vector<double> p((size_t)K * B);
+  std::vector<float> g((size_t)K * B);
   PSR_CUDA(cudaMemcpyAsync(p.data(), w.prof.p, p.size() * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
   const double norm = (double)n * w.var;
@@ -295,14 +345,14 @@ int eval_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu_r, double 
     for (int b = 0; b < B; ++b) {
       const double d = p[(size_t)k * B + b] - mean;
       j += d * d;
-      g[(size_t)k * B + b] = 2.0 * d / norm;
+      g[(size_t)k * B + b] = (float)(2.0 * d / norm);
     }
     J[k] = j / norm;
   }
-  PSR_CUDA(cudaMemcpyAsync(w.g.p, g.data(), g.size() * 8, cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(w.g.p, g.data(), g.size() * 4, cudaMemcpyHostToDevice, st));
   dim3 gg((unsigned)std::min<uint64_t>((w.rows + 7) / 8, 2048), (unsigned)K);
   k_cube_grad<<<gg, CB_NT, 0, st>>>(w.cube.as<float>(), w.rows, S, B, w.kc.as<double>(), Tsub,
-                                    nu_r, nudot_r, dm_r, w.cands.as<CandDev>(), w.g.as<double>(),
+                                    nu_r, nudot_r, dm_r, w.cands.as<CandDev>(), w.g.as<float>(),
                                     w.grad.as<double>());
   PSR_CUDA(cudaGetLastError());
   grad.resize((size_t)K * 3);
@@ -380,7 +430,10 @@ int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, u
     const double nudot0 = -start[k].pdot * nu0 * nu0;
     c.nu = nu0 + (2.0 * q[0] - 4.0 * q[1]) / (Bd * T);
     c.nudot = nudot0 + 8.0 * q[1] / (Bd * T * T);
-    c.dm = std::fmin(std::fmax(start[k].dm + q[2] * s3, 0.0), dm_hi);
+    double dm = start[k].dm + q[2] * s3;
+    if (opt.dm_window > 0.0)
+      dm = std::fmin(std::fmax(dm, start[k].dm - opt.dm_window), start[k].dm + opt.dm_window);
+    c.dm = std::fmin(std::fmax(dm, 0.0), dm_hi);
     return c;
   };
   std::vector<double> J, grad;

@@ -12,6 +12,7 @@ struct RefineOptions {
   uint64_t max_evals = 40;
   double tol = 1e-3;  // stop when a step moves every parameter by < tol phase bins
   bool exact = false;  // optimise the filterbank objective itself (no cube)
+  double dm_window = 0.0;  // > 0: keep DM within start +- dm_window
 };
 
 struct RefineEval {

@@ -67,11 +67,12 @@ class Timing(C.Structure):
 
 class RefineOptions(C.Structure):
     _fields_ = [("bins", C.c_uint64), ("subints", C.c_uint64), ("max_evals", C.c_uint64),
-                ("tol_bins", C.c_double), ("exact", C.c_int32)]
+                ("tol_bins", C.c_double), ("exact", C.c_int32), ("dm_window", C.c_double)]
 
     @staticmethod
-    def make(bins=128, subints=64, max_evals=40, tol_bins=1e-3, exact=False) -> "RefineOptions":
-        return RefineOptions(bins, subints, max_evals, tol_bins, 1 if exact else 0)
+    def make(bins=128, subints=64, max_evals=40, tol_bins=1e-3, exact=False,
+             dm_window=0.0) -> "RefineOptions":
+        return RefineOptions(bins, subints, max_evals, tol_bins, 1 if exact else 0, dm_window)
 
 
 TIMING_DTYPE = np.dtype([("period_s", "<f8"), ("pdot", "<f8"), ("dm", "<f8")])
@@ -96,7 +97,8 @@ def refine_objective(fb, n: int, period: float, pdot: float, dm: float, bins: in
 
 
 def refine_gradient(fb, n: int, starts, bins: int = 128, subints: int = 64,
-                    max_evals: int = 40, tol_bins: float = 1e-3, exact: bool = False):
+                    max_evals: int = 40, tol_bins: float = 1e-3, exact: bool = False,
+                    dm_window: float = 0.0):
     """Gradient refinement of every starting point (a TIMING_DTYPE array or
     (P, Pdot, DM) tuples); returns (refined, J, evaluations).  exact=False
     optimises on a folded cube per group of nearby starts, exact=True on the
@@ -105,7 +107,7 @@ def refine_gradient(fb, n: int, starts, bins: int = 128, subints: int = 64,
     out = np.zeros_like(s)
     J = np.zeros(s.size)
     ev = np.zeros(s.size, dtype=np.uint64)
-    opt = RefineOptions.make(bins, subints, max_evals, tol_bins, exact)
+    opt = RefineOptions.make(bins, subints, max_evals, tol_bins, exact, dm_window)
     check(lib().psr_refine_gradient(fb.handle, C.c_uint64(n), s.ctypes.data_as(C.c_void_p),
                                     C.c_uint64(s.size), C.byref(opt),
                                     out.ctypes.data_as(C.c_void_p),
