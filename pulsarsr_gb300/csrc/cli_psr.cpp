@@ -4,6 +4,8 @@
 //   psr fold FILE --period P --dm DM [--bins 64] [--out output_fold]
 //   psr dedisperse FILE --dm DM [--out output]
 //   psr inspect FILE [--out output] [--max-samples N]
+//   psr synth FILE [--samples 65536] [--channels 32] [--tsamp 0.00025]
+//              [--period 0.032] [--dm 62] [--amplitude 0.5] [--duty 0.05] [--seed 42]
 //   psr search FILE [--dm-min 0] [--dm-max 500] [--dm-step S] [--min-hz 15]
 //              [--max-hz 2000] [--threshold 8] [--top 5] [--bins 64] [--no-rfi]
 //              [--birdie HZ:HALF_WIDTH_HZ]... [--max-samples N] [--threads N]
@@ -193,7 +195,8 @@ struct Args {
 
 Args parse_args(int argc, char **argv) {
   Args a;
-  if (argc < 2) throw Fail("usage: psr <header|fold|dedisperse|inspect|search> FILE [options]");
+  if (argc < 2)
+    throw Fail("usage: psr <header|fold|dedisperse|inspect|search|synth> FILE [options]");
   a.cmd = argv[1];
   for (int i = 2; i < argc; ++i) {
     std::string s = argv[i];
@@ -359,6 +362,99 @@ int cmd_inspect(const Args &a) {
   open_fb(fb, a.file, a.has("max-samples") ? (int64_t)a.count("max-samples", 0) : -1);
   make_dirs(out);
   write_json(join(out, "header.json"), header_value(fb.bytes));
+  return 0;
+}
+
+// main.rs:341-367 and fbank::write (fbank/src/lib.rs:216-250): a 32-bit
+// filterbank (keywords in sorted order, time-major samples) and
+// FILE.truth.json with the configuration.  The samples come from the device
+// generator (psr_fb_synth): same signal model and header, different noise
+// stream than the reference's ChaCha8 generator.
+int cmd_synth(const Args &a) {
+  const uint64_t samples = a.count("samples", 65536), channels = a.count("channels", 32);
+  const double tsamp = a.num("tsamp", 0.00025), period = a.num("period", 0.032);
+  const double dm = a.num("dm", 62.0), amplitude = a.num("amplitude", 0.5);
+  const double duty = a.num("duty", 0.05);
+  const uint64_t seed = a.count("seed", 42);
+  const double fch1 = 1450.0, foff = -4.0;
+  if (samples < 2 || channels < 1 || !std::isfinite(period) || period <= 0.0 ||
+      !std::isfinite(duty) || duty <= 0.0 || duty >= 0.5 || !std::isfinite(amplitude) ||
+      amplitude < 0.0)
+    throw Fail("invalid synthetic configuration");
+  {
+    std::vector<double> f(channels);
+    for (uint64_t c = 0; c < channels; ++c) f[c] = fch1 + (double)c * foff;
+    std::vector<uint64_t> d(channels);
+    check(psr_delays(f.data(), f.size(), tsamp, dm, d.data()));
+  }
+  psr_synth_pulsar p{period, 0.0, dm, duty, amplitude, 0.25};
+  psr_synth_config cfg{(int64_t)channels, 32, samples, tsamp, fch1, foff, seed,
+                       100.0, 1.0, 0.0, &p, 1};
+  psr_fb *fb = nullptr;
+  check(psr_fb_synth(&cfg, &fb));
+  std::vector<float> data(channels * samples);
+  const int rc = psr_fb_download(fb, data.data());
+  psr_fb_free(fb);
+  check(rc);
+  std::ofstream f(a.file, std::ios::binary);
+  if (!f) throw Fail("cannot write " + a.file);
+  auto put_i32 = [&](int32_t v) {
+    uint8_t b[4];
+    for (int i = 0; i < 4; ++i) b[i] = (uint8_t)((uint32_t)v >> (8 * i));
+    f.write(reinterpret_cast<const char *>(b), 4);
+  };
+  auto put_f64 = [&](double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    uint8_t b[8];
+    for (int i = 0; i < 8; ++i) b[i] = (uint8_t)(u >> (8 * i));
+    f.write(reinterpret_cast<const char *>(b), 8);
+  };
+  auto put_str = [&](const std::string &t) {
+    put_i32((int32_t)t.size());
+    f.write(t.data(), (std::streamsize)t.size());
+  };
+  put_str("HEADER_START");
+  // BTreeMap order: data_type, fch1, foff, nbits, nchans, nifs, signed,
+  // source_name, tsamp.
+  put_str("data_type"); put_i32(1);
+  put_str("fch1"); put_f64(fch1);
+  put_str("foff"); put_f64(foff);
+  put_str("nbits"); put_i32(32);
+  put_str("nchans"); put_i32((int32_t)channels);
+  put_str("nifs"); put_i32(1);
+  put_str("signed"); put_i32(0);
+  put_str("source_name"); put_str("seeded synthetic pulsar");
+  put_str("tsamp"); put_f64(tsamp);
+  put_str("HEADER_END");
+  std::vector<uint8_t> frame(channels * 4);
+  for (uint64_t t = 0; t < samples; ++t) {
+    for (uint64_t c = 0; c < channels; ++c) {
+      uint32_t u;
+      std::memcpy(&u, &data[c * samples + t], 4);
+      for (int i = 0; i < 4; ++i) frame[c * 4 + i] = (uint8_t)(u >> (8 * i));
+    }
+    f.write(reinterpret_cast<const char *>(frame.data()), (std::streamsize)frame.size());
+  }
+  f.close();
+  std::string truth = a.file;
+  const size_t dot = truth.find_last_of('.'), slash = truth.find_last_of('/');
+  if (dot != std::string::npos && (slash == std::string::npos || dot > slash))
+    truth = truth.substr(0, dot);
+  truth += ".truth.json";
+  Value j = Value::object();
+  j.set("nsamples", Value::u64(samples));
+  j.set("nchans", Value::u64(channels));
+  j.set("tsamp", Value::num(tsamp));
+  j.set("fch1", Value::num(fch1));
+  j.set("foff", Value::num(foff));
+  j.set("period_s", Value::num(period));
+  j.set("dm", Value::num(dm));
+  j.set("duty_cycle", Value::num(duty));
+  j.set("amplitude", Value::num(amplitude));
+  j.set("seed", Value::u64(seed));
+  write_json(truth, j);
+  std::printf("Wrote %s and truth metadata\n", a.file.c_str());
   return 0;
 }
 
@@ -550,6 +646,7 @@ int main(int argc, char **argv) {
     if (a.cmd == "dedisperse") return cmd_dedisperse(a);
     if (a.cmd == "inspect") return cmd_inspect(a);
     if (a.cmd == "search") return cmd_search(a);
+    if (a.cmd == "synth") return cmd_synth(a);
     throw Fail("unrecognized subcommand '" + a.cmd + "'");
   } catch (const std::exception &e) {
     std::fprintf(stderr, "Error: %s\n", e.what());

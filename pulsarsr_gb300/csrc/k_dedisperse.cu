@@ -84,7 +84,7 @@ struct StageInfo {
 // Run by warp 0: lane i stages row c0+i.
 template <int DB>
 __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns,
-                            uint64_t nch, const uint32_t *__restrict__ delays,
+                            uint64_t nch, uint64_t dstride, const uint32_t *__restrict__ delays,
                             uint64_t ntrials, uint64_t d0, uint64_t t0, uint64_t c0, int cc,
                             uint8_t *buf, int rowcap, StageInfo *info, uint64_t *bar) {
   const int lane = threadIdx.x & 31;
@@ -94,7 +94,7 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
     uint32_t dmin = 0xffffffffu, dmax = 0;
     for (int d = 0; d < DB; ++d) {
       uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
-      uint32_t v = delays[tr * nch + c];
+      uint32_t v = delays[tr * dstride + c];
       dmin = min(dmin, v);
       dmax = max(dmax, v);
     }
@@ -122,9 +122,9 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
 template <bool BYTE_LANES, int DB>
 __global__ void __launch_bounds__(DD_NT, 2)
     k_dedisp_u8(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
-                const uint32_t *__restrict__ delays, uint64_t ntrials, uint64_t n,
-                float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
-                uint64_t ntiles, int cc, int rowcap, int group, unsigned *err) {
+                uint64_t dstride, const uint32_t *__restrict__ delays, uint64_t ntrials,
+                uint64_t n, float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
+                uint64_t ntiles, int cc, int rowcap, int group, int accumulate, unsigned *err) {
   extern __shared__ __align__(128) uint8_t smem[];
   uint8_t *bufs[2] = {smem, smem + (size_t)cc * rowcap};
   __shared__ uint64_t bars[2];
@@ -143,10 +143,10 @@ __global__ void __launch_bounds__(DD_NT, 2)
   }
   __syncthreads();
   if (tl < 32) {
-    issue_stage<DB>(s, ld, ns, nch, delays, ntrials, d0, t0, 0, cc, bufs[0], rowcap, &info[0],
+    issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, 0, cc, bufs[0], rowcap, &info[0],
                 &bars[0]);
     if (nchunks > 1)
-      issue_stage<DB>(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)cc, cc, bufs[1], rowcap,
+      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)cc, cc, bufs[1], rowcap,
                   &info[1], &bars[1]);
   }
 
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(DD_NT, 2)
 #pragma unroll
       for (int d = 0; d < DB; ++d) {
         const uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
-        const int off = rel0 + (int)__ldg(&delays[tr * nch + c]);
+        const int off = rel0 + (int)__ldg(&delays[tr * dstride + c]);
         if (off != prev) {  // uniform across the CTA
           prev = off;
           const int q = tl + (off >> 4);
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(DD_NT, 2)
     __syncthreads();  // every thread is done reading buffer b
     if (tl < 32 && k + 2 < nchunks) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue_stage<DB>(s, ld, ns, nch, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc, cc,
+      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc, cc,
                   bufs[b], rowcap, &info[b], &bars[b]);
     }
   }
@@ -263,15 +263,26 @@ __global__ void __launch_bounds__(DD_NT, 2)
       local += (in0 ? lo : 0u) + (in1 ? hi : 0u);
     }
     if (tr < ntrials) {
+      // Channel groups after the first add their (integer) partial sums to
+      // the earlier groups' in f32: exact while every sum stays below 2^24.
       float *dst = out + tr * ldo + tb;
       if (tb + 16 <= n) {
         float4 *d4 = reinterpret_cast<float4 *>(dst);
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          d4[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        for (int i = 0; i < 4; ++i) {
+          float4 w = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+          if (accumulate) {
+            const float4 o = d4[i];
+            w.x += o.x;
+            w.y += o.y;
+            w.z += o.z;
+            w.w += o.w;
+          }
+          d4[i] = w;
+        }
       } else {
         for (int i = 0; i < 16; ++i)
-          if (tb + i < n) dst[i] = v[i];
+          if (tb + i < n) dst[i] = accumulate ? dst[i] + v[i] : v[i];
       }
     }
 #pragma unroll
@@ -282,7 +293,8 @@ __global__ void __launch_bounds__(DD_NT, 2)
   if (tl < DB && d0 + tl < ntrials) {
     unsigned long long t = 0;
     for (int w = 0; w < DD_NT / 32; ++w) t += wsum[w][tl];
-    part[(d0 + tl) * ntiles + blockIdx.x] = (double)t;
+    double *pp = &part[(d0 + tl) * ntiles + blockIdx.x];
+    *pp = accumulate ? *pp + (double)t : (double)t;
   }
 }
 
@@ -364,7 +376,12 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part,
                          double *d_sums, float *d_means, uint64_t max_spread, unsigned *d_err,
                          cudaStream_t st) {
-  const bool packed = o.kind == SAMPLE_U8 && (double)o.nch * o.max_value() <= 65535.0;
+  // Integer samples: channel groups small enough that a group's sum fits the
+  // 16-bit lanes (nch * max <= 65535 when there is one group); the groups'
+  // sums are added in f32, exact while the total stays below 2^24.
+  const double maxv = o.kind == SAMPLE_U8 ? o.max_value() : 0.0;
+  const uint64_t gch = maxv > 0.0 ? (uint64_t)(65535.0 / maxv) : 0;
+  const bool packed = o.kind == SAMPLE_U8 && gch >= 1 && (double)o.nch * maxv < 16777216.0;
   if (packed) {
     const uint64_t ntiles = (n + DD_TT - 1) / DD_TT;
     int rowcap = (int)(((uint64_t)DD_TT + max_spread + 32 + 15) & ~(uint64_t)15);
@@ -376,26 +393,34 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
     int smsm = 0;
     cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     size_t budget = std::min((size_t)smax, (size_t)smsm / 2) - 4096;
-    int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, o.nch, budget / (2 * (size_t)rowcap)});
+    const uint64_t glen = std::min<uint64_t>(gch, o.nch);
+    int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, glen, budget / (2 * (size_t)rowcap)});
     if (cc >= 1) {
       size_t smem = 2 * (size_t)cc * rowcap;
-      const int group = (int)(255.0 / o.max_value());
-      if (group >= 2) {
-        dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB8 - 1) / DD_DB8));
-        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<true, DD_DB8>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_dedisp_u8<true, DD_DB8><<<grid, DD_NT, smem, st>>>(
-            o.samples.as<uint8_t>(), o.ld, o.ns, o.nch, d_delays, ntrials, n, d_out, ldo, d_part,
-            ntiles, cc, rowcap, group, d_err);
-      } else {
-        dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
-        PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false, DD_DB>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_dedisp_u8<false, DD_DB><<<grid, DD_NT, smem, st>>>(
-            o.samples.as<uint8_t>(), o.ld, o.ns, o.nch, d_delays, ntrials, n, d_out, ldo, d_part,
-            ntiles, cc, rowcap, 1, d_err);
+      const int group = (int)(255.0 / maxv);
+      for (uint64_t c0 = 0; c0 < o.nch; c0 += glen) {
+        const uint64_t ng = std::min(glen, o.nch - c0);
+        const uint8_t *sg = o.samples.as<uint8_t>() + c0 * o.ld;
+        const uint32_t *dg = d_delays + c0;
+        const int acc = c0 > 0 ? 1 : 0;
+        const int ccg = (int)std::min<uint64_t>((uint64_t)cc, ng);
+        if (group >= 2) {
+          dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB8 - 1) / DD_DB8));
+          PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<true, DD_DB8>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          k_dedisp_u8<true, DD_DB8><<<grid, DD_NT, smem, st>>>(
+              sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo, d_part, ntiles, ccg, rowcap,
+              group, acc, d_err);
+        } else {
+          dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
+          PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false, DD_DB>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+          k_dedisp_u8<false, DD_DB><<<grid, DD_NT, smem, st>>>(
+              sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo, d_part, ntiles, ccg, rowcap,
+              1, acc, d_err);
+        }
+        PSR_CUDA(cudaGetLastError());
       }
-      PSR_CUDA(cudaGetLastError());
       k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles,
                                                                          ntrials, n, d_sums,
                                                                          d_means);
@@ -429,8 +454,7 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
 }
 
 uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n) {
-  const bool packed = o.kind == SAMPLE_U8 && (double)o.nch * o.max_value() <= 65535.0;
-  return packed ? (n + DD_TT - 1) / DD_TT : (n + DG_TT - 1) / DG_TT;
+  return std::max((n + DD_TT - 1) / DD_TT, (n + DG_TT - 1) / DG_TT);
 }
 
 }  // namespace psr

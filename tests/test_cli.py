@@ -120,3 +120,30 @@ def test_fold_and_dedisperse_outputs(gpu, oracle, psr, tmp_path):
     assert fold["profile"]["counts"] == [int(c) for c in p["counts"]]
     assert np.array_equal(np.array(fold["profile"]["bins"], dtype=np.float32), p["bins"])
     assert fold["searched"] is False
+
+
+@pytest.mark.gpu
+def test_synth_writes_reference_layout_and_searchable_file(gpu, psr, tmp_path):
+    """psr synth (main.rs:341-367): the reference's header keywords, 32-bit
+    time-major samples and FILE.truth.json; the injected pulsar is found."""
+    from pulsarsr_gb300 import fbank
+    fil = tmp_path / "s.fil"
+    r = run(psr, "synth", fil, "--samples", 65536, "--channels", 32, "--seed", 5)
+    assert r.returncode == 0, r.stderr
+    truth = json.loads((tmp_path / "s.truth.json").read_text())
+    assert list(truth) == ["nsamples", "nchans", "tsamp", "fch1", "foff", "period_s", "dm",
+                           "duty_cycle", "amplitude", "seed"]
+    raw = fil.read_bytes()
+    h = json.loads(run(psr, "header", fil).stdout)
+    assert list(h["fields"]) == ["data_type", "fch1", "foff", "nbits", "nchans", "nifs",
+                                 "signed", "source_name", "tsamp"]
+    assert h["nbits"] == 32 and h["nchans"] == 32
+    assert len(raw) == h["data_offset"] + 65536 * 32 * 4
+    x = fbank.decode(raw).data
+    assert abs(float(x.mean()) - 100.0) < 0.05
+    out = tmp_path / "out"
+    r = run(psr, "search", fil, "--dm-max", 120, "--dm-step", 2, "--out", out)
+    assert r.returncode == 0, r.stderr
+    rep = json.loads((out / "report.json").read_text())
+    f = [c["candidate"]["frequency_hz"] for c in rep["confirmation"]["candidates"]]
+    assert any(abs(v * k - 31.25) < 0.05 for v in f for k in (1, 2, 4))

@@ -163,6 +163,25 @@ def test_dedisperse_matches_oracle(gpu, oracle, nbits):
         assert out[i].tobytes() == ref.tobytes(), i
 
 
+def test_dedisperse_many_channels_8bit_groups(gpu, oracle):
+    """600 channels of 8-bit data: the packed kernel runs in channel groups of
+    257 whose sums are added in f32 (exact below 2^24)."""
+    from pulsarsr_gb300 import dedisperse, fbank, synth
+    o = synth.Observation(nchans=600, nbits=8, nsamples=20000, tsamp=64e-6, fch1=1600.,
+                          foff=-400.0 / 600, seed=12, noise_mean=120., noise_sigma=40.,
+                          pulsars=[synth.Pulsar(0.0123, 150.0, 0.04, 0.5)])
+    raw = o.to_bytes()
+    fb = fbank.decode(raw)
+    _, d = oracle.decode(raw)
+    freqs = fb.header.frequencies()
+    trials = dedisperse.plan(0, 100, dedisperse.dm_step(freqs, o.tsamp))[::5]
+    n = 20000 - int(dedisperse.delays(freqs, o.tsamp, trials[-1]).max())
+    out = dedisperse.apply_trials(fb, trials, n)
+    for i in range(0, len(trials), 7):
+        ref = oracle.apply(d, oracle.delays(freqs, o.tsamp, trials[i]), n)
+        assert out[i].tobytes() == ref.tobytes(), i
+
+
 def test_dedisperse_errors(gpu):
     from pulsarsr_gb300 import DedisperseError, dedisperse, fbank
     fb = fbank.decode(fixture(8, [1, 2, 3, 4]))
