@@ -417,6 +417,43 @@ int psr_session_stage_times(psr_session *s, double *ms, uint64_t *launches, int 
  * command, cli/src/main.rs:474-478), on the session's masked observation. */
 int psr_session_analyze(psr_session *s, uint64_t limit, uint64_t bins,
                         const psr_rules *rules, psr_outcome **out);
+/* ------------------------------------------------------------- batch */
+/* Many observations of uneven shape (channels, length, DM plan) searched by
+ * one CUDA graph launch (the examples' serial observation loops,
+ * cli/src/main.rs:462-473 per observation).  No reference counterpart for the
+ * batching itself.  Each observation keeps its own session; psr_batch_run
+ * captures all of them, concurrently, into one graph on first use and
+ * launches that graph afterwards.  hbm_budget_bytes bounds the dedispersed
+ * series and spectra held at once (0: 64 GiB): it sets the trials per
+ * dedispersion block. */
+typedef struct {
+  psr_header header;
+  uint64_t nsamples;
+  const double *trials;
+  uint64_t ntrials;
+  uint64_t discovery;
+  psr_search_config config;
+  uint64_t rfi_block_samples;
+  float rfi_threshold;
+} psr_batch_obs;
+typedef struct psr_batch psr_batch;
+int psr_batch_create(const psr_batch_obs *obs, uint64_t n, uint64_t hbm_budget_bytes,
+                     psr_batch **out);
+int psr_batch_load(psr_batch *b, uint64_t i, const uint8_t *payload, uint64_t nbytes);
+/* Load observation i from an 8-bit device filterbank of the same shape (its
+ * samples packed into the time-major payload on the device). */
+int psr_batch_load_fb(psr_batch *b, uint64_t i, const psr_fb *fb);
+/* Autotuner: times whole searches of every loaded observation at a few
+ * (dedispersion block, FFT chunk) pairs and keeps the fastest; chunk/inner
+ * (n entries each, may be NULL) receive the choices. */
+int psr_batch_tune(psr_batch *b, uint64_t *chunk, uint64_t *inner);
+int psr_batch_run(psr_batch *b);
+int psr_batch_sync(psr_batch *b);
+int psr_batch_candidates(psr_batch *b, uint64_t i, uint64_t *counts, psr_candidate *out,
+                         uint64_t cap, uint64_t *n_total);
+void *psr_batch_stream(psr_batch *b);
+void psr_batch_free(psr_batch *b);
+
 /* Device copy of the packed payload buffer (for device-resident timing). */
 void *psr_session_payload_device(psr_session *s);
 /* The session's CUDA stream (cudaStream_t), for event timing. */

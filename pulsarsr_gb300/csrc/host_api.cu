@@ -325,6 +325,8 @@ struct psr_session {
   float rfi_threshold = 8.0f;
   SearchEngine eng;
   std::vector<double> trials;
+  uint64_t discovery = 0;
+  SpecConfig spec;
   DevBuf errbuf;
   bool have_run = false;
   // unpack / rfi timing (the engine times its own stages)
@@ -1010,8 +1012,9 @@ int psr_session_create(const psr_header *header, uint64_t nsamples, const double
   s->rfi_block = rfi_block_samples;
   s->rfi_threshold = rfi_threshold;
   s->trials.assign(trials, trials + ntrials);
-  PSR_TRY(s->eng.prepare(o, trials, ntrials, discovery, to_spec(cfg, header->tsamp),
-                         s->stream.s));
+  s->discovery = discovery;
+  s->spec = to_spec(cfg, header->tsamp);
+  PSR_TRY(s->eng.prepare(o, trials, ntrials, discovery, s->spec, s->stream.s));
   PSR_TRY(s->errbuf.ensure(8));
   PSR_CUDA(cudaStreamSynchronize(s->stream.s));
   *out = s.release();
@@ -1159,5 +1162,229 @@ int psr_session_analyze(psr_session *s, uint64_t limit, uint64_t bins, const psr
 }
 
 void psr_session_free(psr_session *s) { delete s; }
+
+// ------------------------------------------------------------------ batch
+// Many observations of uneven shape searched by one CUDA graph: each
+// observation is a session (its own stream and buffers); the first run after
+// any change of the work captures every session's whole pipeline (unpack,
+// RFI, all trial chunks) into one graph whose branches run concurrently;
+// later runs launch that graph.
+struct psr_batch {
+  std::vector<std::unique_ptr<psr_session>> obs;
+  Stream main;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaEvent_t> events;
+  bool warm = false;
+  std::vector<uint64_t> chunk, inner;  // chosen by psr_batch_tune (0: defaults)
+  ~psr_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+  }
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    warm = false;
+  }
+};
+
+namespace {
+// Trials per dedispersion launch so that the batch's dedispersed series and
+// spectra stay within `budget` bytes of HBM (at least 16 per observation).
+uint64_t chunk_for_budget(const psr_batch_obs *obs, uint64_t n, double budget) {
+  double per_trial = 0.0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint64_t len = obs[i].discovery;
+    uint64_t p = 1;
+    while (p < len) p <<= 1;
+    per_trial += 4.0 * (double)series_ld(len) + 4.0 * (double)(p + 64);
+  }
+  const double c = per_trial > 0.0 ? budget / per_trial : 256.0;
+  return (uint64_t)std::max(16.0, std::min(256.0, std::floor(c)));
+}
+
+int reprepare(psr_session *s, uint64_t chunk, uint64_t inner) {
+  s->eng.chunk = chunk;
+  s->eng.inner = inner;
+  PSR_TRY(s->eng.prepare(s->o, s->trials.data(), s->trials.size(), s->discovery, s->spec,
+                         s->stream.s));
+  PSR_CUDA(cudaStreamSynchronize(s->stream.s));
+  return PSR_OK;
+}
+}  // namespace
+
+int psr_batch_create(const psr_batch_obs *obs, uint64_t n, uint64_t hbm_budget_bytes,
+                     psr_batch **out) {
+  if (!obs || n == 0 || !out) {
+    set_error("batch: invalid arguments");
+    return PSR_EINVAL;
+  }
+  std::unique_ptr<psr_batch> b(new psr_batch());
+  const double budget = hbm_budget_bytes ? (double)hbm_budget_bytes : 64.0 * (1ull << 30);
+  const uint64_t chunk = chunk_for_budget(obs, n, budget);
+  for (uint64_t i = 0; i < n; ++i) {
+    const psr_batch_obs &q = obs[i];
+    psr_session *s = nullptr;
+    PSR_TRY(psr_session_create(&q.header, q.nsamples, q.trials, q.ntrials, q.discovery, &q.config,
+                               q.rfi_block_samples, q.rfi_threshold, &s));
+    b->obs.emplace_back(s);
+    if (chunk < std::min<uint64_t>(256, q.ntrials)) PSR_TRY(reprepare(s, chunk, 0));
+    b->chunk.push_back(s->eng.chunk);
+    b->inner.push_back(s->eng.inner);
+  }
+  *out = b.release();
+  return PSR_OK;
+}
+
+int psr_batch_load(psr_batch *b, uint64_t i, const uint8_t *payload, uint64_t nbytes) {
+  if (!b || i >= b->obs.size()) {
+    set_error("batch: observation index out of range");
+    return PSR_EINVAL;
+  }
+  return psr_session_load(b->obs[i].get(), payload, nbytes);
+}
+
+int psr_batch_load_fb(psr_batch *b, uint64_t i, const psr_fb *fb) {
+  if (!b || i >= b->obs.size() || !fb) {
+    set_error("batch: observation index out of range");
+    return PSR_EINVAL;
+  }
+  psr_session *s = b->obs[i].get();
+  if (fb->o.nch != s->o.nch || fb->o.ns != s->o.ns || s->o.h.nbits != 8) {
+    set_error("batch: the filterbank's shape differs from the observation's");
+    return PSR_EINVAL;
+  }
+  PSR_CUDA(cudaStreamSynchronize(fb->stream.s));
+  PSR_TRY(pack_payload_u8(fb->o, s->o.payload.as<uint8_t>(), s->stream.s));
+  PSR_CUDA(cudaStreamSynchronize(s->stream.s));
+  return PSR_OK;
+}
+
+// Autotuner: for every observation, time one whole search at each (DM block,
+// FFT chunk) pair of a small set around the defaults, on the loaded data,
+// and keep the fastest.  Results per observation are in chunk/inner.
+int psr_batch_tune(psr_batch *b, uint64_t *chunk_out, uint64_t *inner_out) {
+  if (!b) {
+    set_error("batch: null handle");
+    return PSR_EINVAL;
+  }
+  b->drop_graph();
+  for (size_t i = 0; i < b->obs.size(); ++i) {
+    psr_session *s = b->obs[i].get();
+    const uint64_t c0 = b->chunk[i];
+    std::vector<std::pair<uint64_t, uint64_t>> cand;
+    for (uint64_t c : {c0, std::max<uint64_t>(16, c0 / 2)})
+      for (uint64_t inner : {(uint64_t)0, (uint64_t)4, (uint64_t)8})
+        cand.emplace_back(c, inner);
+    double best = 1e300;
+    std::pair<uint64_t, uint64_t> pick{c0, 0};
+    cudaEvent_t e0, e1;
+    PSR_CUDA(cudaEventCreate(&e0));
+    PSR_CUDA(cudaEventCreate(&e1));
+    for (const auto &c : cand) {
+      PSR_TRY(reprepare(s, c.first, c.second));
+      PSR_TRY(psr_session_run(s));  // warm (first use of the new buffers)
+      PSR_TRY(psr_session_sync(s));
+      PSR_CUDA(cudaEventRecord(e0, s->stream.s));
+      PSR_TRY(psr_session_run(s));
+      PSR_CUDA(cudaEventRecord(e1, s->stream.s));
+      PSR_TRY(psr_session_sync(s));
+      float ms = 0.0f;
+      PSR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        pick = {s->eng.chunk, s->eng.inner};
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    PSR_TRY(reprepare(s, pick.first, pick.second));
+    b->chunk[i] = pick.first;
+    b->inner[i] = pick.second;
+    if (chunk_out) chunk_out[i] = pick.first;
+    if (inner_out) inner_out[i] = pick.second;
+  }
+  return PSR_OK;
+}
+
+int psr_batch_run(psr_batch *b) {
+  if (!b) {
+    set_error("batch: null handle");
+    return PSR_EINVAL;
+  }
+  if (!b->warm) {
+    // One direct run settles every buffer and kernel attribute, so that the
+    // capture below records stream work only.
+    for (auto &s : b->obs) PSR_TRY(psr_session_run(s.get()));
+    for (auto &s : b->obs) PSR_TRY(psr_session_sync(s.get()));
+    b->warm = true;
+  }
+  if (!b->exec) {
+    cudaStream_t m = b->main.s;
+    for (cudaEvent_t e : b->events) cudaEventDestroy(e);
+    b->events.assign(b->obs.size() + 1, nullptr);
+    for (auto &e : b->events) PSR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    PSR_CUDA(cudaStreamBeginCapture(m, cudaStreamCaptureModeRelaxed));
+    int rc = PSR_OK;
+    rc = cudaEventRecord(b->events[0], m) == cudaSuccess ? PSR_OK : PSR_ECUDA;
+    for (size_t i = 0; i < b->obs.size() && rc == PSR_OK; ++i) {
+      psr_session *s = b->obs[i].get();
+      if (cudaStreamWaitEvent(s->stream.s, b->events[0], 0) != cudaSuccess) rc = PSR_ECUDA;
+      if (rc == PSR_OK) rc = psr_session_run(s);
+      if (rc == PSR_OK && cudaEventRecord(b->events[i + 1], s->stream.s) != cudaSuccess)
+        rc = PSR_ECUDA;
+      if (rc == PSR_OK && cudaStreamWaitEvent(m, b->events[i + 1], 0) != cudaSuccess)
+        rc = PSR_ECUDA;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(m, &g);
+    if (rc != PSR_OK || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (rc == PSR_OK) set_error(std::string("batch: graph capture failed: ") +
+                                  cudaGetErrorString(ec));
+      return rc == PSR_OK ? PSR_ECUDA : rc;
+    }
+    b->graph = g;
+    PSR_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  }
+  PSR_CUDA(cudaGraphLaunch(b->exec, b->main.s));
+  for (auto &s : b->obs) s->have_run = true;
+  return PSR_OK;
+}
+
+int psr_batch_sync(psr_batch *b) {
+  if (!b) {
+    set_error("batch: null handle");
+    return PSR_EINVAL;
+  }
+  PSR_CUDA(cudaStreamSynchronize(b->main.s));
+  bool regrown = false;
+  for (auto &s : b->obs) {
+    // A raw-candidate overflow makes finish() regrow that session's buffers
+    // and redo the chunk; the captured graph would then hold stale pointers,
+    // so it is captured again on the next run.
+    const void *raw = s->eng.sw.raw.p, *gq = s->eng.sw.gq.p;
+    PSR_TRY(psr_session_sync(s.get()));
+    regrown = regrown || s->eng.sw.raw.p != raw || s->eng.sw.gq.p != gq;
+  }
+  if (regrown) b->drop_graph();
+  return PSR_OK;
+}
+
+int psr_batch_candidates(psr_batch *b, uint64_t i, uint64_t *counts, psr_candidate *out,
+                         uint64_t cap, uint64_t *n_total) {
+  if (!b || i >= b->obs.size()) {
+    set_error("batch: observation index out of range");
+    return PSR_EINVAL;
+  }
+  return psr_session_candidates(b->obs[i].get(), counts, out, cap, n_total);
+}
+
+void *psr_batch_stream(psr_batch *b) { return b ? (void *)b->main.s : nullptr; }
+
+void psr_batch_free(psr_batch *b) { delete b; }
 
 }  // extern "C"

@@ -170,4 +170,35 @@ int synth_obs(const psr_synth_config &cfg, DeviceObs &o, cudaStream_t st) {
   return PSR_OK;
 }
 
+namespace {
+// payload[t * nch + c] = samples[c * ld + t] for 8-bit samples: 32 x 32
+// tiles through shared memory (coalesced reads along t, writes along c).
+__global__ void k_pack_u8(const uint8_t *__restrict__ samples, uint64_t ld, uint64_t ns,
+                          uint64_t nch, uint8_t *__restrict__ payload) {
+  __shared__ uint8_t tile[32][33];
+  const uint64_t t0 = (uint64_t)blockIdx.x * 32, c0 = (uint64_t)blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const uint64_t c = c0 + r, t = t0 + threadIdx.x;
+    tile[r][threadIdx.x] = (c < nch && t < ns) ? samples[c * ld + t] : 0;
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const uint64_t t = t0 + r, c = c0 + threadIdx.x;
+    if (t < ns && c < nch) payload[t * nch + c] = tile[threadIdx.x][r];
+  }
+}
+}  // namespace
+
+int pack_payload_u8(const DeviceObs &src, uint8_t *d_payload, cudaStream_t st) {
+  if (src.kind != SAMPLE_U8 || src.h.nbits != 8) {
+    set_error("batch: device observations must hold 8-bit samples");
+    return PSR_EINVAL;
+  }
+  dim3 grid((unsigned)((src.ns + 31) / 32), (unsigned)((src.nch + 31) / 32));
+  k_pack_u8<<<grid, dim3(32, 8), 0, st>>>(src.samples.as<uint8_t>(), src.ld, src.ns, src.nch,
+                                           d_payload);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
 }  // namespace psr

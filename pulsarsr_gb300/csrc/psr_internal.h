@@ -99,6 +99,8 @@ struct DeviceObs {
 
 // Seeded synthetic observation generated on the device (k_synth.cu).
 int synth_obs(const psr_synth_config &cfg, DeviceObs &o, cudaStream_t st);
+// Time-major 8-bit payload (as read from a file) of a device observation.
+int pack_payload_u8(const DeviceObs &src, uint8_t *d_payload, cudaStream_t st);
 
 // Host-side restatements that stay on the host (FP64 tables, small sorts).
 bool host_delays(const double *f, size_t n, double tsamp, double dm,
