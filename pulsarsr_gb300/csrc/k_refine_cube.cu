@@ -10,11 +10,15 @@
 // with cloud-in-cell weights.  For parameters theta near the reference, the
 // samples of (c, s) move in phase by d_cs = B (phi_theta(c, T_s) -
 // phi_r(c, T_s)) bins, T_s the subint centre (the drift within one subint is
-// neglected), so the folded profile is
-//   p[b] = sum_cs (1 - f) C[c][s][b - k] + f C[c][s][b - k - 1],
-//   d_cs = k + f  (linear interpolation in phase),
-// and J = sum_b (p[b] - mean p)^2 / (n v), v = sum_c var(x_c).  Its adjoint:
-//   dJ/dd_cs = sum_b g[b] (C[c][s][b-k-1] - C[c][s][b-k]),  g = 2 (p - mean)/(n v),
+// neglected).  Each cube row's DFT R_cs[k] (k = 1..B/2) is taken once;
+// shifting a row by d bins multiplies harmonic k by e^(-2 pi i k d / B) (a
+// band-limited shift: no interpolation smoothing that would depend on the
+// fractional shift), so the profile's harmonics are
+//   P_k = sum_cs R_cs[k] e^(-2 pi i k d_cs / B)
+// and, by Parseval, J = sum_b (p_b - mean)^2 / (n v) = sum_k w_k |P_k|^2 /
+// (B n v), w_k = 2 (k < B/2), 1 (k = B/2), v = sum_c var(x_c).  Adjoint:
+//   dJ/dd_cs = sum_k Re(A_k R_cs[k] e^(-2 pi i k d_cs/B) (-2 pi i k / B)),
+//   A_k = 2 w_k conj(P_k) / (B n v),
 //   dd_cs/dnu = B (T_s - tau_c), dd_cs/dnudot = B (T_s - tau_c)^2 / 2,
 //   dd_cs/dDM = -B (nu + nudot (T_s - tau_c)) dtau_c/dDM.
 // Evaluations of every candidate of a group run in the same launches.
@@ -66,12 +70,17 @@ __global__ void __launch_bounds__(CB_NT)
   for (uint64_t base = t0; base < t1; base += CB_TILE) {
     const int len = (int)min((uint64_t)CB_TILE, t1 - base);
     __syncthreads();  // previous tile consumed (and bins zeroed on entry)
+    // At most CB_RUN samples per thread per tile: f32 partial sums (exact for
+    // 8-bit samples), one f64 add per tile (the FP64 pipe is narrow).
+    float ps = 0.0f, pq = 0.0f;
     for (int i = threadIdx.x; i < len; i += CB_NT) {
       const float v = (float)row[base + i];
       tile[i + i / CB_RUN] = v;
-      sum += (double)v;
-      sq += (double)v * (double)v;
+      ps += v;
+      pq += v * v;
     }
+    sum += (double)ps;
+    sq += (double)pq;
     __syncthreads();
     const int r0 = threadIdx.x * CB_RUN;
     if (r0 < len) {
@@ -147,95 +156,125 @@ __device__ __forceinline__ double cube_shift(const CandDev &q, double nu_r, doub
   return (phq - phr) * B;
 }
 
-// Shift of row r = (c, s) for a candidate, in bins: integer part mod B and
-// fraction, plus T_s - tau_c(candidate DM) for the gradient.
-__device__ __forceinline__ void row_shift(const CandDev &q, double nu_r, double nudot_r,
-                                          double dm_r, double Tsub, const double *kc, int S,
-                                          int B, uint64_t r, int &kk, float &f, double &tdq,
-                                          double &kcc) {
+// Shift of row r = (c, s) for a candidate, in bins, and T_s - tau_c(DM).
+__device__ __forceinline__ double row_shift(const CandDev &q, double nu_r, double nudot_r,
+                                            double dm_r, double Tsub, const double *kc, int S,
+                                            int B, uint64_t r, double &tdq, double &kcc) {
   const uint64_t c = r / (uint64_t)S;
   const int s = (int)(r % (uint64_t)S);
   const double Ts = ((double)s + 0.5) * Tsub;
   kcc = kc[c];
-  const double d = cube_shift(q, nu_r, nudot_r, dm_r, Ts, kcc, (double)B, tdq);
-  const double fl = floor(d);
-  f = (float)(d - fl);
-  long long k = (long long)fl % B;
-  if (k < 0) k += B;
-  kk = (int)k;
+  return cube_shift(q, nu_r, nudot_r, dm_r, Ts, kcc, (double)B, tdq);
 }
 
-// Profiles of every candidate: CTA (chunk of rows, candidate) adds its rows'
-// shifted, linearly interpolated bins into a shared f32 profile, then into
-// prof[cand][b] (f64 atomics).
-constexpr int CB_ROWS = 64;
+// R[r][k-1] = sum_b C[r][b] e^(-2 pi i k b / B), k = 1..B/2; one CTA per
+// CB_ROWS rows, twiddles from a shared table.
+constexpr int CB_ROWS = 32;
 __global__ void __launch_bounds__(CB_NT)
-    k_cube_profile(const float *__restrict__ cube, uint64_t rows, int S, int B,
-                   const double *__restrict__ kc, double Tsub, double nu_r, double nudot_r,
-                   double dm_r, const CandDev *__restrict__ cands, double *__restrict__ prof) {
-  __shared__ float acc[CB_MAXB];
-  __shared__ int ks[CB_ROWS];
-  __shared__ float fs[CB_ROWS];
+    k_cube_dft(const float *__restrict__ cube, uint64_t rows, int B, float2 *__restrict__ R) {
+  __shared__ float2 tw[CB_MAXB];
+  __shared__ float row[CB_MAXB];
+  for (int m = threadIdx.x; m < B; m += blockDim.x) {
+    float sn, cs;
+    sincospif(-2.0f * (float)m / (float)B, &sn, &cs);
+    tw[m] = make_float2(cs, sn);
+  }
+  const int K = B / 2;
+  const uint64_t r1 = min((uint64_t)(blockIdx.x + 1) * CB_ROWS, rows);
+  for (uint64_t r = (uint64_t)blockIdx.x * CB_ROWS; r < r1; ++r) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < B; b += blockDim.x) row[b] = cube[r * (uint64_t)B + b];
+    __syncthreads();
+    for (int k = threadIdx.x + 1; k <= K; k += blockDim.x) {
+      float re = 0.0f, im = 0.0f;
+      int m = 0;
+      for (int b = 0; b < B; ++b) {
+        const float2 w = tw[m];
+        re += row[b] * w.x;
+        im += row[b] * w.y;
+        m += k;
+        if (m >= B) m -= B;
+      }
+      R[r * (uint64_t)K + (k - 1)] = make_float2(re, im);
+    }
+  }
+}
+
+// P[cand][k] for every candidate: CTA (chunk of rows, candidate); thread k
+// accumulates its harmonic over the chunk's rows, then one f64 atomic pair.
+__global__ void __launch_bounds__(CB_NT)
+    k_cube_harmonics(const float2 *__restrict__ R, uint64_t rows, int S, int B,
+                     const double *__restrict__ kc, double Tsub, double nu_r, double nudot_r,
+                     double dm_r, const CandDev *__restrict__ cands, int rows_per_cta,
+                     double *__restrict__ P) {
+  __shared__ float dsh[CB_NT];  // shift / B, reduced to [0, 1)
   const int k = blockIdx.y;
   const CandDev q = cands[k];
-  const uint64_t r0 = (uint64_t)blockIdx.x * CB_ROWS;
-  const int nr = (int)min((uint64_t)CB_ROWS, rows - r0);
-  for (int b = threadIdx.x; b < B; b += blockDim.x) acc[b] = 0.0f;
+  const int K = B / 2;
+  const uint64_t r0 = (uint64_t)blockIdx.x * rows_per_cta;
+  const int nr = (int)min((uint64_t)rows_per_cta, rows - r0);
   if (threadIdx.x < nr) {
     double tdq, kcc;
-    row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r0 + threadIdx.x, ks[threadIdx.x],
-              fs[threadIdx.x], tdq, kcc);
+    const double d = row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r0 + threadIdx.x, tdq,
+                               kcc) / (double)B;
+    dsh[threadIdx.x] = (float)(d - floor(d));
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < B; b += blockDim.x) {
-    float a = 0.0f;
+  for (int h = threadIdx.x + 1; h <= K; h += blockDim.x) {
+    float re = 0.0f, im = 0.0f;
     for (int i = 0; i < nr; ++i) {
-      const float *row = cube + (r0 + i) * (uint64_t)B;
-      int i0 = b - ks[i];
-      if (i0 < 0) i0 += B;
-      const int i1 = i0 == 0 ? B - 1 : i0 - 1;
-      const float f = fs[i];
-      a += (1.0f - f) * row[i0] + f * row[i1];
+      // e^(-2 pi i h d) with h d reduced mod 1 in f32
+      float x = (float)h * dsh[i];
+      x -= floorf(x);
+      float sn, cs;
+      sincospif(-2.0f * x, &sn, &cs);
+      const float2 v = R[(r0 + i) * (uint64_t)K + (h - 1)];
+      re += v.x * cs - v.y * sn;
+      im += v.x * sn + v.y * cs;
     }
-    acc[b] = a;
+    atomicAdd(&P[((uint64_t)k * K + (h - 1)) * 2], (double)re);
+    atomicAdd(&P[((uint64_t)k * K + (h - 1)) * 2 + 1], (double)im);
   }
-  __syncthreads();
-  for (int b = threadIdx.x; b < B; b += blockDim.x)
-    atomicAdd(&prof[(uint64_t)k * B + b], (double)acc[b]);
 }
 
-// Gradient: each warp takes rows; lanes split the bins of a row.
+// Gradient: each warp takes rows; lanes split the harmonics of a row.
 __global__ void __launch_bounds__(CB_NT)
-    k_cube_grad(const float *__restrict__ cube, uint64_t rows, int S, int B,
+    k_cube_grad(const float2 *__restrict__ R, uint64_t rows, int S, int B,
                 const double *__restrict__ kc, double Tsub, double nu_r, double nudot_r,
-                double dm_r, const CandDev *__restrict__ cands, const float *__restrict__ g,
+                double dm_r, const CandDev *__restrict__ cands, const float2 *__restrict__ A,
                 double *__restrict__ grad) {
   __shared__ double red[3][CB_NT / 32];
   const int k = blockIdx.y;
   const CandDev q = cands[k];
-  const float *gk = g + (uint64_t)k * B;
+  const int K = B / 2;
+  const float2 *Ak = A + (uint64_t)k * K;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = (int)(gridDim.x * (CB_NT / 32));
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   for (uint64_t r = (uint64_t)blockIdx.x * (CB_NT / 32) + warp; r < rows; r += nwarps) {
-    int kk;
-    float f;
     double tdq, kcc;
-    row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r, kk, f, tdq, kcc);
-    const float *row = cube + r * (uint64_t)B;
-    float dd = 0.0f;
-    for (int b = lane; b < B; b += 32) {
-      int i0 = b - kk;
-      if (i0 < 0) i0 += B;
-      const int i1 = i0 == 0 ? B - 1 : i0 - 1;
-      dd += gk[b] * (row[i1] - row[i0]);
+    const double dd = row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r, tdq, kcc) / (double)B;
+    const float d = (float)(dd - floor(dd));
+    float g = 0.0f;
+    for (int h = lane + 1; h <= K; h += 32) {
+      float x = (float)h * d;
+      x -= floorf(x);
+      float sn, cs;
+      sincospif(-2.0f * x, &sn, &cs);
+      const float2 v = R[r * (uint64_t)K + (h - 1)];
+      // z = R e^(-2 pi i h d) (-2 pi i h / B); contribution Re(A_h z)
+      const float zr = v.x * cs - v.y * sn, zi = v.x * sn + v.y * cs;
+      const float f = 6.283185307179586f * (float)h / (float)B;
+      const float wr = zi * f, wi = -zr * f;  // (zr + i zi) * (-i f)
+      const float2 a = Ak[h - 1];
+      g += a.x * wr - a.y * wi;
     }
-    for (int o = 16; o; o >>= 1) dd += __shfl_down_sync(0xffffffffu, dd, o);
+    for (int o = 16; o; o >>= 1) g += __shfl_down_sync(0xffffffffu, g, o);
     if (lane == 0) {
-      const double Bd = (double)B, ddd = (double)dd;
-      a0 += ddd * Bd * tdq;
-      a1 += ddd * Bd * 0.5 * tdq * tdq;
-      a2 += ddd * (-Bd * (q.nu + q.nudot * tdq) * kcc);
+      const double Bd = (double)B, gg = (double)g;
+      a0 += gg * Bd * tdq;
+      a1 += gg * Bd * 0.5 * tdq * tdq;
+      a2 += gg * (-Bd * (q.nu + q.nudot * tdq) * kcc);
     }
   }
   if (lane == 0) {
@@ -252,7 +291,7 @@ __global__ void __launch_bounds__(CB_NT)
 }
 
 struct CubeWork {
-  DevBuf cube, chsum, tau, kc, cands, prof, g, grad;
+  DevBuf cube, R, chsum, tau, kc, cands, prof, g, grad;
   uint64_t rows = 0;
   double var = 1.0;
 };
@@ -293,6 +332,10 @@ int build_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu, double n
                                                   w.cube.as<float>(), w.chsum.as<double>());
   }
   PSR_CUDA(cudaGetLastError());
+  PSR_TRY(w.R.ensure(w.rows * (uint64_t)(B / 2) * sizeof(float2)));
+  k_cube_dft<<<(unsigned)((w.rows + CB_ROWS - 1) / CB_ROWS), CB_NT, 0, st>>>(
+      w.cube.as<float>(), w.rows, B, w.R.as<float2>());
+  PSR_CUDA(cudaGetLastError());
   std::vector<double> cs(w.rows * 2);
   PSR_CUDA(cudaMemcpyAsync(cs.data(), w.chsum.p, cs.size() * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
@@ -317,43 +360,45 @@ int eval_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu_r, double 
               double dm_r, const std::vector<CandDev> &cand, CubeWork &w, std::vector<double> &J,
               std::vector<double> &grad, cudaStream_t st) {
   const int K = (int)cand.size();
+  const int H = B / 2;
   const double Tsub = (double)n * o.h.tsamp / (double)S;
   PSR_TRY(w.cands.ensure(K * sizeof(CandDev)));
-  PSR_TRY(w.prof.ensure((size_t)K * B * 8));
-  PSR_TRY(w.g.ensure((size_t)K * B * 8));
+  PSR_TRY(w.prof.ensure((size_t)K * H * 2 * 8));
+  PSR_TRY(w.g.ensure((size_t)K * H * sizeof(float2)));
   PSR_TRY(w.grad.ensure((size_t)K * 3 * 8));
   PSR_CUDA(cudaMemcpyAsync(w.cands.p, cand.data(), K * sizeof(CandDev), cudaMemcpyHostToDevice,
                            st));
-  PSR_CUDA(cudaMemsetAsync(w.prof.p, 0, (size_t)K * B * 8, st));
+  PSR_CUDA(cudaMemsetAsync(w.prof.p, 0, (size_t)K * H * 2 * 8, st));
   PSR_CUDA(cudaMemsetAsync(w.grad.p, 0, (size_t)K * 3 * 8, st));
-  dim3 gp((unsigned)((w.rows + CB_ROWS - 1) / CB_ROWS), (unsigned)K);
-  k_cube_profile<<<gp, CB_NT, 0, st>>>(w.cube.as<float>(), w.rows, S, B, w.kc.as<double>(), Tsub,
-                                       nu_r, nudot_r, dm_r, w.cands.as<CandDev>(),
-                                       w.prof.as<double>());
+  const int rows_per_cta = CB_NT;
+  dim3 gp((unsigned)((w.rows + rows_per_cta - 1) / rows_per_cta), (unsigned)K);
+  k_cube_harmonics<<<gp, CB_NT, 0, st>>>(w.R.as<float2>(), w.rows, S, B, w.kc.as<double>(), Tsub,
+                                         nu_r, nudot_r, dm_r, w.cands.as<CandDev>(),
+                                         rows_per_cta, w.prof.as<double>());
   PSR_CUDA(cudaGetLastError());
-  std::vector<double> p((size_t)K * B);
-  std::vector<float> g((size_t)K * B);
-  PSR_CUDA(cudaMemcpyAsync(p.data(), w.prof.p, p.size() * 8, cudaMemcpyDeviceToHost, st));
+  std::vector<double> P((size_t)K * H * 2);
+  PSR_CUDA(cudaMemcpyAsync(P.data(), w.prof.p, P.size() * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
-  const double norm = (double)n * w.var;
+  const double norm = (double)B * (double)n * w.var;
+  std::vector<float2> A((size_t)K * H);
   J.assign(K, 0.0);
   for (int k = 0; k < K; ++k) {
-    double mean = 0.0;
-    for (int b = 0; b < B; ++b) mean += p[(size_t)k * B + b];
-    mean /= (double)B;
     double j = 0.0;
-    for (int b = 0; b < B; ++b) {
-      const double d = p[(size_t)k * B + b] - mean;
-      j += d * d;
-      g[(size_t)k * B + b] = (float)(2.0 * d / norm);
+    for (int h = 1; h <= H; ++h) {
+      const double re = P[((size_t)k * H + h - 1) * 2], im = P[((size_t)k * H + h - 1) * 2 + 1];
+      const double wk = h < H ? 2.0 : 1.0;
+      j += wk * (re * re + im * im);
+      A[(size_t)k * H + h - 1] = make_float2((float)(2.0 * wk * re / norm),
+                                             (float)(-2.0 * wk * im / norm));
     }
     J[k] = j / norm;
   }
-  PSR_CUDA(cudaMemcpyAsync(w.g.p, g.data(), g.size() * 4, cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(w.g.p, A.data(), A.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                           st));
   dim3 gg((unsigned)std::min<uint64_t>((w.rows + 7) / 8, 2048), (unsigned)K);
-  k_cube_grad<<<gg, CB_NT, 0, st>>>(w.cube.as<float>(), w.rows, S, B, w.kc.as<double>(), Tsub,
-                                    nu_r, nudot_r, dm_r, w.cands.as<CandDev>(), w.g.as<float>(),
-                                    w.grad.as<double>());
+  k_cube_grad<<<gg, CB_NT, 0, st>>>(w.R.as<float2>(), w.rows, S, B, w.kc.as<double>(), Tsub,
+                                    nu_r, nudot_r, dm_r, w.cands.as<CandDev>(),
+                                    w.g.as<float2>(), w.grad.as<double>());
   PSR_CUDA(cudaGetLastError());
   grad.resize((size_t)K * 3);
   PSR_CUDA(cudaMemcpyAsync(grad.data(), w.grad.p, grad.size() * 8, cudaMemcpyDeviceToHost, st));
