@@ -72,40 +72,55 @@ __global__ void k_fold_reduce(const double *__restrict__ psums,
   counts[id] = cnt;
 }
 
-// Series mean and variance in f64 (fold/src/lib.rs:63-68); one CTA per
-// series at x + blockIdx.x * xstride.
-__global__ void k_series_moments(const float *__restrict__ x, uint64_t xstride, uint64_t n,
-                                 double *out) {
-  __shared__ double red[32];
-  __shared__ double mean_s;
-  x += blockIdx.x * xstride;
-  out += 2 * blockIdx.x;
-  double a = 0.0;
-  for (uint64_t t = threadIdx.x; t < n; t += blockDim.x) a += (double)x[t];
-  for (int o = 16; o; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+// Series mean and variance in f64 (fold/src/lib.rs:63-68), for series at
+// x + blockIdx.y * xstride: pass 1 sums each CTA's slice (partials), pass 2
+// (k_series_var) sums (x - mean)^2 with the mean taken from all partials.
+constexpr int MOM_NT = 256, MOM_PER = 8192;
+__global__ void __launch_bounds__(MOM_NT)
+    k_series_sum(const float *__restrict__ x, uint64_t xstride, uint64_t n,
+                 double *__restrict__ parts) {
+  __shared__ double red[MOM_NT / 32];
+  x += blockIdx.y * xstride;
+  const uint64_t t0 = (uint64_t)blockIdx.x * MOM_PER, t1 = min(t0 + MOM_PER, n);
+  double acc = 0.0;
+  for (uint64_t t = t0 + threadIdx.x; t < t1; t += MOM_NT) acc += (double)x[t];
+  for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
+    for (int w = 0; w < MOM_NT / 32; ++w) s += red[w];
+    parts[blockIdx.y * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(MOM_NT)
+    k_series_var(const float *__restrict__ x, uint64_t xstride, uint64_t n,
+                 const double *__restrict__ sparts, uint32_t nparts,
+                 double *__restrict__ vparts) {
+  __shared__ double red[MOM_NT / 32];
+  __shared__ double mean_s;
+  x += blockIdx.y * xstride;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (uint32_t i = 0; i < nparts; ++i) s += sparts[blockIdx.y * nparts + i];
     mean_s = s / (double)n;
-    out[0] = s;
   }
   __syncthreads();
   const double m = mean_s;
-  double v = 0.0;
-  for (uint64_t t = threadIdx.x; t < n; t += blockDim.x) {
+  const uint64_t t0 = (uint64_t)blockIdx.x * MOM_PER, t1 = min(t0 + MOM_PER, n);
+  double acc = 0.0;
+  for (uint64_t t = t0 + threadIdx.x; t < t1; t += MOM_NT) {
     const double d = __dsub_rn((double)x[t], m);
-    v = __dadd_rn(v, __dmul_rn(d, d));
+    acc = __dadd_rn(acc, __dmul_rn(d, d));
   }
-  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x / 32); ++w) s += red[w];
-    out[1] = s;
+    for (int w = 0; w < MOM_NT / 32; ++w) s += red[w];
+    vparts[blockIdx.y * gridDim.x + blockIdx.x] = s;
   }
 }
 
@@ -220,14 +235,13 @@ int fold_profiles_ex(const float *d_x, uint64_t xstride, uint64_t n, double tsam
   }
   const uint64_t per_cta = 8192;
   const uint64_t nparts = (n + per_cta - 1) / per_cta;
-  DevBuf dper, psums, pcounts, sums, cnts, mom;
+  DevBuf dper, psums, pcounts, sums, cnts;
   PSR_TRY(dper.ensure(nper * 8));
   PSR_TRY(psums.ensure(nper * nparts * bins * 8));
   PSR_TRY(pcounts.ensure(nper * nparts * bins * 8));
   PSR_TRY(sums.ensure(nper * bins * 8));
   PSR_TRY(cnts.ensure(nper * bins * 8));
   const uint64_t nser = xstride ? nper : 1;
-  PSR_TRY(mom.ensure(16 * nser));
   PSR_CUDA(cudaMemcpyAsync(dper.p, periods, nper * 8, cudaMemcpyHostToDevice, st));
   const size_t smem = bins * (8 + 4);
   dim3 grid((unsigned)nparts, (unsigned)nper);
@@ -238,14 +252,33 @@ int fold_profiles_ex(const float *d_x, uint64_t xstride, uint64_t n, double tsam
   k_fold_reduce<<<(unsigned)((nper * bins + 255) / 256), 256, 0, st>>>(
       psums.as<double>(), pcounts.as<unsigned long long>(), nparts, bins, nper,
       sums.as<double>(), cnts.as<unsigned long long>());
-  k_series_moments<<<(unsigned)nser, 1024, 0, st>>>(d_x, xstride, n, mom.as<double>());
+  const uint32_t mparts = (uint32_t)((n + MOM_PER - 1) / MOM_PER);
+  DevBuf sp, vp;
+  PSR_TRY(sp.ensure((size_t)nser * mparts * 8));
+  PSR_TRY(vp.ensure((size_t)nser * mparts * 8));
+  k_series_sum<<<dim3(mparts, (unsigned)nser), MOM_NT, 0, st>>>(d_x, xstride, n,
+                                                               sp.as<double>());
+  k_series_var<<<dim3(mparts, (unsigned)nser), MOM_NT, 0, st>>>(d_x, xstride, n,
+                                                               sp.as<double>(), mparts,
+                                                               vp.as<double>());
   PSR_CUDA(cudaGetLastError());
-  std::vector<double> hs(nper * bins), hm(2 * nser);
+  std::vector<double> hs(nper * bins), hm(2 * nser), hsp((size_t)nser * mparts),
+      hvp((size_t)nser * mparts);
   std::vector<unsigned long long> hc(nper * bins);
   PSR_CUDA(cudaMemcpyAsync(hs.data(), sums.p, nper * bins * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaMemcpyAsync(hc.data(), cnts.p, nper * bins * 8, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaMemcpyAsync(hm.data(), mom.p, 16 * nser, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hsp.data(), sp.p, hsp.size() * 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hvp.data(), vp.p, hvp.size() * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
+  for (uint64_t m = 0; m < nser; ++m) {
+    double s1 = 0.0, s2 = 0.0;
+    for (uint32_t i = 0; i < mparts; ++i) {
+      s1 += hsp[m * mparts + i];
+      s2 += hvp[m * mparts + i];
+    }
+    hm[2 * m] = s1;
+    hm[2 * m + 1] = s2;
+  }
   for (uint64_t p = 0; p < nper; ++p) {
     const uint64_t m = xstride ? p : 0;
     const double smean = hm[2 * m] / (double)n;

@@ -85,10 +85,16 @@ __global__ void __launch_bounds__(CB_NT)
     const int r0 = threadIdx.x * CB_RUN;
     if (r0 < len) {
       const int r1 = min(r0 + CB_RUN, len);
-      const double td = (double)(base + r0) * tsamp - tc;
-      const double ph = nu * td + 0.5 * nudot * td * td;
+      // Phase at the tile start (f64, once per tile and thread, shared
+      // expression) plus the run offset: a quadratic in the offset, with the
+      // tile's cycles per sample (the f64 pipe is narrow on this GPU).
+      const double tdt = (double)base * tsamp - tc;
+      const double pht = nu * tdt + 0.5 * nudot * tdt * tdt;
+      const double dps_t = (nu + nudot * tdt) * tsamp;  // cycles per sample at the tile start
+      const double off = (double)r0;
+      const double ph = pht + off * (dps_t + 0.5 * nudot * tsamp * tsamp * off);
       float u = (float)((ph - floor(ph)) * (double)B);
-      const double dps = (nu + nudot * td) * tsamp;  // cycles per sample
+      const double dps = dps_t + nudot * tsamp * tsamp * off;
       const float du = (float)((dps - floor(dps)) * (double)B);
       int cur = -1;
       float a0 = 0.0f, a1 = 0.0f;
@@ -237,7 +243,9 @@ __global__ void __launch_bounds__(CB_NT)
   }
 }
 
-// Gradient: each warp takes rows; lanes split the harmonics of a row.
+// Gradient: each warp takes 32 rows at a time; lane l computes row l's shift
+// (the only f64 work), then the warp walks the 32 rows with the lanes
+// splitting each row's harmonics.
 __global__ void __launch_bounds__(CB_NT)
     k_cube_grad(const float2 *__restrict__ R, uint64_t rows, int S, int B,
                 const double *__restrict__ kc, double Tsub, double nu_r, double nudot_r,
@@ -249,33 +257,51 @@ __global__ void __launch_bounds__(CB_NT)
   const int K = B / 2;
   const float2 *Ak = A + (uint64_t)k * K;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nwarps = (int)(gridDim.x * (CB_NT / 32));
+  const uint64_t nwarps = (uint64_t)gridDim.x * (CB_NT / 32);
+  const float twopi_b = 6.283185307179586f / (float)B;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-  for (uint64_t r = (uint64_t)blockIdx.x * (CB_NT / 32) + warp; r < rows; r += nwarps) {
-    double tdq, kcc;
-    const double dd = row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, r, tdq, kcc) / (double)B;
-    const float d = (float)(dd - floor(dd));
-    float g = 0.0f;
-    for (int h = lane + 1; h <= K; h += 32) {
-      float x = (float)h * d;
-      x -= floorf(x);
-      float sn, cs;
-      sincospif(-2.0f * x, &sn, &cs);
-      const float2 v = R[r * (uint64_t)K + (h - 1)];
-      // z = R e^(-2 pi i h d) (-2 pi i h / B); contribution Re(A_h z)
-      const float zr = v.x * cs - v.y * sn, zi = v.x * sn + v.y * cs;
-      const float f = 6.283185307179586f * (float)h / (float)B;
-      const float wr = zi * f, wi = -zr * f;  // (zr + i zi) * (-i f)
-      const float2 a = Ak[h - 1];
-      g += a.x * wr - a.y * wi;
+  for (uint64_t r0 = ((uint64_t)blockIdx.x * (CB_NT / 32) + warp) * 32; r0 < rows;
+       r0 += nwarps * 32) {
+    const uint64_t rl = r0 + lane;
+    double tdq = 0.0, kcc = 0.0;
+    float dl = 0.0f;
+    if (rl < rows) {
+      const double dd = row_shift(q, nu_r, nudot_r, dm_r, Tsub, kc, S, B, rl, tdq, kcc) /
+                        (double)B;
+      dl = (float)(dd - floor(dd));
     }
-    for (int o = 16; o; o >>= 1) g += __shfl_down_sync(0xffffffffu, g, o);
-    if (lane == 0) {
-      const double Bd = (double)B, gg = (double)g;
+    float gl = 0.0f;  // this lane's row's dJ/dd, assembled below
+    const int nr = (int)min((uint64_t)32, rows - r0);
+    for (int i = 0; i < nr; ++i) {
+      const float d = __shfl_sync(0xffffffffu, dl, i);
+      const float2 *Rr = R + (r0 + i) * (uint64_t)K;
+      float g = 0.0f;
+      for (int h = lane + 1; h <= K; h += 32) {
+        float x = (float)h * d;
+        x -= floorf(x);
+        float sn, cs;
+        sincospif(-2.0f * x, &sn, &cs);
+        const float2 v = Rr[h - 1];
+        // z = R e^(-2 pi i h d) (-2 pi i h / B); contribution Re(A_h z)
+        const float zr = v.x * cs - v.y * sn, zi = v.x * sn + v.y * cs;
+        const float f = twopi_b * (float)h;
+        const float2 a = Ak[h - 1];
+        g += a.x * (zi * f) - a.y * (-zr * f);
+      }
+      for (int o = 16; o; o >>= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+      if (lane == i) gl = g;
+    }
+    if (rl < rows) {
+      const double Bd = (double)B, gg = (double)gl;
       a0 += gg * Bd * tdq;
       a1 += gg * Bd * 0.5 * tdq * tdq;
       a2 += gg * (-Bd * (q.nu + q.nudot * tdq) * kcc);
     }
+  }
+  for (int o = 16; o; o >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
   }
   if (lane == 0) {
     red[0][warp] = a0;
@@ -395,7 +421,7 @@ int eval_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu_r, double 
   }
   PSR_CUDA(cudaMemcpyAsync(w.g.p, A.data(), A.size() * sizeof(float2), cudaMemcpyHostToDevice,
                            st));
-  dim3 gg((unsigned)std::min<uint64_t>((w.rows + 7) / 8, 2048), (unsigned)K);
+  dim3 gg((unsigned)std::min<uint64_t>((w.rows + 255) / 256, 1024), (unsigned)K);
   k_cube_grad<<<gg, CB_NT, 0, st>>>(w.R.as<float2>(), w.rows, S, B, w.kc.as<double>(), Tsub,
                                     nu_r, nudot_r, dm_r, w.cands.as<CandDev>(),
                                     w.g.as<float2>(), w.grad.as<double>());
