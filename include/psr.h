@@ -118,6 +118,10 @@ typedef struct psr_fb psr_fb;
  * packed payload copied once to the device and unpacked there. */
 int psr_fb_decode(const uint8_t *bytes, uint64_t len, int64_t limit /* <0: none */,
                   psr_fb **out);
+/* fbank::read (fbank/src/lib.rs:198-203): the file's payload streams to the
+ * device in chunks through pinned staging buffers (reads overlap copies) and
+ * is unpacked there; limit as in psr_fb_decode. */
+int psr_fb_read(const char *path, int64_t limit, psr_fb **out);
 int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples);
 /* A seeded synthetic filterbank generated directly on the device (the psr
  * synth command, synth/src/lib.rs:37-88, and large test shapes).  Same signal

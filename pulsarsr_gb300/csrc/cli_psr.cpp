@@ -242,9 +242,12 @@ struct Fb {
 };
 
 void open_fb(Fb &fb, const std::string &path, int64_t limit) {
-  fb.bytes = read_file(path);
-  check(psr_fb_decode(fb.bytes.data(), fb.bytes.size(), limit, &fb.fb));
+  check(psr_fb_read(path.c_str(), limit, &fb.fb));
   check(psr_fb_info(fb.fb, &fb.h, &fb.ns));
+  // The header bytes (for header.json): SIGPROC headers are short.
+  std::ifstream f(path, std::ios::binary);
+  fb.bytes.resize((size_t)fb.h.data_offset);
+  f.read(reinterpret_cast<char *>(fb.bytes.data()), (std::streamsize)fb.bytes.size());
 }
 
 Value header_value(const std::vector<uint8_t> &bytes) {
@@ -583,7 +586,14 @@ int cmd_search(const Args &a) {
     folded.push(std::move(f));
   }
   Sha256 sha;
-  sha.update(fb.bytes.data(), fb.bytes.size());
+  {
+    std::ifstream f(a.file, std::ios::binary);
+    std::vector<char> buf(1 << 20);
+    while (f) {
+      f.read(buf.data(), (std::streamsize)buf.size());
+      sha.update(reinterpret_cast<const uint8_t *>(buf.data()), (size_t)f.gcount());
+    }
+  }
   Value revision = Value::null();
   if (FILE *p = popen("git rev-parse HEAD 2>/dev/null", "r")) {
     char buf[128] = {0};

@@ -2,9 +2,13 @@
 // own terms (header parsing, FP64 delay tables, DM plans, sifting) and the
 // entry points that drive the device kernels.
 #include <cuda_runtime.h>
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cerrno>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -424,6 +428,107 @@ int psr_fb_decode(const uint8_t *bytes, uint64_t len, int64_t limit, psr_fb **ou
   PSR_TRY(obs_from_bytes(bytes, len, limit, fb->o, fb->stream.s));
   DevBuf e;
   PSR_TRY(unpack_checked(fb->o, e, fb->stream.s));
+  *out = fb.release();
+  return PSR_OK;
+}
+
+// fbank::read (fbank/src/lib.rs:198-203): the header is parsed from the
+// file's first bytes, then the payload streams to the device through two
+// pinned staging buffers (the read of one chunk overlaps the copy of the
+// previous one) and is unpacked there; the file is never held whole in host
+// memory.
+int psr_fb_read(const char *path, int64_t limit, psr_fb **out) {
+  if (!path || !out) {
+    set_error("read: null argument");
+    return PSR_EINVAL;
+  }
+  const int fd = open(path, O_RDONLY);
+  if (fd < 0) {
+    set_error(std::string(std::strerror(errno)) + " (os error " + std::to_string(errno) + ")");
+    return PSR_EIO;
+  }
+  struct Closer {
+    int fd;
+    ~Closer() { close(fd); }
+  } closer{fd};
+  struct stat stt;
+  if (fstat(fd, &stt) != 0) {
+    set_error(std::string(std::strerror(errno)));
+    return PSR_EIO;
+  }
+  const uint64_t fsize = (uint64_t)stt.st_size;
+  auto read_at = [&](uint8_t *dst, uint64_t n, uint64_t off) -> bool {
+    uint64_t done = 0;
+    while (done < n) {
+      const ssize_t r = pread(fd, dst + done, n - done, (off_t)(off + done));
+      if (r <= 0) return false;
+      done += (uint64_t)r;
+    }
+    return true;
+  };
+  // Header: SIGPROC headers are a few hundred bytes; 64 KiB bounds them.
+  std::vector<uint8_t> head((size_t)std::min<uint64_t>(fsize, 65536));
+  if (!read_at(head.data(), head.size(), 0)) {
+    set_error("failed to fill whole buffer");
+    return PSR_EIO;
+  }
+  std::unique_ptr<psr_fb> fb(new psr_fb());
+  DeviceObs &o = fb->o;
+  PSR_TRY(parse_header(head.data(), head.size(), o.h));
+  const uint64_t plen = fsize - (uint64_t)o.h.data_offset;
+  const uint64_t bpf = (uint64_t)o.h.nchans * (uint64_t)o.h.nbits;
+  if ((plen * 8) % bpf != 0) {
+    set_error("invalid or unsupported filterbank: truncated frame or packed padding unsupported");
+    return PSR_EFORMAT;
+  }
+  const uint64_t total = plen * 8 / bpf;
+  const uint64_t ns = limit < 0 ? total : std::min<uint64_t>((uint64_t)limit, total);
+  if (ns < 2) {
+    set_error("invalid or unsupported filterbank: need at least two samples");
+    return PSR_EFORMAT;
+  }
+  o.ns = ns;
+  o.nch = (uint64_t)o.h.nchans;
+  o.kind = kind_for_bits(o.h.nbits);
+  o.payload_bytes = (ns * bpf + 7) / 8;
+  PSR_TRY(o.payload.ensure(o.payload_bytes + 16));
+  PSR_TRY(o.alloc());
+  cudaStream_t st = fb->stream.s;
+  constexpr uint64_t CHUNK = 64ull << 20;
+  uint8_t *stage[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  struct Staging {
+    uint8_t **b;
+    cudaEvent_t *e;
+    ~Staging() {
+      for (int i = 0; i < 2; ++i) {
+        if (e[i]) {
+          cudaEventSynchronize(e[i]);
+          cudaEventDestroy(e[i]);
+        }
+        if (b[i]) cudaFreeHost(b[i]);
+      }
+    }
+  } staging{stage, done};
+  for (int i = 0; i < 2; ++i) {
+    PSR_CUDA(cudaHostAlloc((void **)&stage[i], CHUNK, cudaHostAllocDefault));
+    PSR_CUDA(cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming));
+  }
+  uint64_t off = 0;
+  for (int i = 0; off < o.payload_bytes; ++i, off += CHUNK) {
+    const int k = i & 1;
+    const uint64_t n = std::min(CHUNK, o.payload_bytes - off);
+    PSR_CUDA(cudaEventSynchronize(done[k]));  // the copy that last used stage[k]
+    if (!read_at(stage[k], n, (uint64_t)o.h.data_offset + off)) {
+      set_error("failed to fill whole buffer");
+      return PSR_EIO;
+    }
+    PSR_CUDA(cudaMemcpyAsync(o.payload.as<uint8_t>() + off, stage[k], n, cudaMemcpyHostToDevice,
+                             st));
+    PSR_CUDA(cudaEventRecord(done[k], st));
+  }
+  DevBuf e;
+  PSR_TRY(unpack_checked(o, e, st));
   *out = fb.release();
   return PSR_OK;
 }

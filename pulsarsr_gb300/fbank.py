@@ -84,8 +84,13 @@ def decode(data: bytes, limit: int | None = None) -> Filterbank:
 
 
 def read(path: str, limit: int | None = None) -> Filterbank:
-    with open(path, "rb") as f:
-        return decode(f.read(), limit)
+    """fbank::read (fbank/src/lib.rs:198-203): the payload streams from the
+    file to the device in chunks (psr_fb_read) and is unpacked there."""
+    import os
+    h = C.c_void_p()
+    check(lib().psr_fb_read(os.fsencode(path), C.c_int64(-1 if limit is None else limit),
+                            C.byref(h)))
+    return Filterbank(h.value)
 
 
 def read_header(path: str) -> HeaderInfo:

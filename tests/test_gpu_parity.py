@@ -372,3 +372,20 @@ def test_fold_reference_case(gpu):
     y = np.where(within, 2., (i % 7) * 0.1).astype(np.float32)
     assert fold.measure(y[137:], 137, 0.001, 0.016, 2, 2, 16)["snr"] > 50.
     assert fold.measure(y[137:], 137, 0.001, 0.016, 10, 2, 16)["snr"] < 0.
+
+
+def test_read_streams_file_like_decode(gpu, tmp_path):
+    """fbank.read streams the payload in chunks; same samples as decode."""
+    from pulsarsr_gb300 import IoError, fbank, synth
+    o = synth.Observation(nchans=96, nbits=8, nsamples=1500000, tsamp=72e-6, fch1=1448.,
+                          foff=-1.0, seed=21, noise_mean=100., noise_sigma=10.)
+    raw = o.to_bytes()  # 144 MB payload: three 64 MiB chunks
+    p = tmp_path / "x.fil"
+    p.write_bytes(raw)
+    a = fbank.read(str(p))
+    b = fbank.decode(raw)
+    assert a.nsamples == b.nsamples and a.data.tobytes() == b.data.tobytes()
+    c = fbank.read(str(p), 12345)
+    assert c.nsamples == 12345 and c.data.tobytes() == b.data[:, :12345].tobytes()
+    with pytest.raises(IoError):
+        fbank.read(str(tmp_path / "missing.fil"))
