@@ -196,6 +196,18 @@ __device__ __forceinline__ void stages16(float2 *sm, const float2 *Wl) {
   }
 }
 
+// The stages after the first radix-16 stage (used when stage 0 runs fused
+// with the global loads).
+template <int L, int C, int NT>
+__device__ __forceinline__ void subfft_rest(float2 *sm, const float2 *Wl) {
+  constexpr int q = ilog2(L);
+  constexpr int NsLast = 1 << (4 * (q / 4));
+  stages16<L, C, NT, 1>(sm, Wl);
+  if constexpr (q % 4 == 1) stage<2, L, C, NT, NsLast>(sm, Wl);
+  else if constexpr (q % 4 == 2) stage<4, L, C, NT, NsLast>(sm, Wl);
+  else if constexpr (q % 4 == 3) stage<8, L, C, NT, NsLast>(sm, Wl);
+}
+
 template <int L, int C, int NT>
 __device__ __forceinline__ void subfft(float2 *sm, const float2 *Wl) {
   constexpr int q = ilog2(L);
@@ -318,24 +330,33 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
   build_wl<M1>(Wl, N, Q, lq);
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
   constexpr int total = M1 * C;
-  // Batches of LB independent loads per thread keep many requests in flight.
-#pragma unroll 1
-  for (int base = 0; base < total; base += LB * NT) {
-    float2 v[LB];
+  __syncthreads();  // Wl
+  {
+    // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
+    // (col, j) takes positions j + r*M1/16 of its column and stores its
+    // outputs at 16j + r.  The zero padding (n >= nz) is never loaded.
+    constexpr int nb = M1 / 16;
+    constexpr int nbt = nb * C;
+    constexpr int BPT = (nbt + NT - 1) / NT;
 #pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * NT + (int)threadIdx.x;
-      const uint64_t n = (uint64_t)(idx / C) * M2 + n2_0 + (idx % C);
-      v[u] = (idx < total && n < nz) ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
-    }
+    for (int i = 0; i < BPT; ++i) {
+      const int w = (int)threadIdx.x + i * NT;
+      if (nbt % NT == 0 || w < nbt) {
+        const int col = w % C, j = w / C;
+        float2 v[16];
 #pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * NT + (int)threadIdx.x;
-      if (idx < total) sm[lay<C>(idx / C, idx % C)] = v[u];
+        for (int r = 0; r < 16; ++r) {
+          const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+          v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+        }
+        dft16<M1>(v, Wl);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
+      }
     }
   }
   __syncthreads();
-  subfft<M1, C, NT>(sm, Wl);
+  subfft_rest<M1, C, NT>(sm, Wl);
   float2 *out = work + trial * (uint64_t)M;
   // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 + n2]
   // (values identical to the quarter-table lookup), so these reads coalesce.
