@@ -61,7 +61,10 @@ typedef struct {
 } psr_candidate;
 
 /* search::Config (search/src/lib.rs:14-32); birdies are (center, half width)
- * pairs, 2*nbirdies doubles. */
+ * pairs, 2*nbirdies doubles.  max_harmonics is the largest harmonic sum:
+ * 0 or 16 gives the reference's levels h = 1, 2, 4, 8, 16
+ * (search/src/lib.rs:76); 32 adds h = 32 (an extension with no reference
+ * counterpart, same score formula).  Other values are rejected. */
 typedef struct {
   double min_hz;
   double max_hz;
@@ -69,6 +72,7 @@ typedef struct {
   uint64_t max_candidates;
   const double *birdies;
   uint64_t nbirdies;
+  uint64_t max_harmonics;
 } psr_search_config;
 
 /* fold::Profile scalars (fold/src/lib.rs:3-11); bins/counts are arrays. */

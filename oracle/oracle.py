@@ -31,7 +31,7 @@ class Candidate(C.Structure):
 class Config(C.Structure):
     _fields_ = [("min_hz", C.c_double), ("max_hz", C.c_double), ("threshold", C.c_double),
                 ("max_candidates", C.c_uint64), ("birdies", C.POINTER(C.c_double)),
-                ("nbirdies", C.c_uint64)]
+                ("nbirdies", C.c_uint64), ("max_harmonics", C.c_uint64)]
 
 
 class ProfileStats(C.Structure):
@@ -189,10 +189,10 @@ def raw_power_f64(series) -> np.ndarray:
 
 
 def make_config(min_hz=1.0, max_hz=float("inf"), threshold=6.0, max_candidates=32,
-                birdies=()):
+                birdies=(), max_harmonics=16):
     b = np.ascontiguousarray(np.array(birdies, dtype=np.float64).reshape(-1))
     cfg = Config(min_hz, max_hz, threshold, max_candidates,
-                 _ptr(b, C.c_double) if b.size else None, b.size // 2)
+                 _ptr(b, C.c_double) if b.size else None, b.size // 2, max_harmonics)
     cfg._keep = b  # keep the birdie buffer alive with the struct
     return cfg
 

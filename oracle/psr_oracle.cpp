@@ -461,6 +461,7 @@ struct Config {
   double min_hz = 1, max_hz = INFINITY, threshold = 6;
   size_t max_candidates = 32;
   std::vector<std::pair<double, double>> birdies;
+  size_t max_harmonics = 16;  // 32 extends the reference's level list by h = 32
 };
 
 void stable_sort_by_score_desc(std::vector<Cand> &c) {
@@ -513,7 +514,8 @@ std::vector<Cand> periodicity(const float *series, size_t len, double tsamp,
     return 0.0;
   };
   std::vector<Cand> cands;
-  for (size_t h : {1, 2, 4, 8, 16}) {
+  for (size_t h : {1, 2, 4, 8, 16, 32}) {
+    if (h > cfg.max_harmonics) break;
     size_t end = std::min(last, (plen - 2) / h);
     if (end <= first + 1) continue;
     std::vector<double> scores(end - first + 1);
@@ -1317,6 +1319,7 @@ Config make_config(const orc_config *c) {
   k.max_hz = c->max_hz;
   k.threshold = c->threshold;
   k.max_candidates = c->max_candidates;
+  k.max_harmonics = c->max_harmonics == 32 ? 32 : 16;
   for (uint64_t i = 0; i < c->nbirdies; ++i)
     k.birdies.push_back({c->birdies[2 * i], c->birdies[2 * i + 1]});
   return k;

@@ -56,6 +56,7 @@ typedef struct {
   uint64_t max_candidates;
   const double *birdies; /* pairs (center_hz, half_width_hz) */
   uint64_t nbirdies;
+  uint64_t max_harmonics; /* 0/16: h = 1..16 as the reference; 32 adds h = 32 */
 } orc_config;
 
 typedef struct {

@@ -70,7 +70,7 @@ class Candidate(C.Structure):
 class SearchConfig(C.Structure):
     _fields_ = [("min_hz", C.c_double), ("max_hz", C.c_double), ("threshold", C.c_double),
                 ("max_candidates", C.c_uint64), ("birdies", C.POINTER(C.c_double)),
-                ("nbirdies", C.c_uint64)]
+                ("nbirdies", C.c_uint64), ("max_harmonics", C.c_uint64)]
 
 
 class ProfileStats(C.Structure):

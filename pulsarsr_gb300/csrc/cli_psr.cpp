@@ -537,7 +537,7 @@ int cmd_search(const Args &a) {
     throw Fail("DM range leaves no independent discovery/confirmation split");
   const uint64_t discovery = (length - max_delay) / 2;
   psr_search_config cfg{min_hz, max_hz, threshold, 32,
-                        birdies.empty() ? nullptr : birdies.data(), birdies.size() / 2};
+                        birdies.empty() ? nullptr : birdies.data(), birdies.size() / 2, 16};
   std::printf("%llu samples, %lld channels, %llu DM trials (step %s), %llu threads\n",
               (unsigned long long)fb.ns, (long long)fb.h.nchans, (unsigned long long)nt,
               fixed(step, 6).c_str(), (unsigned long long)threads);

@@ -282,7 +282,8 @@ int unpack_checked(DeviceObs &o, DevBuf &errbuf, cudaStream_t st) {
 
 bool valid_config(const psr_search_config *c) {
   return c && c->max_candidates >= 1 && c->max_candidates <= 64 && !std::isnan(c->min_hz) &&
-         !std::isnan(c->max_hz) && !std::isnan(c->threshold) && (c->nbirdies == 0 || c->birdies);
+         !std::isnan(c->max_hz) && !std::isnan(c->threshold) && (c->nbirdies == 0 || c->birdies) &&
+         (c->max_harmonics == 0 || c->max_harmonics == 16 || c->max_harmonics == 32);
 }
 
 SpecConfig to_spec(const psr_search_config *c, double tsamp) {
@@ -293,6 +294,7 @@ SpecConfig to_spec(const psr_search_config *c, double tsamp) {
   s.threshold = c->threshold;
   s.max_candidates = c->max_candidates;
   s.birdies.assign(c->birdies, c->birdies + 2 * c->nbirdies);
+  s.levels = c->max_harmonics == 32 ? 6 : 5;
   return s;
 }
 

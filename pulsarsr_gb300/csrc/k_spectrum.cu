@@ -69,7 +69,7 @@ struct HarmArgs {
   double threshold;
   float t1;  // smallest float v with (double)v - 1.0 >= threshold
   uint64_t first;
-  uint64_t end[5];  // end_h for h = 1,2,4,8,16 (0 when the h loop is skipped)
+  uint64_t end[6];  // end_h for h = 1,2,4,8,16,32 (0 when the h loop is skipped)
   RawCand *raw;
   unsigned *raw_count;
   uint64_t raw_cap;
@@ -106,7 +106,8 @@ __device__ __forceinline__ double inv_sqrt_div(double x, int hi) {
     case 1: return __ddiv_rn(x, 1.4142135623730951);
     case 2: return __dmul_rn(x, 0.5);
     case 3: return __ddiv_rn(x, 2.8284271247461903);
-    default: return __dmul_rn(x, 0.25);
+    case 4: return __dmul_rn(x, 0.25);
+    default: return __ddiv_rn(x, 5.656854249492381);
   }
 }
 
@@ -144,9 +145,9 @@ __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64
 }
 
 
-// round(RN(kf * j)) for a positive normal double kf and 1 <= j <= 16, in
+// round(RN(kf * j)) for a positive normal double kf and 1 <= j <= 32, in
 // exact 64-bit integer arithmetic: kf = m * 2^E (53-bit m), the product m*j
-// is exact in 57 bits, rounded to 53 bits (nearest, ties to even) as the FPU
+// is exact in 58 bits, rounded to 53 bits (nearest, ties to even) as the FPU
 // would, then rounded to an integer half away from zero as f64::round does.
 // Bit-identical to (uint64_t)round(__dmul_rn(kf, (double)j)).
 __device__ __forceinline__ uint64_t round_mul(double kf, uint32_t j) {
@@ -177,19 +178,22 @@ __device__ __forceinline__ uint64_t round_mul(double kf, uint32_t j) {
 // All harmonic levels h >= 2 of one gated bin (pw(k) >= 4), one lane per
 // bin: the offset is computed once, the harmonic positions and gathers are
 // issued together, and the f64 sums accumulate in j order (the reference's
-// per-h sums are the same prefix sums).
+// per-h sums are the same prefix sums).  NL = number of levels (5: h <= 16,
+// 6: h <= 32).
+template <int NL>
 __device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, const float *sc,
                           uint64_t k) {
+  constexpr int HMAX = 1 << (NL - 1);
   int hmax = 0;
 #pragma unroll
-  for (int hi = 1; hi < 5; ++hi)
+  for (int hi = 1; hi < NL; ++hi)
     if (a.end[hi] != 0 && k + 1 <= a.end[hi]) hmax = hi;
   if (hmax == 0 || pw(a, raw, sc, k) < 4.0f) return;  // queue entries are a superset
   const double kf = __dadd_rn((double)k, offset_at(raw, k));
   const int H = 1 << hmax;
-  float v[16];
+  float v[HMAX];
 #pragma unroll
-  for (int j = 1; j <= 16; ++j) {
+  for (int j = 1; j <= HMAX; ++j) {
     float x = 0.0f;
     if (j <= H) {
       uint64_t idx = round_mul(kf, (uint32_t)j);
@@ -200,7 +204,7 @@ __device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, c
   }
   double sum = -0.0;
 #pragma unroll
-  for (int hi = 1; hi < 5; ++hi) {
+  for (int hi = 1; hi < NL; ++hi) {
     if (hi > hmax) break;
     const int h = 1 << hi;
     // harmonics j = h/2+1 .. h (v[j-1]); for h = 2 also j = 1
@@ -427,6 +431,7 @@ __global__ void __launch_bounds__(SC_NT)
 constexpr int HI_NT = 256;
 constexpr int HI_CTAS_PER_TRIAL = 12;
 
+template <int NL>
 __global__ void __launch_bounds__(HI_NT) k_harm_items(HarmArgs a, GateArgs g) {
   const uint64_t trial = blockIdx.y;
   const float *raw = a.power + trial * a.ldp;
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(HI_NT) k_harm_items(HarmArgs a, GateArgs g) {
         if (s > sm && s >= sp) emit(a, trial, raw, k, 0, s);
       }
     } else {
-      harm_item(a, trial, raw, sc, q2[idx - n1]);
+      harm_item<NL>(a, trial, raw, sc, q2[idx - n1]);
     }
   }
 }
@@ -693,7 +698,7 @@ HarmArgs harm_args(const FftPlan &p, const SpecConfig &c, const float *d_power, 
   const double lastf = std::floor(std::fmin(c.max_hz, 0.5 / c.tsamp) / bin_hz);
   const uint64_t last = std::min<uint64_t>(lastf <= 0.0 ? 0 : (uint64_t)lastf, plen - 2);
   a.first = first;
-  for (int hi = 0; hi < 5; ++hi) {
+  for (int hi = 0; hi < c.levels; ++hi) {
     const uint64_t h = 1ull << hi;
     const uint64_t e = std::min(last, (plen - 2) / h);
     a.end[hi] = (e <= first + 1) ? 0 : e;
@@ -747,7 +752,10 @@ int spectrum_items(const FftPlan &p, const SpecConfig &c, const float *d_power, 
   HarmArgs a = harm_args(p, c, d_power, ldp, w);
   if (a.end[0] == 0) return PSR_OK;
   dim3 grid(HI_CTAS_PER_TRIAL, (unsigned)ntrials);
-  k_harm_items<<<grid, HI_NT, 0, st>>>(a, gate_args(w, 0));
+  if (c.levels == 6)
+    k_harm_items<6><<<grid, HI_NT, 0, st>>>(a, gate_args(w, 0));
+  else
+    k_harm_items<5><<<grid, HI_NT, 0, st>>>(a, gate_args(w, 0));
   PSR_CUDA(cudaGetLastError());
   return PSR_OK;
 }

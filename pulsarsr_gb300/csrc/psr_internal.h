@@ -151,6 +151,7 @@ struct SpecConfig {
   double min_hz = 1, max_hz = 0, threshold = 6;
   uint64_t max_candidates = 32;
   std::vector<double> birdies;  // pairs
+  int levels = 5;               // harmonic sums h = 1 .. 2^(levels-1)
 };
 struct SpecWork {
   DevBuf scale, raw, raw_count, birdies, overflow, gq, gn;

@@ -26,12 +26,15 @@ class Config:
     threshold: float = 6.0
     max_candidates: int = 32
     birdies: list = field(default_factory=list)
+    # Largest harmonic sum: 16 as the reference (h = 1, 2, 4, 8, 16); 32 adds
+    # h = 32, an extension with the same score formula.
+    max_harmonics: int = 16
 
     def _c(self) -> SearchConfig:
         b = np.ascontiguousarray(np.array(self.birdies, dtype=np.float64).reshape(-1))
         cfg = SearchConfig(self.min_hz, self.max_hz, self.threshold, self.max_candidates,
                            b.ctypes.data_as(C.POINTER(C.c_double)) if b.size else None,
-                           b.size // 2)
+                           b.size // 2, self.max_harmonics)
         cfg._keep = b
         return cfg
 

@@ -91,3 +91,33 @@ def test_sift_matches_oracle(L, oracle):
                    (137., 1 / 137., 0., 1, 20.)], dtype=search.CAND_DTYPE)
     k = search.sift(c2, 0.1, 10, True)
     assert len(k) == 1 and k[0]["dm"] == 20.
+
+
+def harmonic_comb(rng, n, cycles):
+    """32 equal harmonics of `cycles` cycles per n samples in weak noise: a
+    high S/N comb whose parabolic bin offsets are accurate enough for the
+    h = 32 sum to win."""
+    t = np.arange(n)
+    x = rng.normal(0, 0.1, n)
+    for j in range(1, 33):
+        x += 0.05 * np.cos(2 * np.pi * j * cycles * t / n + rng.uniform(0, 2 * np.pi))
+    return np.rint(40 * x + 500).astype(np.float32)
+
+
+def test_max_harmonics_levels(L, oracle):
+    """max_harmonics 0/16 keeps the reference's levels; 32 adds h = 32 (the
+    oracle's lists gain h = 32 entries for a narrow pulse); other values are
+    rejected by the library before any device work."""
+    from pulsarsr_gb300 import InvalidArgument, search
+    x = harmonic_comb(np.random.default_rng(11), 1 << 16, 300)
+    ref = oracle.periodicity(x, 1e-3, 0.0, min_hz=0.5, threshold=6.0, max_candidates=64)
+    assert ref.tobytes() == oracle.periodicity(x, 1e-3, 0.0, min_hz=0.5, threshold=6.0,
+                                               max_candidates=64, max_harmonics=16).tobytes()
+    ext = oracle.periodicity(x, 1e-3, 0.0, min_hz=0.5, threshold=6.0, max_candidates=64,
+                             max_harmonics=32)
+    assert set(ref["harmonics"].tolist()) <= {1, 2, 4, 8, 16}
+    assert 32 in ext["harmonics"].tolist()
+    assert ext["score"].max() >= ref["score"].max()
+    for bad in (1, 8, 24, 64):
+        with pytest.raises(InvalidArgument, match="valid config"):
+            search.periodicity(x, 1e-3, 0.0, search.Config(max_harmonics=bad))

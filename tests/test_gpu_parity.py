@@ -236,6 +236,22 @@ def test_periodicity_random_matches_oracle(gpu, oracle, seed):
     assert c.tobytes() == o.tobytes()
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_periodicity_32_harmonics_matches_oracle(gpu, oracle, seed):
+    """The h = 32 extension level: candidate lists bit-identical to the
+    oracle's, with h = 32 entries present for a narrow pulse train."""
+    from pulsarsr_gb300 import search
+    from test_abi import harmonic_comb
+    rng = np.random.default_rng(100 + seed)
+    n = 1 << int(rng.integers(16, 19))
+    x = harmonic_comb(rng, n, int(rng.integers(150, n // 160)))
+    cfg = dict(min_hz=2.0, max_hz=3000.0, threshold=6.0, max_candidates=64, max_harmonics=32)
+    c = search.periodicity(x, 64e-6, 3.0, search.Config(**cfg))
+    o = oracle.periodicity(x, 64e-6, 3.0, **cfg)
+    assert 32 in o["harmonics"].tolist()
+    assert c.tobytes() == o.tobytes()
+
+
 def search_case(obs, dm_max, ntake=None, rfi_on=True):
     from pulsarsr_gb300 import dedisperse, synth
     raw = obs.to_bytes()
@@ -250,16 +266,18 @@ def search_case(obs, dm_max, ntake=None, rfi_on=True):
     return raw, trials, discovery
 
 
-@pytest.mark.parametrize("cfgname", ["c1", "c2"])
+@pytest.mark.parametrize("cfgname", ["c1", "c2", "c1h32"])
 def test_search_trials_match_oracle(gpu, oracle, cfgname):
     """Candidate lists of the trial loop, GPU vs oracle, bit for bit, after
     the same RFI mask (the psr search path up to grouping)."""
     from pulsarsr_gb300 import fbank, rfi, search, synth
-    if cfgname == "c1":
+    if cfgname.startswith("c1"):
         obs = synth.config_c1(1)
         raw, trials, disc = search_case(obs, 120.0)
         trials = np.arange(0, 120.0 + 1e-9, 2.0)
         cfg = dict(min_hz=15.0, max_hz=2000.0, threshold=8.0, max_candidates=32)
+        if cfgname == "c1h32":
+            cfg["max_harmonics"] = 32
     else:
         obs = synth.config_c2(2)
         raw, trials, disc = search_case(obs, 500.0, ntake=64)
