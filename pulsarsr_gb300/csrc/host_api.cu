@@ -944,6 +944,7 @@ int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start, u
     return start[a].period_s > start[b].period_s;
   });
   std::vector<uint64_t> pending = idx;
+  CubeCache cache;
   while (!pending.empty()) {
     const uint64_t lead = pending.front();
     const double nu0 = 1.0 / start[lead].period_s;
@@ -961,7 +962,7 @@ int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start, u
     std::vector<uint64_t> ge(group.size());
     for (size_t i = 0; i < group.size(); ++i) gs[i] = start[group[i]];
     PSR_TRY(refine_cube_group(o, n, gs.data(), group.size(), ro, go.data(), gj.data(),
-                              ge.data(), fb->stream.s));
+                              ge.data(), cache, fb->stream.s));
     for (size_t i = 0; i < group.size(); ++i) {
       out[group[i]] = go[i];
       if (J) J[group[i]] = gj[i];

@@ -26,12 +26,22 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "psr_internal.h"
 #include "refine.h"
 
 namespace psr {
+
+// Device buffers of one cube, reused by every group of a refinement call.
+struct CubeWork {
+  DevBuf cube, R, chsum, tau, kc, cands, prof, g, grad;
+  uint64_t rows = 0;
+  double var = 1.0;
+};
+CubeCache::~CubeCache() { delete w; }
+
 namespace {
 
 constexpr double K_DM_C = 4148.808;  // dedisperse/src/lib.rs:3
@@ -40,111 +50,629 @@ constexpr int CB_MAXB = 1024;
 
 // Fold subint s of channel c (one CTA) into C[c][s][*] (the row's mean
 // removed, which leaves every shifted profile's deviations unchanged and keeps
-// f32 sums accurate) and the channel's sum / sum of squares.  Tiles of
-// CB_NT x CB_RUN samples are loaded coalesced into shared memory (one pad word
-// per CB_RUN so that per-thread runs are free of bank conflicts); thread j
-// then folds the run [j*CB_RUN, (j+1)*CB_RUN) of the tile, its phase anchored
-// in f64 at the run's first sample and advanced in f32, summing consecutive
-// samples of the same bin in registers and issuing shared-memory atomics only
-// when the bin changes (slow pulsars stay in one bin for many samples).
+// f32 sums accurate) and the channel's sum / sum of squares.
+//
+// The row is cut into runs of 32 samples aligned to the global sample grid
+// (rows start 64-element aligned and carry >= 64 elements of padding, so a
+// run is one to eight aligned 16-byte loads that never leave the row); thread
+// j folds a contiguous stretch of runs of the subint, prefetching its next run
+// while it folds the current one.  Samples of a boundary run outside [t0, t1) are
+// zeroed.  Phases are fixed-point fractions of a cycle (u64, 2^-64 cycle
+// resolution): one CTA-wide f64 anchor at the first run, then per-thread
+// offsets and per-stride advances by exact integer second differences, so no
+// thread does f64 work per run.  Inside a run the bin position u (in bins)
+// advances in f32; for du < 1 bin per sample the bin index is walked
+// incrementally (one compare per sample), otherwise floored per sample.
+// Consecutive samples of one bin are summed in registers (a0 = sum v, a1 =
+// sum w v; CIC weights 1 - w and w), across run boundaries, and flushed with
+// two shared-memory atomics when the bin changes.  Channel sums are integer (u8, u16) or f32
+// per run (f32 data) before the f64 reduction.
 constexpr int CB_RUN = 32;
-constexpr int CB_TILE = CB_NT * CB_RUN;
 
 template <class T>
+struct RunRegs {
+  static constexpr int W = (CB_RUN * (int)sizeof(T)) / 16;  // 16-byte words per run
+  uint4 r[W];
+};
+
+template <class T>
+__device__ __forceinline__ void load_run(const T *p, RunRegs<T> &x) {
+  const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+  for (int k = 0; k < RunRegs<T>::W; ++k) x.r[k] = __ldg(q + k);
+}
+
+__device__ __forceinline__ uint32_t word_of(const uint4 &v, int k) {
+  return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+
+// Sample i (0..31) of a run as f32 (integer samples are exact: 2^23 + v
+// assembled by a byte permute, then 2^23 subtracted).
+template <class T>
+__device__ __forceinline__ float run_sample(const RunRegs<T> &x, int i);
+template <>
+__device__ __forceinline__ float run_sample<uint8_t>(const RunRegs<uint8_t> &x, int i) {
+  const uint32_t w = word_of(x.r[i >> 4], (i >> 2) & 3);
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (unsigned)(i & 3))) - 8388608.0f;
+}
+template <>
+__device__ __forceinline__ float run_sample<uint16_t>(const RunRegs<uint16_t> &x, int i) {
+  const uint32_t w = word_of(x.r[i >> 3], (i >> 1) & 3);
+  const unsigned lo = (unsigned)(i & 1) * 2u;
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7500u | ((lo + 1u) << 4) | lo)) -
+         8388608.0f;
+}
+template <>
+__device__ __forceinline__ float run_sample<float>(const RunRegs<float> &x, int i) {
+  return __uint_as_float(word_of(x.r[i >> 2], i & 3));
+}
+
+// Zero the samples of a run outside [lo, hi) (boundary runs only).
+template <class T>
+__device__ __forceinline__ void mask_run(RunRegs<T> &x, int lo, int hi) {
+  constexpr int PER_WORD = 4 / (int)sizeof(T);
+#pragma unroll
+  for (int k = 0; k < RunRegs<T>::W; ++k) {
+    uint32_t w[4] = {x.r[k].x, x.r[k].y, x.r[k].z, x.r[k].w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+#pragma unroll
+      for (int b = 0; b < PER_WORD; ++b) {
+        const int i = (k * 4 + e) * PER_WORD + b;
+        if (i < lo || i >= hi) {
+          const uint32_t m = sizeof(T) == 4 ? 0xffffffffu
+                                            : (((1u << (8 * sizeof(T))) - 1u) << (8 * sizeof(T) * b));
+          w[e] &= ~m;
+        }
+      }
+    }
+    x.r[k] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// Channel-sum accumulators: exact integers for 8/16-bit samples.
+template <class T>
+struct RunSums {
+  unsigned long long s = 0, q = 0;
+  __device__ __forceinline__ void add(const RunRegs<T> &x) {
+    unsigned s32 = 0, q32 = 0;
+#pragma unroll
+    for (int k = 0; k < RunRegs<T>::W; ++k)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const uint32_t w = word_of(x.r[k], e);
+        if (sizeof(T) == 1) {
+          s32 = __dp4a(w, 0x01010101u, s32);
+          q32 = __dp4a(w, w, q32);  // <= 32 * 255^2 per run
+        } else {
+          const uint32_t a = w & 0xffffu, b = w >> 16;
+          s32 += a + b;
+          q += (unsigned long long)(a * a) + (unsigned long long)(b * b);
+        }
+      }
+    s += s32;
+    q += q32;
+  }
+  // One 16-byte chunk (staged tiles).
+  __device__ __forceinline__ void add_chunk(const uint4 &v) {
+    unsigned s32 = 0, q32 = 0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const uint32_t w = word_of(v, e);
+      if (sizeof(T) == 1) {
+        s32 = __dp4a(w, 0x01010101u, s32);
+        q32 = __dp4a(w, w, q32);
+      } else {
+        const uint32_t a = w & 0xffffu, b = w >> 16;
+        s32 += a + b;
+        q += (unsigned long long)(a * a) + (unsigned long long)(b * b);
+      }
+    }
+    s += s32;
+    q += q32;
+  }
+  __device__ __forceinline__ double sum() const { return (double)s; }
+  __device__ __forceinline__ double sq() const { return (double)q; }
+};
+template <>
+struct RunSums<float> {
+  double s = 0.0, q = 0.0;
+  __device__ __forceinline__ void add(const RunRegs<float> &x) {
+    float ps = 0.0f, pq = 0.0f;
+#pragma unroll
+    for (int i = 0; i < CB_RUN; ++i) {
+      const float v = run_sample<float>(x, i);
+      ps += v;
+      pq = fmaf(v, v, pq);
+    }
+    s += (double)ps;
+    q += (double)pq;
+  }
+  __device__ __forceinline__ void add_chunk(const uint4 &v) {
+    float ps = 0.0f, pq = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float x = __uint_as_float(word_of(v, e));
+      ps += x;
+      pq = fmaf(x, x, pq);
+    }
+    s += (double)ps;
+    q += (double)pq;
+  }
+  __device__ __forceinline__ double sum() const { return s; }
+  __device__ __forceinline__ double sq() const { return q; }
+};
+
+// frac(x) as a u64 fraction of a cycle.
+__device__ __forceinline__ unsigned long long fix_frac(double x) {
+  const double f = x - floor(x);
+  return __double2ull_rz(ldexp(f, 64));
+}
+
+// Bin accumulators of one CTA.  PrivateBins: one column per thread,
+// h[b * nt + tid] (bank = tid mod 32 for every b: no conflicts, no atomics),
+// summed over threads at the end; for B * threads <= CB_PRIV floats.
+// SharedBins: one row updated with shared-memory atomics (large B).
+constexpr int CB_PRIV = 8192;
+struct PrivateBins {
+  float *h;
+  int nt, tid;
+  __device__ __forceinline__ void add(int b, float x) const { h[b * nt + tid] += x; }
+};
+struct SharedBins {
+  float *h;
+  __device__ __forceinline__ void add(int b, float x) const { atomicAdd(&h[b], x); }
+};
+
+template <class Bins>
+__device__ __forceinline__ void flush_bins(const Bins &bins, int bin, int B, float a0, float a1) {
+  bins.add(bin, a0 - a1);
+  bins.add(bin + 1 == B ? 0 : bin + 1, a1);
+}
+
+// Open bin of a thread's walk: samples of bin `bin` summed so far (a0 = sum
+// v, a1 = sum w v); bin < 0 when nothing is open.
+struct OpenBin {
+  int bin = -1;
+  float a0 = 0.0f, a1 = 0.0f;
+  template <class Bins>
+  __device__ __forceinline__ void move_to(int b, const Bins &bins, int B) {
+    if (b != bin) {
+      if (bin >= 0) flush_bins(bins, bin, B, a0, a1);
+      bin = b;
+      a0 = a1 = 0.0f;
+    }
+  }
+};
+
+// Fold one run starting at bin position u (bins) advancing du per sample;
+// the open bin carries over from the previous run of the same thread.
+template <class T, class Bins>
+__device__ __forceinline__ void fold_run(const RunRegs<T> &x, float u, float du, int B,
+                                         const Bins &bins, OpenBin &ob, RunSums<T> &sums) {
+  sums.add(x);
+  const float fB = (float)B;
+  if (du < 1.0f) {
+    int b = (int)u;
+    if (b >= B) b = 0, u = 0.0f;
+    float w = u - (float)b;
+    ob.move_to(b, bins, B);
+#pragma unroll
+    for (int i = 0; i < CB_RUN; ++i) {
+      const float v = run_sample<T>(x, i);
+      ob.a0 += v;
+      ob.a1 = fmaf(w, v, ob.a1);
+      w += du;
+      if (w >= 1.0f) {
+        flush_bins(bins, ob.bin, B, ob.a0, ob.a1);
+        ob.bin = ob.bin + 1 == B ? 0 : ob.bin + 1;
+        w -= 1.0f;
+        ob.a0 = ob.a1 = 0.0f;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < CB_RUN; ++i) {
+      const float v = run_sample<T>(x, i);
+      const float fl = floorf(u);
+      int b0 = (int)fl;
+      float w = u - fl;
+      if (b0 >= B) b0 = 0, w = 0.0f;
+      ob.move_to(b0, bins, B);
+      ob.a0 += v;
+      ob.a1 = fmaf(w, v, ob.a1);
+      u += du;
+      if (u >= fB) u -= fB;
+    }
+  }
+}
+
+// 8-bit runs: a run that stays inside one bin (or crosses one bin edge) is
+// folded from two integer sums instead of sample by sample.  With w_i = w0 +
+// i du the run adds sum (1 - w_i) v_i and sum w_i v_i to bins b and b + 1,
+// i.e. a0 += S and a1 += w0 S + du T with S = sum v_i, T = sum i v_i (dp4a
+// over the packed bytes, exact); a run whose w reaches 1 at sample p is split
+// there (byte-masked dp4a for the prefix).  Runs with more crossings (du >=
+// 1/31 bins per sample) take the sample-by-sample walk.
+__device__ __forceinline__ uint32_t prefix_mask(int p, int k) {
+  const int cnt = min(max(p - 4 * k, 0), 4);
+  return cnt == 0 ? 0u : (0xffffffffu >> (32 - 8 * cnt));
+}
+
+template <class Bins>
+__device__ __forceinline__ void fold_run(const RunRegs<uint8_t> &x, float u, float du, int B,
+                                         const Bins &bins, OpenBin &ob,
+                                         RunSums<uint8_t> &sums) {
+  // S = sum v, Q = sum v^2 (the channel statistics), T = sum i v.
+  unsigned S = 0, Q = 0, T = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t wd = word_of(x.r[k >> 2], k & 3);
+    S = __dp4a(wd, 0x01010101u, S);
+    Q = __dp4a(wd, wd, Q);
+    T = __dp4a(wd, 0x03020100u + 0x04040404u * (unsigned)k, T);
+  }
+  sums.s += S;
+  sums.q += Q;
+  int b = (int)u;
+  if (b >= B) b = 0, u = 0.0f;
+  const float w0 = u - (float)b;
+  const float wend = fmaf(31.0f, du, w0);
+  if (du < 1.0f && wend < 2.0f) {
+    ob.move_to(b, bins, B);
+    if (wend < 1.0f) {
+      ob.a0 += (float)S;
+      ob.a1 += fmaf(w0, (float)S, du * (float)T);
+      return;
+    }
+    // first sample with w >= 1 (the walk's rule, with its f32 rounding)
+    int p = min(max((int)ceilf((1.0f - w0) / du), 1), 31);
+    if (fmaf((float)(p - 1), du, w0) >= 1.0f) --p;
+    else if (fmaf((float)p, du, w0) < 1.0f) ++p;
+    unsigned S1 = 0, T1 = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t wd = word_of(x.r[k >> 2], k & 3) & prefix_mask(p, k);
+      S1 = __dp4a(wd, 0x01010101u, S1);
+      T1 = __dp4a(wd, 0x03020100u + 0x04040404u * (unsigned)k, T1);
+    }
+    const float s1 = (float)S1, t1 = (float)T1, s2 = (float)(S - S1), t2 = (float)(T - T1);
+    flush_bins(bins, ob.bin, B, ob.a0 + s1, ob.a1 + fmaf(w0, s1, du * t1));
+    ob.bin = ob.bin + 1 == B ? 0 : ob.bin + 1;
+    ob.a0 = s2;
+    ob.a1 = fmaf(w0 - 1.0f, s2, du * t2);
+    return;
+  }
+  // Sample-by-sample walk.
+  const float fB = (float)B;
+  if (du < 1.0f) {
+    float w = w0;
+    ob.move_to(b, bins, B);
+#pragma unroll
+    for (int i = 0; i < CB_RUN; ++i) {
+      const float v = run_sample<uint8_t>(x, i);
+      ob.a0 += v;
+      ob.a1 = fmaf(w, v, ob.a1);
+      w += du;
+      if (w >= 1.0f) {
+        flush_bins(bins, ob.bin, B, ob.a0, ob.a1);
+        ob.bin = ob.bin + 1 == B ? 0 : ob.bin + 1;
+        w -= 1.0f;
+        ob.a0 = ob.a1 = 0.0f;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < CB_RUN; ++i) {
+      const float v = run_sample<uint8_t>(x, i);
+      const float fl = floorf(u);
+      int b0 = (int)fl;
+      float w = u - fl;
+      if (b0 >= B) b0 = 0, w = 0.0f;
+      ob.move_to(b0, bins, B);
+      ob.a0 += v;
+      ob.a1 = fmaf(w, v, ob.a1);
+      u += du;
+      if (u >= fB) u -= fB;
+    }
+  }
+}
+
+// PRIV: per-thread bin columns in dynamic shared memory (B * blockDim.x
+// floats); otherwise one shared row with atomics.  blockDim.x is a multiple
+// of 32, at most CB_NT.
+template <class T, bool PRIV>
 __global__ void __launch_bounds__(CB_NT)
     k_cube_fold(const T *__restrict__ x, uint64_t ld, uint64_t n, int S, int B, double tsamp,
                 double nu, double nudot, const double *__restrict__ tau,
                 float *__restrict__ cube, double *__restrict__ chsum) {
-  __shared__ float bins[CB_MAXB];
-  __shared__ float tile[CB_TILE + CB_TILE / CB_RUN];
+  extern __shared__ float hist[];
+  __shared__ unsigned long long fx[5];
   __shared__ double red[2][CB_NT / 32];
   __shared__ float mean_s;
+  const int nt = (int)blockDim.x, tid = (int)threadIdx.x;
   const int s = blockIdx.x;
   const uint64_t c = blockIdx.y;
-  for (int b = threadIdx.x; b < B; b += blockDim.x) bins[b] = 0.0f;
+  const int hn = PRIV ? B * nt : B;
+  for (int i = tid; i < hn; i += nt) hist[i] = 0.0f;
   const uint64_t t0 = (n * (uint64_t)s) / (uint64_t)S, t1 = (n * (uint64_t)(s + 1)) / (uint64_t)S;
-  const T *row = x + c * ld;
-  const double tc = tau[c];
-  const float fB = (float)B;
-  double sum = 0.0, sq = 0.0;
-  for (uint64_t base = t0; base < t1; base += CB_TILE) {
-    const int len = (int)min((uint64_t)CB_TILE, t1 - base);
-    __syncthreads();  // previous tile consumed (and bins zeroed on entry)
-    // At most CB_RUN samples per thread per tile: f32 partial sums (exact for
-    // 8-bit samples), one f64 add per tile (the FP64 pipe is narrow).
-    float ps = 0.0f, pq = 0.0f;
-    for (int i = threadIdx.x; i < len; i += CB_NT) {
-      const float v = (float)row[base + i];
-      tile[i + i / CB_RUN] = v;
-      ps += v;
-      pq += v * v;
-    }
-    sum += (double)ps;
-    sq += (double)pq;
-    __syncthreads();
-    const int r0 = threadIdx.x * CB_RUN;
-    if (r0 < len) {
-      const int r1 = min(r0 + CB_RUN, len);
-      // Phase at the tile start (f64, once per tile and thread, shared
-      // expression) plus the run offset: a quadratic in the offset, with the
-      // tile's cycles per sample (the f64 pipe is narrow on this GPU).
-      const double tdt = (double)base * tsamp - tc;
-      const double pht = nu * tdt + 0.5 * nudot * tdt * tdt;
-      const double dps_t = (nu + nudot * tdt) * tsamp;  // cycles per sample at the tile start
-      const double off = (double)r0;
-      const double ph = pht + off * (dps_t + 0.5 * nudot * tsamp * tsamp * off);
-      float u = (float)((ph - floor(ph)) * (double)B);
-      const double dps = dps_t + nudot * tsamp * tsamp * off;
-      const float du = (float)((dps - floor(dps)) * (double)B);
-      int cur = -1;
-      float a0 = 0.0f, a1 = 0.0f;
-      const float *run = tile + threadIdx.x * (CB_RUN + 1);
-      for (int i = r0; i < r1; ++i) {
-        const float v = run[i - r0];
-        float fl = floorf(u);
-        int b0 = (int)fl;
-        float w = u - fl;
-        if (b0 >= B) {
-          b0 = 0;
-          w = 0.0f;
-        }
-        if (b0 != cur) {
-          if (cur >= 0) {
-            atomicAdd(&bins[cur], a0);
-            atomicAdd(&bins[cur + 1 == B ? 0 : cur + 1], a1);
-          }
-          cur = b0;
-          a0 = a1 = 0.0f;
-        }
-        a0 += (1.0f - w) * v;
-        a1 += w * v;
-        u += du;
-        if (u >= fB) u -= fB;
-      }
-      if (cur >= 0) {
-        atomicAdd(&bins[cur], a0);
-        atomicAdd(&bins[cur + 1 == B ? 0 : cur + 1], a1);
-      }
-    }
+  const uint64_t rlo = t0 / CB_RUN, rhi = (t1 + CB_RUN - 1) / CB_RUN;  // runs [rlo, rhi)
+  if (tid == 0) {
+    // Phase (cycles) at sample m of the channel: nu td + nudot td^2 / 2,
+    // td = m tsamp - tau_c; f = d phase / d sample, g = d f / d sample.
+    const double td = (double)(rlo * CB_RUN) * tsamp - tau[c];
+    const double f = (nu + nudot * td) * tsamp, g = nudot * tsamp * tsamp;
+    const double R = (double)CB_RUN;
+    fx[0] = fix_frac(nu * td + 0.5 * nudot * td * td);  // phase at the first run
+    fx[1] = fix_frac(f);                                // cycles/sample there
+    fx[2] = fix_frac(R * f + 0.5 * g * R * R);          // run 1 - run 0
+    fx[3] = fix_frac(g * R * R);                        // its change per run
+    fx[4] = fix_frac(g * R);                            // f change per run
   }
+  __syncthreads();
+  // Thread j folds the contiguous runs [rlo + j q, rlo + (j + 1) q) so that
+  // the open bin carries from run to run.  Phase at run m (from rlo):
+  // P0 + m d1 + m (m - 1) / 2 d2, exact modulo 1.
+  const uint64_t q = (rhi - rlo + nt - 1) / nt;
+  const unsigned long long m = (unsigned long long)tid * q;
+  unsigned long long P = fx[0] + m * fx[2] + (m * (m - 1) / 2) * fx[3];
+  unsigned long long A = fx[2] + m * fx[3];
+  unsigned long long F = fx[1] + m * fx[4];
+  const unsigned long long D2 = fx[3], G = fx[4];
+  const float Bs = (float)B * 5.42101086242752217e-20f;  // B 2^-64
+  const float fB = (float)B;
+  const T *row = x + c * ld;
+  typename std::conditional<PRIV, PrivateBins, SharedBins>::type bins;
+  if constexpr (PRIV) bins = PrivateBins{hist, nt, tid};
+  else bins = SharedBins{hist};
+  RunSums<T> sums;
+  OpenBin ob;
+  const uint64_t r0 = rlo + m;
+  const int cnt = r0 < rhi ? (int)(min(r0 + q, rhi) - r0) : 0;
+  // Only the subint's first and last runs can hold samples outside [t0, t1).
+  const int lo0 = (int)(t0 - rlo * CB_RUN), hi1 = (int)(t1 - (rhi - 1) * CB_RUN);
+  const bool has_first = r0 == rlo, has_last = r0 + (uint64_t)cnt == rhi;
+  const T *src = row + r0 * CB_RUN;
+  RunRegs<T> cur, nxt;
+  if (cnt > 0) load_run(src, cur);
+  for (int i = 0; i < cnt; ++i) {
+    if (i + 1 < cnt) load_run(src + (i + 1) * CB_RUN, nxt);
+    if ((has_first && i == 0 && lo0 != 0) || (has_last && i == cnt - 1 && hi1 != CB_RUN))
+      mask_run(cur, (has_first && i == 0) ? lo0 : 0, (has_last && i == cnt - 1) ? hi1 : CB_RUN);
+    float u = __ull2float_rn(P) * Bs;
+    if (u >= fB) u -= fB;
+    fold_run(cur, u, __ull2float_rn(F) * Bs, B, bins, ob, sums);
+    P += A;
+    A += D2;
+    F += G;
+    cur = nxt;
+  }
+  if (ob.bin >= 0) flush_bins(bins, ob.bin, B, ob.a0, ob.a1);
+  double sum = sums.sum(), sq = sums.sq();
   for (int o = 16; o; o >>= 1) {
     sum += __shfl_down_sync(0xffffffffu, sum, o);
     sq += __shfl_down_sync(0xffffffffu, sq, o);
   }
-  if ((threadIdx.x & 31) == 0) {
-    red[0][threadIdx.x >> 5] = sum;
-    red[1][threadIdx.x >> 5] = sq;
+  if ((tid & 31) == 0) {
+    red[0][tid >> 5] = sum;
+    red[1][tid >> 5] = sq;
   }
   __syncthreads();
-  if (threadIdx.x < 2) {
+  if (tid < 2) {
     double a = 0.0;
-    for (int w2 = 0; w2 < CB_NT / 32; ++w2) a += red[threadIdx.x][w2];
-    chsum[(c * (uint64_t)S + (uint64_t)s) * 2 + threadIdx.x] = a;
-    if (threadIdx.x == 0) mean_s = (float)(a / (double)B);
+    for (int w2 = 0; w2 < nt / 32; ++w2) a += red[tid][w2];
+    chsum[(c * (uint64_t)S + (uint64_t)s) * 2 + tid] = a;
+    if (tid == 0) mean_s = (float)(a / (double)B);
   }
   __syncthreads();
   float *dst = cube + (c * (uint64_t)S + (uint64_t)s) * (uint64_t)B;
-  for (int b = threadIdx.x; b < B; b += blockDim.x) dst[b] = bins[b] - mean_s;
+  for (int b = tid; b < B; b += nt) {
+    float v;
+    if constexpr (PRIV) {
+      // column sums, skewed by the thread index so that a warp's reads of
+      // 32 consecutive rows fall in 32 different banks
+      const float *hb = hist + b * nt;
+      v = 0.0f;
+      for (int t = 0; t < nt; ++t) {
+        int k = t + tid;
+        if (k >= nt) k -= nt;
+        v += hb[k];
+      }
+    } else {
+      v = hist[b];
+    }
+    dst[b] = v - mean_s;
+  }
+}
+
+// Bin-owner fold for 1/31 <= du < 1 bins per sample (each bin holds 1 to 31
+// consecutive samples per period).  Each warp stages tiles of CB_TL samples
+// of the subint in shared memory; lane l owns bins l, l + 32, ... < B and,
+// for every unwrapped bin index m = b + k B that the tile's phase range
+// crosses, gathers the samples i in [Q(m), Q(m + 1)), Q(m) = ceil((m - ua) /
+// du) clamped to the tile (ua = bin position of the tile's first sample, the
+// phase linear across the tile).  Adjacent bins use the same Q, so every
+// sample is counted once.  The lane keeps S_b = sum v and T_b = sum (u - m) v
+// in registers; at the end bin b of the cloud-in-cell fold is S_b - T_b +
+// T_(b-1).  No atomics, no per-sample branches.
+constexpr int CB_TL = 2048;
+constexpr int CB_BO_MAXB = 256;
+constexpr int CB_BO_NB = CB_BO_MAXB / 32;
+
+template <class T>
+__global__ void __launch_bounds__(CB_NT)
+    k_cube_fold_bo(const T *__restrict__ x, uint64_t ld, uint64_t n, int S, int B, double tsamp,
+                   double nu, double nudot, const double *__restrict__ tau,
+                   float *__restrict__ cube, double *__restrict__ chsum) {
+  extern __shared__ __align__(16) unsigned char smem_bo[];
+  T *tiles = reinterpret_cast<T *>(smem_bo);  // [warp][CB_TL]
+  float *wS = reinterpret_cast<float *>(smem_bo + (size_t)(CB_NT / 32) * CB_TL * sizeof(T));
+  float *wT = wS + (CB_NT / 32) * B;
+  __shared__ unsigned long long fx[5];
+  __shared__ double red[2][CB_NT / 32];
+  __shared__ float mean_s;
+  const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int s = blockIdx.x;
+  const uint64_t c = blockIdx.y;
+  const uint64_t t0 = (n * (uint64_t)s) / (uint64_t)S, t1 = (n * (uint64_t)(s + 1)) / (uint64_t)S;
+  const uint64_t k0 = t0 / CB_TL, k1 = (t1 + CB_TL - 1) / CB_TL;  // tiles [k0, k1)
+  if (tid == 0) {
+    const double td = (double)(k0 * CB_TL) * tsamp - tau[c];
+    const double f = (nu + nudot * td) * tsamp, g = nudot * tsamp * tsamp;
+    const double L = (double)CB_TL;
+    fx[0] = fix_frac(nu * td + 0.5 * nudot * td * td);  // phase at tile k0
+    fx[1] = fix_frac(f);                                // cycles/sample there
+    fx[2] = fix_frac(L * f + 0.5 * g * L * L);          // tile 1 - tile 0
+    fx[3] = fix_frac(g * L * L);                        // its change per tile
+    fx[4] = fix_frac(g * L);                            // f change per tile
+  }
+  __syncthreads();
+  const float Bs = (float)B * 5.42101086242752217e-20f;  // B 2^-64
+  const float fB = (float)B;
+  const T *row = x + c * ld;
+  T *tile = tiles + (size_t)warp * CB_TL;
+  float Sb[CB_BO_NB], Tb[CB_BO_NB];
+#pragma unroll
+  for (int j = 0; j < CB_BO_NB; ++j) Sb[j] = Tb[j] = 0.0f;
+  RunSums<T> sums;
+  constexpr int PER = 16 / (int)sizeof(T);  // samples per 16-byte chunk
+  for (uint64_t k = k0 + warp; k < k1; k += CB_NT / 32) {
+    const uint64_t ta = k * CB_TL;
+    // Stage the tile (chunks wholly outside [t0, t1) are not loaded).
+    for (int q = lane; q < CB_TL / PER; q += 32) {
+      const uint64_t cs = ta + (uint64_t)q * PER;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (cs < t1 && cs + PER > t0) {
+        v = __ldg(reinterpret_cast<const uint4 *>(row + cs));
+        if (cs < t0 || cs + PER > t1) {  // mask samples outside [t0, t1)
+          T e[PER];
+          memcpy(e, &v, 16);
+#pragma unroll
+          for (int u = 0; u < PER; ++u)
+            if (cs + u < t0 || cs + u >= t1) e[u] = (T)0;
+          memcpy(&v, e, 16);
+        }
+      }
+      reinterpret_cast<uint4 *>(tile)[q] = v;
+      sums.add_chunk(v);
+    }
+    __syncwarp();
+    // Phase of the tile: fixed-point at its first sample, linear across it.
+    const unsigned long long kk = k - k0;
+    const unsigned long long P = fx[0] + kk * fx[2] + (kk * (kk - 1) / 2) * fx[3];
+    const unsigned long long F = fx[1] + kk * fx[4];
+    float ua = __ull2float_rn(P) * Bs;
+    if (ua >= fB) ua -= fB;
+    // (a tile's du only departs from the launch's nominal 1/31..1 through
+    // nudot; the floor keeps the partition finite)
+    const float du = fmaxf(__ull2float_rn(F) * Bs, 1e-3f);
+    const float inv = 1.0f / du;
+    const float uend = fmaf((float)CB_TL, du, ua);  // unwrapped phase past the tile
+    // an interval of 1/du holds at most floor(1/du) + 1 samples; one more
+    // covers the rounding of Q
+    const int cmax = (int)inv + 2;
+    const int mfirst = (int)ua;  // bin of the tile's first sample
+#pragma unroll
+    for (int j = 0; j < CB_BO_NB; ++j) {
+      const int b = lane + 32 * j;
+      if (b >= B) break;
+      // first unwrapped m = b + k B >= mfirst (0 <= mfirst < B)
+      int m = b >= mfirst ? b : b + B;
+      float sj = 0.0f, tj = 0.0f;
+      for (; (float)m < uend; m += B) {
+        const int i0 = max(0, (int)ceilf(((float)m - ua) * inv));
+        const int i1 = min(CB_TL, (int)ceilf(((float)(m + 1) - ua) * inv));
+        // sum v and sum (i - i0) v of the bin's samples, then its weights
+        // w_i = w_0 + (i - i0) du, w_0 = ua + i0 du - m
+        float sl = 0.0f, il = 0.0f, fq = 0.0f;
+        for (int q = 0; q < cmax; ++q) {
+          if (i0 + q >= i1) break;
+          const float v = (float)tile[i0 + q];
+          sl += v;
+          il = fmaf(fq, v, il);
+          fq += 1.0f;
+        }
+        sj += sl;
+        tj = fmaf(fmaf((float)i0, du, ua) - (float)m, sl, fmaf(du, il, tj));
+      }
+      Sb[j] += sj;
+      Tb[j] += tj;
+    }
+    __syncwarp();
+  }
+  // Per-warp bin sums to shared memory, then across warps.
+#pragma unroll
+  for (int j = 0; j < CB_BO_NB; ++j) {
+    const int b = lane + 32 * j;
+    if (b < B) {
+      wS[warp * B + b] = Sb[j];
+      wT[warp * B + b] = Tb[j];
+    }
+  }
+  double sum = sums.sum(), sq = sums.sq();
+  for (int o = 16; o; o >>= 1) {
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    sq += __shfl_down_sync(0xffffffffu, sq, o);
+  }
+  if (lane == 0) {
+    red[0][warp] = sum;
+    red[1][warp] = sq;
+  }
+  __syncthreads();
+  if (tid < 2) {
+    double a = 0.0;
+    for (int w2 = 0; w2 < CB_NT / 32; ++w2) a += red[tid][w2];
+    chsum[(c * (uint64_t)S + (uint64_t)s) * 2 + tid] = a;
+    if (tid == 0) mean_s = (float)(a / (double)B);
+  }
+  __syncthreads();
+  float *dst = cube + (c * (uint64_t)S + (uint64_t)s) * (uint64_t)B;
+  for (int b = tid; b < B; b += CB_NT) {
+    const int bp = b == 0 ? B - 1 : b - 1;
+    float sb = 0.0f, tb = 0.0f, tp = 0.0f;
+    for (int w2 = 0; w2 < CB_NT / 32; ++w2) {
+      sb += wS[w2 * B + b];
+      tb += wT[w2 * B + b];
+      tp += wT[w2 * B + bp];
+    }
+    dst[b] = sb - tb + tp - mean_s;
+  }
+}
+
+// Threads per fold CTA for B bins: private columns when B * threads fits
+// CB_PRIV floats with at least 32 threads.
+int cube_fold_threads(int B, bool &priv) {
+  int nt = (CB_PRIV / B) / 32 * 32;
+  priv = nt >= 32;
+  return priv ? std::min(nt, CB_NT) : CB_NT;
+}
+
+// du = bins per sample at the reference: the bin-owner gather for 1/31 <= du
+// < 1 (B <= 256), otherwise runs (analytic for 8-bit data at du < 1/31,
+// walked or scattered otherwise).
+template <class T>
+void launch_cube_fold(dim3 grid, int B, cudaStream_t st, const T *x, uint64_t ld, uint64_t n,
+                      int S, double tsamp, double nu, double nudot, const double *tau,
+                      float *cube, double *chsum) {
+  const double du = nu * tsamp * (double)B;
+  if (du >= 1.0 / 31.0 && du < 1.0 && B <= CB_BO_MAXB) {
+    const size_t sm = (size_t)(CB_NT / 32) * CB_TL * sizeof(T) + (size_t)2 * (CB_NT / 32) * B * 4;
+    cudaFuncSetAttribute(k_cube_fold_bo<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    k_cube_fold_bo<T><<<grid, CB_NT, sm, st>>>(x, ld, n, S, B, tsamp, nu, nudot, tau, cube,
+                                              chsum);
+    return;
+  }
+  // Below 1/31 bins per sample runs rarely change bin: one shared row with
+  // 256 threads; above 1 every sample changes bin: private columns.
+  bool priv = false;
+  const int nt = du < 1.0 ? CB_NT : cube_fold_threads(B, priv);
+  if (priv)
+    k_cube_fold<T, true><<<grid, nt, (size_t)B * nt * 4, st>>>(x, ld, n, S, B, tsamp, nu, nudot,
+                                                              tau, cube, chsum);
+  else
+    k_cube_fold<T, false><<<grid, nt, (size_t)B * 4, st>>>(x, ld, n, S, B, tsamp, nu, nudot,
+                                                          tau, cube, chsum);
 }
 
 struct CandDev {
@@ -316,11 +844,32 @@ __global__ void __launch_bounds__(CB_NT)
   }
 }
 
-struct CubeWork {
-  DevBuf cube, R, chsum, tau, kc, cands, prof, g, grad;
-  uint64_t rows = 0;
-  double var = 1.0;
-};
+
+// v = sum over channels of each channel's sample variance (the variance of a
+// sum of independent channels), from the per-(channel, subint) sums.
+__global__ void __launch_bounds__(CB_NT)
+    k_cube_var(const double *__restrict__ chsum, uint64_t nch, int S, uint64_t n,
+               double *__restrict__ out) {
+  __shared__ double red[CB_NT / 32];
+  double v = 0.0;
+  for (uint64_t c = threadIdx.x; c < nch; c += CB_NT) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int s = 0; s < S; ++s) {
+      s1 += chsum[(c * S + s) * 2];
+      s2 += chsum[(c * S + s) * 2 + 1];
+    }
+    const double m = s1 / (double)n;
+    v += fmax(s2 / (double)n - m * m, 0.0);
+  }
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < CB_NT / 32; ++w) a += red[w];
+    out[0] = a;
+  }
+}
 
 int build_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu, double nudot, double dm,
                CubeWork &w, cudaStream_t st) {
@@ -343,40 +892,28 @@ int build_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu, double n
   dim3 grid((unsigned)S, (unsigned)nch);
   switch (o.kind) {
     case SAMPLE_U8:
-      k_cube_fold<uint8_t><<<grid, CB_NT, 0, st>>>(o.samples.as<uint8_t>(), o.ld, n, S, B,
-                                                    o.h.tsamp, nu, nudot, w.tau.as<double>(),
-                                                    w.cube.as<float>(), w.chsum.as<double>());
+      launch_cube_fold(grid, B, st, o.samples.as<uint8_t>(), o.ld, n, S, o.h.tsamp, nu, nudot,
+                       w.tau.as<double>(), w.cube.as<float>(), w.chsum.as<double>());
       break;
     case SAMPLE_U16:
-      k_cube_fold<uint16_t><<<grid, CB_NT, 0, st>>>(o.samples.as<uint16_t>(), o.ld, n, S, B,
-                                                     o.h.tsamp, nu, nudot, w.tau.as<double>(),
-                                                     w.cube.as<float>(), w.chsum.as<double>());
+      launch_cube_fold(grid, B, st, o.samples.as<uint16_t>(), o.ld, n, S, o.h.tsamp, nu, nudot,
+                       w.tau.as<double>(), w.cube.as<float>(), w.chsum.as<double>());
       break;
     default:
-      k_cube_fold<float><<<grid, CB_NT, 0, st>>>(o.samples.as<float>(), o.ld, n, S, B,
-                                                  o.h.tsamp, nu, nudot, w.tau.as<double>(),
-                                                  w.cube.as<float>(), w.chsum.as<double>());
+      launch_cube_fold(grid, B, st, o.samples.as<float>(), o.ld, n, S, o.h.tsamp, nu, nudot,
+                       w.tau.as<double>(), w.cube.as<float>(), w.chsum.as<double>());
   }
   PSR_CUDA(cudaGetLastError());
   PSR_TRY(w.R.ensure(w.rows * (uint64_t)(B / 2) * sizeof(float2)));
   k_cube_dft<<<(unsigned)((w.rows + CB_ROWS - 1) / CB_ROWS), CB_NT, 0, st>>>(
       w.cube.as<float>(), w.rows, B, w.R.as<float2>());
   PSR_CUDA(cudaGetLastError());
-  std::vector<double> cs(w.rows * 2);
-  PSR_CUDA(cudaMemcpyAsync(cs.data(), w.chsum.p, cs.size() * 8, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaStreamSynchronize(st));
-  // v = sum over channels of each channel's sample variance (the variance of
-  // a sum of independent channels).
+  PSR_TRY(w.prof.ensure(16));
+  k_cube_var<<<1, CB_NT, 0, st>>>(w.chsum.as<double>(), nch, S, n, w.prof.as<double>());
+  PSR_CUDA(cudaGetLastError());
   double v = 0.0;
-  for (uint64_t c = 0; c < nch; ++c) {
-    double s1 = 0.0, s2 = 0.0;
-    for (int s = 0; s < S; ++s) {
-      s1 += cs[(c * S + s) * 2];
-      s2 += cs[(c * S + s) * 2 + 1];
-    }
-    const double m = s1 / (double)n;
-    v += std::fmax(s2 / (double)n - m * m, 0.0);
-  }
+  PSR_CUDA(cudaMemcpyAsync(&v, w.prof.p, 8, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
   w.var = v > 0.0 ? v : 1.0;
   return PSR_OK;
 }
@@ -461,7 +998,7 @@ void set_direction(Opt &s) {
 
 int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, uint64_t K,
                       const RefineOptions &opt, psr_timing *out, double *Jout, uint64_t *evals,
-                      cudaStream_t st) {
+                      CubeCache &cache, cudaStream_t st) {
   if (K == 0) return PSR_OK;
   const int B = (int)opt.bins, S = (int)opt.subints;
   if (B > CB_MAXB) {
@@ -479,7 +1016,8 @@ int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, u
   std::nth_element(sd.begin(), sd.begin() + K / 2, sd.end());
   const double nu_r = sn[K / 2], dm_r = sd[K / 2];
   const double nudot_r = -start[K / 2].pdot * nu_r * nu_r;
-  CubeWork w;
+  if (!cache.w) cache.w = new CubeWork();
+  CubeWork &w = *cache.w;
   PSR_TRY(build_cube(o, n, S, B, nu_r, nudot_r, dm_r, w, st));
   const double T = (double)n * o.h.tsamp;
   double fmax = 0.0, fmin = 1e300;

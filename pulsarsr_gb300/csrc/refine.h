@@ -40,9 +40,19 @@ int refine_gradient_one(const DeviceObs &o, uint64_t n, const psr_timing &start,
                         const RefineOptions &opt, RefineWork &w, psr_timing &out, double &J,
                         uint64_t &evals, cudaStream_t st);
 
+// Cube buffers shared by the groups of one refinement call.
+struct CubeWork;
+struct CubeCache {
+  CubeWork *w = nullptr;
+  CubeCache() = default;
+  CubeCache(const CubeCache &) = delete;
+  CubeCache &operator=(const CubeCache &) = delete;
+  ~CubeCache();
+};
+
 // Cube-based refinement of K nearby starting points (k_refine_cube.cu).
 int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, uint64_t K,
                       const RefineOptions &opt, psr_timing *out, double *J, uint64_t *evals,
-                      cudaStream_t st);
+                      CubeCache &cache, cudaStream_t st);
 
 }  // namespace psr

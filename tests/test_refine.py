@@ -190,3 +190,52 @@ def test_refinement_on_device_synthesised_pulsar(gpu):
     assert np.median(dp_grad) <= np.median(dp_grid) + P * P * resolution / 40
     assert np.median(dd_grad) <= np.median(dd_grid) + step / 8
     assert np.all(dp_grad < P * P * resolution / 4) and np.all(dd_grad < step)
+
+
+def cube_objective_np(x, freqs, tsamp, n, P, pdot, dm, B):
+    """J of the cube at its reference point (every shift zero): every
+    channel's samples [0, n) folded with cloud-in-cell weights at its own
+    dispersed phase, summed over channels, J = sum_b (p_b - mean)^2 / (n v),
+    v = sum of the channels' variances (f64 per sample)."""
+    nu = 1.0 / P
+    nudot = -pdot * nu * nu
+    fmax = freqs.max()
+    kc = 4148.808 * (1.0 / freqs ** 2 - 1.0 / fmax ** 2)
+    t = np.arange(n) * tsamp
+    prof = np.zeros(B)
+    v = 0.0
+    for c in range(x.shape[0]):
+        xc = x[c, :n].astype(np.float64)
+        td = t - kc[c] * dm
+        ph = nu * td + 0.5 * nudot * td * td
+        u = (ph - np.floor(ph)) * B
+        b0 = np.floor(u).astype(np.int64)
+        w = u - b0
+        b0 %= B
+        prof += np.bincount(b0, (1 - w) * xc, B) + np.bincount((b0 + 1) % B, w * xc, B)
+        v += xc.var()
+    return float(((prof - prof.mean()) ** 2).sum() / (n * v))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nbits,P,pdot", [(8, 0.0237, 0.0), (8, 0.0041, 2e-9),
+                                          (32, 0.0237, -1e-9), (32, 0.0041, 0.0),
+                                          (8, 1.3, 0.0), (8, 0.2, 5e-9), (16, 0.05, 0.0)])
+def test_cube_objective_matches_numpy_fold(gpu, nbits, P, pdot):
+    """The folded cube (one CTA per channel and subint, 32-sample runs,
+    fixed-point phases) against a plain f64 fold: J at the cube's reference
+    point, which refine_gradient returns after one evaluation.  Slow (< 1 bin
+    per sample) and fast pulsars, 8-bit and f32 data, n not a multiple of the
+    run length or the subint count."""
+    from pulsarsr_gb300 import fold, synth
+    DM = 57.3
+    fb = synth.device(48, nbits, 1 << 17, 64e-6, 1500.0, -400.0 / 48, seed=21,
+                      noise_mean={8: 100.0, 16: 3000.0}.get(nbits, 0.0),
+                      noise_sigma={8: 12.0, 16: 300.0}.get(nbits, 1.0),
+                      pulsars=[synth.Pulsar(P, DM, 0.05, 0.3, phase=0.2, pdot=pdot)])
+    x = fb.data
+    n = (1 << 17) - 3001
+    _, J, ev = fold.refine_gradient(fb, n, [(P, pdot, DM)], 128, 64, max_evals=1)
+    assert ev[0] == 1
+    Jn = cube_objective_np(x, fb.header.frequencies(), 64e-6, n, P, pdot, DM, 128)
+    assert np.isclose(J[0], Jn, rtol=2e-4), (J[0], Jn)
