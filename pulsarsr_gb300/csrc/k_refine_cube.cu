@@ -211,17 +211,28 @@ __device__ __forceinline__ unsigned long long fix_frac(double x) {
 
 // Bin accumulators of one CTA.  PrivateBins: one column per thread,
 // h[b * nt + tid] (bank = tid mod 32 for every b: no conflicts, no atomics),
-// summed over threads at the end; for B * threads <= CB_PRIV floats.
+// summed over threads at the end; for (B + 1) * threads <= CB_PRIV floats.
 // SharedBins: one row updated with shared-memory atomics (large B).
-constexpr int CB_PRIV = 8192;
+constexpr int CB_PRIV = 8448;  // 33 KB: 64 threads at B = 128
+// Both carry B + 1 rows: add2 puts a sample's second cloud-in-cell share in
+// row b + 1 without wrapping, and row B is folded into row 0 at the end.
 struct PrivateBins {
-  float *h;
-  int nt, tid;
-  __device__ __forceinline__ void add(int b, float x) const { h[b * nt + tid] += x; }
+  float *h;  // this thread's column: h[b * nt]
+  int nt;
+  __device__ __forceinline__ void add(int b, float x) const { h[b * nt] += x; }
+  __device__ __forceinline__ void add2(int b, float x0, float x1) const {
+    float *p = h + b * nt;
+    p[0] += x0;
+    p[nt] += x1;
+  }
 };
 struct SharedBins {
   float *h;
   __device__ __forceinline__ void add(int b, float x) const { atomicAdd(&h[b], x); }
+  __device__ __forceinline__ void add2(int b, float x0, float x1) const {
+    atomicAdd(&h[b], x0);
+    atomicAdd(&h[b + 1], x1);
+  }
 };
 
 template <class Bins>
@@ -244,6 +255,30 @@ struct OpenBin {
     }
   }
 };
+
+// du >= 1 bin per sample: every sample starts a new bin, so each goes
+// straight to its two bins (the open bin, if any, is flushed first).
+template <class T, class Bins>
+__device__ __forceinline__ void scatter_run(const RunRegs<T> &x, float u, float du, int B,
+                                            const Bins &bins, OpenBin &ob) {
+  if (ob.bin >= 0) {
+    flush_bins(bins, ob.bin, B, ob.a0, ob.a1);
+    ob.bin = -1;
+    ob.a0 = ob.a1 = 0.0f;
+  }
+  const float fB = (float)B;
+#pragma unroll
+  for (int i = 0; i < CB_RUN; ++i) {
+    // 0 <= u < B here (u >= B is wrapped below and at run starts), so
+    // floor(u) <= B - 1 and its second share lands in rows 1..B
+    const float v = run_sample<T>(x, i);
+    const float fl = floorf(u);
+    const float wv = (u - fl) * v;
+    bins.add2((int)fl, v - wv, wv);
+    u += du;
+    if (u >= fB) u -= fB;
+  }
+}
 
 // Fold one run starting at bin position u (bins) advancing du per sample;
 // the open bin carries over from the previous run of the same thread.
@@ -271,19 +306,7 @@ __device__ __forceinline__ void fold_run(const RunRegs<T> &x, float u, float du,
       }
     }
   } else {
-#pragma unroll
-    for (int i = 0; i < CB_RUN; ++i) {
-      const float v = run_sample<T>(x, i);
-      const float fl = floorf(u);
-      int b0 = (int)fl;
-      float w = u - fl;
-      if (b0 >= B) b0 = 0, w = 0.0f;
-      ob.move_to(b0, bins, B);
-      ob.a0 += v;
-      ob.a1 = fmaf(w, v, ob.a1);
-      u += du;
-      if (u >= fB) u -= fB;
-    }
+    scatter_run(x, u, du, B, bins, ob);
   }
 }
 
@@ -362,19 +385,7 @@ __device__ __forceinline__ void fold_run(const RunRegs<uint8_t> &x, float u, flo
       }
     }
   } else {
-#pragma unroll
-    for (int i = 0; i < CB_RUN; ++i) {
-      const float v = run_sample<uint8_t>(x, i);
-      const float fl = floorf(u);
-      int b0 = (int)fl;
-      float w = u - fl;
-      if (b0 >= B) b0 = 0, w = 0.0f;
-      ob.move_to(b0, bins, B);
-      ob.a0 += v;
-      ob.a1 = fmaf(w, v, ob.a1);
-      u += du;
-      if (u >= fB) u -= fB;
-    }
+    scatter_run(x, u, du, B, bins, ob);
   }
 }
 
@@ -393,7 +404,7 @@ __global__ void __launch_bounds__(CB_NT)
   const int nt = (int)blockDim.x, tid = (int)threadIdx.x;
   const int s = blockIdx.x;
   const uint64_t c = blockIdx.y;
-  const int hn = PRIV ? B * nt : B;
+  const int hn = PRIV ? (B + 1) * nt : B + 1;
   for (int i = tid; i < hn; i += nt) hist[i] = 0.0f;
   const uint64_t t0 = (n * (uint64_t)s) / (uint64_t)S, t1 = (n * (uint64_t)(s + 1)) / (uint64_t)S;
   const uint64_t rlo = t0 / CB_RUN, rhi = (t1 + CB_RUN - 1) / CB_RUN;  // runs [rlo, rhi)
@@ -423,7 +434,7 @@ __global__ void __launch_bounds__(CB_NT)
   const float fB = (float)B;
   const T *row = x + c * ld;
   typename std::conditional<PRIV, PrivateBins, SharedBins>::type bins;
-  if constexpr (PRIV) bins = PrivateBins{hist, nt, tid};
+  if constexpr (PRIV) bins = PrivateBins{hist + tid, nt};
   else bins = SharedBins{hist};
   RunSums<T> sums;
   OpenBin ob;
@@ -469,17 +480,20 @@ __global__ void __launch_bounds__(CB_NT)
   for (int b = tid; b < B; b += nt) {
     float v;
     if constexpr (PRIV) {
-      // column sums, skewed by the thread index so that a warp's reads of
-      // 32 consecutive rows fall in 32 different banks
-      const float *hb = hist + b * nt;
+      // row sums (row B joins row 0), skewed by the thread index so that a
+      // warp's reads of 32 consecutive rows fall in 32 different banks
       v = 0.0f;
-      for (int t = 0; t < nt; ++t) {
-        int k = t + tid;
-        if (k >= nt) k -= nt;
-        v += hb[k];
+      for (int r = b; r <= B; r += B) {
+        const float *hb = hist + r * nt;
+        for (int t = 0; t < nt; ++t) {
+          int k = t + tid;
+          if (k >= nt) k -= nt;
+          v += hb[k];
+        }
+        if (b != 0) break;
       }
     } else {
-      v = hist[b];
+      v = hist[b] + (b == 0 ? hist[B] : 0.0f);
     }
     dst[b] = v - mean_s;
   }
@@ -639,10 +653,10 @@ __global__ void __launch_bounds__(CB_NT)
   }
 }
 
-// Threads per fold CTA for B bins: private columns when B * threads fits
+// Threads per fold CTA for B bins: private columns when (B + 1) * threads fits
 // CB_PRIV floats with at least 32 threads.
 int cube_fold_threads(int B, bool &priv) {
-  int nt = (CB_PRIV / B) / 32 * 32;
+  int nt = (CB_PRIV / (B + 1)) / 32 * 32;
   priv = nt >= 32;
   return priv ? std::min(nt, CB_NT) : CB_NT;
 }
@@ -668,11 +682,11 @@ void launch_cube_fold(dim3 grid, int B, cudaStream_t st, const T *x, uint64_t ld
   bool priv = false;
   const int nt = du < 1.0 ? CB_NT : cube_fold_threads(B, priv);
   if (priv)
-    k_cube_fold<T, true><<<grid, nt, (size_t)B * nt * 4, st>>>(x, ld, n, S, B, tsamp, nu, nudot,
-                                                              tau, cube, chsum);
+    k_cube_fold<T, true><<<grid, nt, (size_t)(B + 1) * nt * 4, st>>>(
+        x, ld, n, S, B, tsamp, nu, nudot, tau, cube, chsum);
   else
-    k_cube_fold<T, false><<<grid, nt, (size_t)B * 4, st>>>(x, ld, n, S, B, tsamp, nu, nudot,
-                                                          tau, cube, chsum);
+    k_cube_fold<T, false><<<grid, nt, (size_t)(B + 1) * 4, st>>>(x, ld, n, S, B, tsamp, nu,
+                                                                nudot, tau, cube, chsum);
 }
 
 struct CandDev {
