@@ -547,6 +547,46 @@ def run_survey(args):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------ cube fold
+def run_fold(args):
+    """The cube fold of gradient refinement by regime: 256 ch x 8-bit x 2^23
+    samples (2.1 GB, larger than L2) at 64 us with three pulsars, each refined
+    alone with one evaluation (fold, row DFTs, one objective + adjoint) at 128
+    bins x 64 subints.  P 0.794 s: 0.010 bins per sample (8-bit run sums);
+    P 24.04 ms: 0.34 (bin-owner gather); P 2.04 ms: 4.0 (per-sample scatter)."""
+    from pulsarsr_gb300 import dedisperse, fold, synth
+    rt = cudart()
+    nch, ns, tsamp, fch1, foff = 256, 1 << 23, 64e-6, 1600.0, -400.0 / 256
+    regimes = [("slow", 0.79372, 2020.8), ("walk", 0.02404, 1024.1), ("fast", 0.00204, 2113.1)]
+    pulsars = [synth.Pulsar(P, dm, 0.04, 0.03, phase=0.3) for _, P, dm in regimes]
+    fb = synth.device(nch, 8, ns, tsamp, fch1, foff, seed=5, noise_mean=128.0,
+                      noise_sigma=16.0, gain_spread=0.1, pulsars=pulsars)
+    md = int(dedisperse.delays(fb.header.frequencies(), tsamp, 3000.0).max())
+    n = ns - md - 4
+    out = {}
+    for name, P, dm in regimes:
+        start = [(P * (1 + 1e-7), 0.0, dm + 0.3)]
+        for _ in range(max(args.warmup, 1)):
+            fold.refine_gradient(fb, n, start, max_evals=1)
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fold.refine_gradient(fb, n, start, max_evals=1)
+        rt.cudaDeviceSynchronize()
+        ms = (time.perf_counter() - t0) / args.steps * 1e3
+        out[name] = {"period_s": P, "bins_per_sample": round(128 * tsamp / P, 4),
+                     "ms_per_refine": round(ms, 4),
+                     "effective_GBps": round(nch * n / (ms * 1e-3) / 1e9, 1)}
+    line = {"metric": "cube fold + one evaluation, ms per call", "unit": "ms",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "dtype": "u8 data, f32 bins, fixed-point phases",
+            "data": "synthetic, generated on the device",
+            "config": {"workload": "256 ch x 8-bit x 2^23 samples (2.1 GB), 64 us, 128 bins x "
+                                   "64 subints, one start per regime", "n": int(n)},
+            "regimes": out}
+    print(json.dumps(line))
+
+
 # ------------------------------------------------------------ batch
 def run_batch(args):
     """64 seeded observations of uneven shape searched by one CUDA graph:
@@ -645,9 +685,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "fold"],
                     help="c1/c2: searches; c3: batch of 64 observations; c4: gradient vs "
-                         "grid refinement; c5: survey scale")
+                         "grid refinement; c5: survey scale; fold: the refinement cube "
+                         "fold by regime")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--trials", type=int, default=0,
                     help="search only the first N trial DMs (small profiling case)")
@@ -663,6 +704,8 @@ def main():
             run_survey(args)
         elif args.config == "c3":
             run_batch(args)
+        elif args.config == "fold":
+            run_fold(args)
         else:
             run_ours(args)
 
