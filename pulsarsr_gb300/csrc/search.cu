@@ -59,6 +59,10 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 16, st));
   nchunks = (ntrials + chunk - 1) / chunk;
   PSR_TRY(chunk_overflow.ensure(nchunks * 4 + 16));
+  if (!aux) PSR_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+  for (cudaEvent_t *e : {&ev_fft[0], &ev_fft[1], &ev_sel})
+    if (!*e) PSR_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  sel_pending = false;
   return PSR_OK;
 }
 
@@ -77,28 +81,47 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
     PSR_CUDA(cudaMemcpyAsync(means.p, host_means.data() + t0, nt * 4, cudaMemcpyHostToDevice,
                              st));
   }
-  PSR_TRY(spectrum_reset(sw, nt, st));
-  for (uint64_t i0 = 0; i0 < nt; i0 += inner) {
+  // aux runs after everything st has queued so far (the previous chunk's
+  // work is ordered on aux already), then resets the candidate queues.
+  PSR_CUDA(cudaEventRecord(ev_fft[1], st));
+  PSR_CUDA(cudaStreamWaitEvent(aux, ev_fft[1], 0));
+  PSR_TRY(spectrum_reset(sw, nt, aux));
+  // The power and psum slices are rewritten below: the previous chunk's
+  // selection must be done with them.
+  if (sel_pending) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel, 0));
+  uint64_t k = 0;
+  for (uint64_t i0 = 0; i0 < nt; i0 += inner, ++k) {
     const uint64_t ni = std::min(inner, nt - i0);
     PSR_TRY(record(ST_FFT, true, st));
     PSR_TRY(launch_raw_power_ex(fft, series.as<float>() + i0 * ldo, ldo, means.as<float>() + i0,
                                 ni, work.as<float2>(), power.as<float>() + i0 * ldp, ldp,
                                 psum.as<double>() + i0 * npsum, st));
     PSR_TRY(record(ST_FFT, false, st));
-    PSR_TRY(record(ST_SPEC, true, st));
+    cudaEvent_t e = ev_fft[k & 1];
+    PSR_CUDA(cudaEventRecord(e, st));
+    PSR_CUDA(cudaStreamWaitEvent(aux, e, 0));
+    PSR_TRY(record(ST_SPEC, true, aux));
     PSR_TRY(spectrum_gate(fft, spec, power.as<float>() + i0 * ldp, ldp,
-                          psum.as<double>() + i0 * npsum, npsum, ni, i0, sw, st));
-    PSR_TRY(record(ST_SPEC, false, st));
+                          psum.as<double>() + i0 * npsum, npsum, ni, i0, sw, aux));
+    PSR_TRY(record(ST_SPEC, false, aux));
   }
   const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
-  PSR_TRY(record(ST_SPEC, true, st));
-  PSR_TRY(spectrum_items(fft, spec, power.as<float>(), ldp, nt, sw, st));
+  PSR_TRY(record(ST_SPEC, true, aux));
+  PSR_TRY(spectrum_items(fft, spec, power.as<float>(), ldp, nt, sw, aux));
   PSR_TRY(spectrum_select(fft, spec, trial_dm.as<double>() + t0, nt, sw,
                           kept.as<psr_candidate>() + t0 * maxc, kept_count.as<unsigned>() + t0,
-                          st));
-  PSR_TRY(record(ST_SPEC, false, st));
+                          aux));
+  PSR_TRY(record(ST_SPEC, false, aux));
   PSR_CUDA(cudaMemcpyAsync(chunk_overflow.as<unsigned>() + ci, sw.overflow.p, 4,
-                           cudaMemcpyDeviceToDevice, st));
+                           cudaMemcpyDeviceToDevice, aux));
+  PSR_CUDA(cudaEventRecord(ev_sel, aux));
+  sel_pending = true;
+  return PSR_OK;
+}
+
+int SearchEngine::join(cudaStream_t st) {
+  if (sel_pending) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel, 0));
+  sel_pending = false;
   return PSR_OK;
 }
 
@@ -132,11 +155,14 @@ SearchEngine::~SearchEngine() {
     for (cudaEvent_t e : ev_begin[s]) cudaEventDestroy(e);
     for (cudaEvent_t e : ev_end[s]) cudaEventDestroy(e);
   }
+  for (cudaEvent_t e : {ev_fft[0], ev_fft[1], ev_sel})
+    if (e) cudaEventDestroy(e);
+  if (aux) cudaStreamDestroy(aux);
 }
 
 int SearchEngine::enqueue(const DeviceObs &o, cudaStream_t st) {
   for (uint64_t ci = 0; ci < nchunks; ++ci) PSR_TRY(enqueue_chunk(o, ci, st));
-  return PSR_OK;
+  return join(st);
 }
 
 int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
@@ -162,6 +188,7 @@ int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
       sw.queue_full = true;
       PSR_TRY(spectrum_prepare(fft, spec, chunk, inner, sw, st));
       PSR_TRY(enqueue_chunk(o, ci, st));
+      PSR_TRY(join(st));
       unsigned v = 0;
       PSR_CUDA(cudaMemcpyAsync(&v, chunk_overflow.as<unsigned>() + ci, 4,
                                cudaMemcpyDeviceToHost, st));

@@ -31,13 +31,22 @@ struct SearchEngine {
   ~SearchEngine();
   DevBuf delays, trial_dm, series, parts, sums, means, work, power, psum, kept, kept_count, err,
       chunk_overflow;
+  // The gates, harmonic items and selection of a chunk run on `aux`, so that
+  // they overlap the FFTs of the following inner chunks on the caller's
+  // stream.  ev_fft[i % 2]: FFT of inner chunk i done; ev_sel: the chunk's
+  // selection done (its power buffer may be overwritten).
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fft[2] = {nullptr, nullptr}, ev_sel = nullptr;
+  bool sel_pending = false;
 
   // Delay tables, FFT plan and buffers for ntrials trials of length n.
   int prepare(const DeviceObs &o, const double *trials, uint64_t ntrials, uint64_t n,
               const SpecConfig &cfg, cudaStream_t st);
   int enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st);
-  // All chunks, asynchronously.
+  // All chunks, asynchronously (joined back into st).
   int enqueue(const DeviceObs &o, cudaStream_t st);
+  // Make st wait for the aux-stream work queued so far.
+  int join(cudaStream_t st);
   // Synchronise; redo chunks whose raw candidate storage overflowed.
   int finish(const DeviceObs &o, cudaStream_t st);
   int collect(cudaStream_t st, uint64_t *counts, psr_candidate *out, uint64_t cap,
