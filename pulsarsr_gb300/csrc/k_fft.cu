@@ -23,6 +23,8 @@
 // inputs, the block synchronises, then stores.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <cmath>
 #include <vector>
 
@@ -151,6 +153,13 @@ __device__ __forceinline__ void dftR(float2 *v, const float2 *Wl) {
 
 // One in-place Stockham stage (radix R, Ns = product of earlier radices) on
 // C columns of length L; NT threads, each owning 16/R butterflies.
+// Slot distance of D positions when D*C is a multiple of 16 (the padding is
+// then D*C/16 slots): lay<C>(p + D, c) = lay<C>(p, c) + lay_step<C, D>().
+template <int C, int D>
+__host__ __device__ constexpr int lay_step() {
+  return D * C + (D * C) / 16;
+}
+
 template <int R, int L, int C, int NT, int Ns>
 __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
   constexpr int nb = L / R;
@@ -162,8 +171,14 @@ __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
     const int w = (int)threadIdx.x + i * NT;
     if (total % NT == 0 || w < total) {
       const int col = w % C, j = w / C;
+      if constexpr ((nb * C) % 16 == 0) {
+        const float2 *src = sm + lay<C>(j, col);
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[i][r] = sm[lay<C>(j + r * nb, col)];
+        for (int r = 0; r < R; ++r) v[i][r] = src[r * lay_step<C, nb>()];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[i][r] = sm[lay<C>(j + r * nb, col)];
+      }
       if constexpr (Ns > 1) {
         const int k = j % Ns;
         if (k != 0) {
@@ -181,8 +196,14 @@ __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
     if (total % NT == 0 || w < total) {
       const int col = w % C, j = w / C;
       const int base = (j / Ns) * Ns * R + j % Ns;
+      if constexpr ((Ns * C) % 16 == 0) {
+        float2 *dst = sm + lay<C>(base, col);
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[lay<C>(base + r * Ns, col)] = v[i][r];
+        for (int r = 0; r < R; ++r) dst[r * lay_step<C, Ns>()] = v[i][r];
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm[lay<C>(base + r * Ns, col)] = v[i][r];
+      }
     }
   }
   __syncthreads();
@@ -350,8 +371,16 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
           v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
         }
         dft16<M1>(v, Wl);
+        if constexpr (16 % C == 0) {
+          // e = (16j + r) C + col with col < C | 16: the padding of r C + col
+          // is (r C) / 16, so every r is a constant offset
+          float2 *dst = sm + 17 * C * j + col;
 #pragma unroll
-        for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
+          for (int r = 0; r < 16; ++r) dst[r * C + (r * C) / 16] = v[r];
+        } else {
+#pragma unroll
+          for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
+        }
       }
     }
   }
@@ -454,38 +483,47 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
       acc.add(p);
     }
   } else {
-    constexpr int PB = LB / 2;  // bins per batch (two twiddles each)
-    const int tot2 = M2 * h;
+    // Bins k = kb + p + M1 k2 and M - k.  W_N^(M-k) = (-W_N^k.re, W_N^k.im)
+    // holds bit for bit for the quarter-table lookup (its mirrored half is
+    // the swapped first half), up to the sign of zero components, which
+    // cannot change |X|^2.  Full groups (h == H) divide by a constant.
+    auto rows = [&](auto hc) {
+      constexpr int HC = decltype(hc)::value;
+      const int hh = HC > 0 ? HC : h;
+      constexpr int PB = LB;
+      const int tot2 = M2 * hh;
 #pragma unroll 1
-    for (int base = 0; base < tot2; base += PB * NT) {
-      float2 wk[PB], wm[PB];
+      for (int base = 0; base < tot2; base += PB * NT) {
+        float2 wk[PB];
+        uint32_t kk[PB];
+        int pp[PB], k2s[PB];
 #pragma unroll
-      for (int u = 0; u < PB; ++u) {
-        const int idx = base + u * NT + (int)threadIdx.x;
-        const uint32_t k = kb + (uint32_t)(idx % h) + M1 * (uint32_t)(idx / h);
-        const bool inb = idx < tot2;
-        wk[u] = inb ? twN(Q, k, lq) : make_float2(1.0f, 0.0f);
-        wm[u] = inb ? twN(Q, M - k, lq) : make_float2(1.0f, 0.0f);
-      }
+        for (int u = 0; u < PB; ++u) {
+          const int idx = base + u * NT + (int)threadIdx.x;
+          pp[u] = HC > 0 ? idx % HC : idx % hh;
+          k2s[u] = HC > 0 ? idx / HC : idx / hh;
+          kk[u] = kb + (uint32_t)pp[u] + M1 * (uint32_t)k2s[u];
+          wk[u] = idx < tot2 ? twN(Q, kk[u], lq) : make_float2(1.0f, 0.0f);
+        }
 #pragma unroll
-      for (int u = 0; u < PB; ++u) {
-        const int idx = base + u * NT + (int)threadIdx.x;
-        if (idx < tot2) {
-          const int p = idx % h;
-          const uint32_t k2 = (uint32_t)(idx / h);
-          const uint32_t k = kb + (uint32_t)p + M1 * k2;
-          const uint32_t mk = M - k;
-          const float2 zk = sm[lay<C>(k2, p)];
-          const float2 zm = sm[lay<C>(M2 - 1 - k2, h + p)];
-          const float pk = post_power(zk, zm, wk[u]);
-          const float pm = post_power(zm, zk, wm[u]);
-          out[k] = pk;
-          out[mk] = pm;
-          acc.add(pk);
-          acc.add(pm);
+        for (int u = 0; u < PB; ++u) {
+          const int idx = base + u * NT + (int)threadIdx.x;
+          if (idx < tot2) {
+            const uint32_t k = kk[u];
+            const float2 zk = sm[lay<C>(k2s[u], pp[u])];
+            const float2 zm = sm[lay<C>(M2 - 1 - k2s[u], hh + pp[u])];
+            const float pk = post_power(zk, zm, wk[u]);
+            const float pm = post_power(zm, zk, make_float2(-wk[u].x, wk[u].y));
+            out[k] = pk;
+            out[M - k] = pm;
+            acc.add(pk);
+            acc.add(pm);
+          }
         }
       }
-    }
+    };
+    if (h == H) rows(std::integral_constant<int, H>{});
+    else rows(std::integral_constant<int, 0>{});
   }
   block_sum_store<NT>(acc, psum + trial * ngroups + g);
 }
