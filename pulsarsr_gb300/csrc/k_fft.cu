@@ -389,6 +389,34 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
   float2 *out = work + trial * (uint64_t)M;
   // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 + n2]
   // (values identical to the quarter-table lookup), so these reads coalesce.
+  if constexpr (NT % C == 0 && 16 % C == 0 && (NT / C) % 2 == 0) {
+    // thread t drains column t % C at rows k1 = t / C + i NT / C: slot
+    // lay<C>(k1, col) = C k1 + col + (C k1) / 16 advances by a constant
+    constexpr int KS = NT / C;  // row step
+    const int col = (int)threadIdx.x % C, k10 = (int)threadIdx.x / C;
+    const uint32_t n2 = n2_0 + (uint32_t)col;
+    const float2 *src = sm + C * k10 + col + (C * k10) / 16;
+    const float2 *tws = tw1 + (uint64_t)k10 * M2 + n2;
+    float2 *dst = out + (uint64_t)k10 * M2 + n2;
+    constexpr int NI = M1 / KS;
+#pragma unroll 1
+    for (int i0 = 0; i0 < NI; i0 += LB) {
+      float2 w[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u)
+        w[u] = i0 + u < NI ? __ldg(tws + (uint64_t)(i0 + u) * KS * M2) : make_float2(1.0f, 0.0f);
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        if (i0 + u < NI) {
+          const int k1 = k10 + (i0 + u) * KS;
+          float2 v = src[(i0 + u) * lay_step<C, KS>()];
+          if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
+          dst[(uint64_t)(i0 + u) * KS * M2] = v;
+        }
+      }
+    }
+    return;
+  }
 #pragma unroll 1
   for (int base = 0; base < total; base += LB * NT) {
     float2 w[LB];
@@ -441,22 +469,39 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
   const int ncols = 2 * h;
   build_wl<M2>(Wl, N, Q, lq);
   const int total = M2 * ncols;
-#pragma unroll 1
-  for (int base = 0; base < total; base += LB * NT) {
-    float2 v[LB];
+  auto row_of = [&](int ci) -> uint32_t {
+    if (g == 0) return ci == 0 ? 0u : (uint32_t)(M1 / 2);
+    return ci < h ? kb + (uint32_t)ci : (uint32_t)M1 - (kb + (uint32_t)(ci - h));
+  };
+  if constexpr (C == 16 && NT == M2) {
+    // thread t loads position t of every row; slot lay<16>(t, ci) = 17 t + ci
+    const float2 *src = in + threadIdx.x;
+    float2 *dst = sm + 17 * threadIdx.x;
 #pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * NT + (int)threadIdx.x;
-      const int pos = idx % M2, ci = idx / M2;
-      uint32_t k1;
-      if (g == 0) k1 = ci == 0 ? 0 : M1 / 2;
-      else k1 = ci < h ? kb + ci : M1 - (kb + (ci - h));
-      v[u] = idx < total ? in[(uint64_t)k1 * M2 + pos] : make_float2(0.0f, 0.0f);
+    for (int c0 = 0; c0 < C; c0 += LB) {
+      float2 v[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u)
+        v[u] = c0 + u < ncols ? src[(uint64_t)row_of(c0 + u) * M2] : make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int u = 0; u < LB; ++u)
+        if (c0 + u < ncols) dst[c0 + u] = v[u];
     }
+  } else {
+#pragma unroll 1
+    for (int base = 0; base < total; base += LB * NT) {
+      float2 v[LB];
 #pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * NT + (int)threadIdx.x;
-      if (idx < total) sm[lay<C>(idx % M2, idx / M2)] = v[u];
+      for (int u = 0; u < LB; ++u) {
+        const int idx = base + u * NT + (int)threadIdx.x;
+        v[u] = idx < total ? in[(uint64_t)row_of(idx / M2) * M2 + idx % M2]
+                           : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int idx = base + u * NT + (int)threadIdx.x;
+        if (idx < total) sm[lay<C>(idx % M2, idx / M2)] = v[u];
+      }
     }
   }
   __syncthreads();
