@@ -25,6 +25,7 @@
 
 #include <type_traits>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -334,109 +335,128 @@ __global__ void __launch_bounds__(threads_for(M, 1))
 }
 
 // Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
+// Persistent: CTA b takes column groups b, b + gridDim.x, ... (group g =
+// trial g / (M2/C), columns (g % (M2/C)) C ...), builds the twiddle table
+// once, and while it transforms one group prefetches the next group's
+// samples into L2 (one 64-byte run of C complex inputs per row).
 template <int M1, int M2>
 __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
     k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
                 const float *__restrict__ means, const float2 *__restrict__ Q, int lq,
-                uint32_t N, const float2 *__restrict__ tw1, float2 *__restrict__ work) {
+                uint32_t N, const float2 *__restrict__ tw1, float2 *__restrict__ work,
+                uint32_t ngroups) {
   constexpr int C = cols_for(M1), NT = threads_for(M1, C);
   constexpr uint32_t M = (uint32_t)M1 * M2;
+  constexpr uint32_t GPT = M2 / C;  // column groups per trial
   extern __shared__ float2 dyn[];
   float2 *Wl = dyn;       // M1 entries
   float2 *sm = dyn + M1;  // lay_slots<M1, C>() entries
-  const uint64_t trial = blockIdx.y;
-  const uint32_t n2_0 = blockIdx.x * (uint32_t)C;
-  const float *row = series + trial * lds;
-  const float mean = means[trial];
   build_wl<M1>(Wl, N, Q, lq);
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
   constexpr int total = M1 * C;
   __syncthreads();  // Wl
-  {
-    // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
-    // (col, j) takes positions j + r*M1/16 of its column and stores its
-    // outputs at 16j + r.  The zero padding (n >= nz) is never loaded.
-    constexpr int nb = M1 / 16;
-    constexpr int nbt = nb * C;
-    constexpr int BPT = (nbt + NT - 1) / NT;
+  for (uint32_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+    const uint64_t trial = grp / GPT;
+    const uint32_t n2_0 = (grp % GPT) * (uint32_t)C;
+    const float *row = series + trial * lds;
+    const float mean = means[trial];
+    {
+      // (only inputs the next group loads: complex index < nz)
+      const uint32_t nx = grp + gridDim.x;
+      const uint64_t pn = (uint64_t)threadIdx.x * M2 + (nx % GPT) * (uint32_t)C;
+      if (nx < ngroups && pn < nz) {
+        const float *pr = series + (uint64_t)(nx / GPT) * lds + 2 * pn;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
+      }
+    }
+    {
+      // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
+      // (col, j) takes positions j + r*M1/16 of its column and stores its
+      // outputs at 16j + r.  The zero padding (n >= nz) is never loaded.
+      constexpr int nb = M1 / 16;
+      constexpr int nbt = nb * C;
+      constexpr int BPT = (nbt + NT - 1) / NT;
 #pragma unroll
-    for (int i = 0; i < BPT; ++i) {
-      const int w = (int)threadIdx.x + i * NT;
-      if (nbt % NT == 0 || w < nbt) {
-        const int col = w % C, j = w / C;
-        float2 v[16];
+      for (int i = 0; i < BPT; ++i) {
+        const int w = (int)threadIdx.x + i * NT;
+        if (nbt % NT == 0 || w < nbt) {
+          const int col = w % C, j = w / C;
+          float2 v[16];
 #pragma unroll
-        for (int r = 0; r < 16; ++r) {
-          const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
-          v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
-        }
-        dft16<M1>(v, Wl);
-        if constexpr (16 % C == 0) {
-          // e = (16j + r) C + col with col < C | 16: the padding of r C + col
-          // is (r C) / 16, so every r is a constant offset
-          float2 *dst = sm + 17 * C * j + col;
+          for (int r = 0; r < 16; ++r) {
+            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+          }
+          dft16<M1>(v, Wl);
+          if constexpr (16 % C == 0) {
+            // e = (16j + r) C + col with col < C | 16: the padding of r C +
+            // col is (r C) / 16, so every r is a constant offset
+            float2 *dst = sm + 17 * C * j + col;
 #pragma unroll
-          for (int r = 0; r < 16; ++r) dst[r * C + (r * C) / 16] = v[r];
-        } else {
+            for (int r = 0; r < 16; ++r) dst[r * C + (r * C) / 16] = v[r];
+          } else {
 #pragma unroll
-          for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
+            for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
+          }
         }
       }
     }
-  }
-  __syncthreads();
-  subfft_rest<M1, C, NT>(sm, Wl);
-  float2 *out = work + trial * (uint64_t)M;
-  // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 + n2]
-  // (values identical to the quarter-table lookup), so these reads coalesce.
-  if constexpr (NT % C == 0 && 16 % C == 0 && (NT / C) % 2 == 0) {
-    // thread t drains column t % C at rows k1 = t / C + i NT / C: slot
-    // lay<C>(k1, col) = C k1 + col + (C k1) / 16 advances by a constant
-    constexpr int KS = NT / C;  // row step
-    const int col = (int)threadIdx.x % C, k10 = (int)threadIdx.x / C;
-    const uint32_t n2 = n2_0 + (uint32_t)col;
-    const float2 *src = sm + C * k10 + col + (C * k10) / 16;
-    const float2 *tws = tw1 + (uint64_t)k10 * M2 + n2;
-    float2 *dst = out + (uint64_t)k10 * M2 + n2;
-    constexpr int NI = M1 / KS;
+    __syncthreads();
+    subfft_rest<M1, C, NT>(sm, Wl);
+    float2 *out = work + trial * (uint64_t)M;
+    // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 +
+    // n2] (values identical to the quarter-table lookup): reads coalesce.
+    if constexpr (NT % C == 0 && 16 % C == 0) {
+      // thread t drains column t % C at rows k1 = t / C + i NT / C: slot
+      // lay<C>(k1, col) = C k1 + col + (C k1) / 16 advances by a constant
+      constexpr int KS = NT / C;  // row step
+      const int col = (int)threadIdx.x % C, k10 = (int)threadIdx.x / C;
+      const uint32_t n2 = n2_0 + (uint32_t)col;
+      const float2 *src = sm + C * k10 + col + (C * k10) / 16;
+      const float2 *tws = tw1 + (uint64_t)k10 * M2 + n2;
+      float2 *dst = out + (uint64_t)k10 * M2 + n2;
+      constexpr int NI = M1 / KS;
 #pragma unroll 1
-    for (int i0 = 0; i0 < NI; i0 += LB) {
-      float2 w[LB];
+      for (int i0 = 0; i0 < NI; i0 += LB) {
+        float2 w[LB];
 #pragma unroll
-      for (int u = 0; u < LB; ++u)
-        w[u] = i0 + u < NI ? __ldg(tws + (uint64_t)(i0 + u) * KS * M2) : make_float2(1.0f, 0.0f);
+        for (int u = 0; u < LB; ++u)
+          w[u] = i0 + u < NI ? __ldg(tws + (uint64_t)(i0 + u) * KS * M2)
+                             : make_float2(1.0f, 0.0f);
 #pragma unroll
-      for (int u = 0; u < LB; ++u) {
-        if (i0 + u < NI) {
-          const int k1 = k10 + (i0 + u) * KS;
-          float2 v = src[(i0 + u) * lay_step<C, KS>()];
-          if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
-          dst[(uint64_t)(i0 + u) * KS * M2] = v;
+        for (int u = 0; u < LB; ++u) {
+          if (i0 + u < NI) {
+            const int k1 = k10 + (i0 + u) * KS;
+            float2 v = src[(i0 + u) * lay_step<C, KS>()];
+            if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
+            dst[(uint64_t)(i0 + u) * KS * M2] = v;
+          }
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int base = 0; base < total; base += LB * NT) {
+        float2 w[LB];
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+          const int idx = base + u * NT + (int)threadIdx.x;
+          w[u] = idx < total ? __ldg(&tw1[(uint64_t)(idx / C) * M2 + n2_0 + (idx % C)])
+                             : make_float2(1.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < LB; ++u) {
+          const int idx = base + u * NT + (int)threadIdx.x;
+          if (idx < total) {
+            const int col = idx % C, k1 = idx / C;
+            const uint32_t n2 = n2_0 + (uint32_t)col;
+            float2 v = sm[lay<C>(k1, col)];
+            if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
+            out[(uint64_t)k1 * M2 + n2] = v;
+          }
         }
       }
     }
-    return;
-  }
-#pragma unroll 1
-  for (int base = 0; base < total; base += LB * NT) {
-    float2 w[LB];
-#pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * NT + (int)threadIdx.x;
-      w[u] = idx < total ? __ldg(&tw1[(uint64_t)(idx / C) * M2 + n2_0 + (idx % C)])
-                         : make_float2(1.0f, 0.0f);
-    }
-#pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * NT + (int)threadIdx.x;
-      if (idx < total) {
-        const int col = idx % C, k1 = idx / C;
-        const uint32_t n2 = n2_0 + (uint32_t)col;
-        float2 v = sm[lay<C>(k1, col)];
-        if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
-        out[(uint64_t)k1 * M2 + n2] = v;
-      }
-    }
+    __syncthreads();  // the next group's stage 0 overwrites sm
   }
 }
 
@@ -607,9 +627,16 @@ int run_four_step(const FftArgs &a) {
     const size_t smem = (size_t)(M1 + lay_slots<M1, C>()) * sizeof(float2);
     PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
-    dim3 grid((unsigned)(M2 / C), (unsigned)a.ntrials);
-    k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(a.series, a.lds, a.len, a.means,
-                                                                    a.Q, a.lq, a.N, a.tw1, a.work);
+    const uint32_t ngroups = (uint32_t)(M2 / C) * (uint32_t)a.ntrials;
+    static int nsm = 0;
+    if (nsm == 0) {
+      int dev = 0;
+      PSR_CUDA(cudaGetDevice(&dev));
+      PSR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const uint32_t grid = std::min<uint32_t>(ngroups, 2u * (uint32_t)nsm);
+    k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(
+        a.series, a.lds, a.len, a.means, a.Q, a.lq, a.N, a.tw1, a.work, ngroups);
     PSR_CUDA(cudaGetLastError());
   }
   {
