@@ -1101,9 +1101,13 @@ int psr_measure(const float *x, uint64_t n, uint64_t offset, double tsamp, doubl
 }
 
 // ------------------------------------------------------------ session
-int psr_session_create(const psr_header *header, uint64_t nsamples, const double *trials,
-                       uint64_t ntrials, uint64_t discovery, const psr_search_config *cfg,
-                       uint64_t rfi_block_samples, float rfi_threshold, psr_session **out) {
+namespace {
+// psr_session_create with the engine's outer chunk fixed up front (0: the
+// default), so that a batch allocates each session's buffers once.
+int session_create(const psr_header *header, uint64_t nsamples, const double *trials,
+                   uint64_t ntrials, uint64_t discovery, const psr_search_config *cfg,
+                   uint64_t rfi_block_samples, float rfi_threshold, uint64_t chunk,
+                   psr_session **out) {
   if (!header || !trials || !valid_config(cfg) || !out || nsamples < 2 || header->nchans <= 0) {
     set_error("session: invalid arguments");
     return PSR_EINVAL;
@@ -1122,11 +1126,20 @@ int psr_session_create(const psr_header *header, uint64_t nsamples, const double
   s->trials.assign(trials, trials + ntrials);
   s->discovery = discovery;
   s->spec = to_spec(cfg, header->tsamp);
+  s->eng.chunk = chunk;
   PSR_TRY(s->eng.prepare(o, trials, ntrials, discovery, s->spec, s->stream.s));
   PSR_TRY(s->errbuf.ensure(8));
   PSR_CUDA(cudaStreamSynchronize(s->stream.s));
   *out = s.release();
   return PSR_OK;
+}
+}  // namespace
+
+int psr_session_create(const psr_header *header, uint64_t nsamples, const double *trials,
+                       uint64_t ntrials, uint64_t discovery, const psr_search_config *cfg,
+                       uint64_t rfi_block_samples, float rfi_threshold, psr_session **out) {
+  return session_create(header, nsamples, trials, ntrials, discovery, cfg, rfi_block_samples,
+                        rfi_threshold, 0, out);
 }
 
 int psr_session_load(psr_session *s, const uint8_t *payload, uint64_t nbytes) {
@@ -1308,7 +1321,8 @@ uint64_t chunk_for_budget(const psr_batch_obs *obs, uint64_t n, double budget) {
     const uint64_t len = obs[i].discovery;
     uint64_t p = 1;
     while (p < len) p <<= 1;
-    per_trial += 4.0 * (double)series_ld(len) + 4.0 * (double)(p + 64);
+    // series, two halves of power spectra, FFT work buffer (complex, p points)
+    per_trial += 4.0 * (double)series_ld(len) + 8.0 * (double)(p + 64) + 8.0 * (double)p;
   }
   const double c = per_trial > 0.0 ? budget / per_trial : 256.0;
   return (uint64_t)std::max(16.0, std::min(256.0, std::floor(c)));
@@ -1336,10 +1350,9 @@ int psr_batch_create(const psr_batch_obs *obs, uint64_t n, uint64_t hbm_budget_b
   for (uint64_t i = 0; i < n; ++i) {
     const psr_batch_obs &q = obs[i];
     psr_session *s = nullptr;
-    PSR_TRY(psr_session_create(&q.header, q.nsamples, q.trials, q.ntrials, q.discovery, &q.config,
-                               q.rfi_block_samples, q.rfi_threshold, &s));
+    PSR_TRY(session_create(&q.header, q.nsamples, q.trials, q.ntrials, q.discovery, &q.config,
+                           q.rfi_block_samples, q.rfi_threshold, chunk, &s));
     b->obs.emplace_back(s);
-    if (chunk < std::min<uint64_t>(256, q.ntrials)) PSR_TRY(reprepare(s, chunk, 0));
     b->chunk.push_back(s->eng.chunk);
     b->inner.push_back(s->eng.inner);
   }
@@ -1385,7 +1398,7 @@ int psr_batch_tune(psr_batch *b, uint64_t *chunk_out, uint64_t *inner_out) {
     const uint64_t c0 = b->chunk[i];
     std::vector<std::pair<uint64_t, uint64_t>> cand;
     for (uint64_t c : {c0, std::max<uint64_t>(16, c0 / 2)})
-      for (uint64_t inner : {(uint64_t)0, (uint64_t)4, (uint64_t)8})
+      for (uint64_t inner : {(uint64_t)0, (uint64_t)16, (uint64_t)64})
         cand.emplace_back(c, inner);
     double best = 1e300;
     std::pair<uint64_t, uint64_t> pick{c0, 0};

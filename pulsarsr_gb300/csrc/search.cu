@@ -38,8 +38,8 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   if (chunk == 0) chunk = 256;
   chunk = std::min(chunk, ntrials);
   if (inner == 0) {
-    const uint64_t per = (fft.m > 12 ? fft.M * 8 : 0) + ldp * 4;
-    inner = std::max<uint64_t>(1, (96ull << 20) / per);
+    const uint64_t per = fft.m > 12 ? fft.M * 8 : 1;  // FFT work buffer per trial
+    inner = std::max<uint64_t>(1, (4ull << 30) / per);
   }
   inner = std::min(inner, chunk);
   nparts = dedisperse_part_count(o, n);
@@ -49,8 +49,8 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   PSR_TRY(sums.ensure(chunk * 8));
   PSR_TRY(means.ensure(chunk * 4));
   PSR_TRY(work.ensure(fft.m > 12 ? inner * fft.M * 8 : 16));
-  PSR_TRY(power.ensure(chunk * ldp * 4));
-  PSR_TRY(psum.ensure(chunk * npsum * 8));
+  PSR_TRY(power.ensure(2 * chunk * ldp * 4));
+  PSR_TRY(psum.ensure(2 * chunk * npsum * 8));
   PSR_TRY(spectrum_prepare(fft, spec, chunk, inner, sw, st));
   const uint64_t maxc = std::max<uint64_t>(cfg.max_candidates, 1);
   PSR_TRY(kept.ensure(ntrials * maxc * sizeof(psr_candidate)));
@@ -60,9 +60,9 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   nchunks = (ntrials + chunk - 1) / chunk;
   PSR_TRY(chunk_overflow.ensure(nchunks * 4 + 16));
   if (!aux) PSR_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
-  for (cudaEvent_t *e : {&ev_fft[0], &ev_fft[1], &ev_sel})
+  for (cudaEvent_t *e : {&ev_fft[0], &ev_fft[1], &ev_sel[0], &ev_sel[1]})
     if (!*e) PSR_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-  sel_pending = false;
+  sel_pending[0] = sel_pending[1] = false;
   return PSR_OK;
 }
 
@@ -86,42 +86,46 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
   PSR_CUDA(cudaEventRecord(ev_fft[1], st));
   PSR_CUDA(cudaStreamWaitEvent(aux, ev_fft[1], 0));
   PSR_TRY(spectrum_reset(sw, nt, aux));
-  // The power and psum slices are rewritten below: the previous chunk's
-  // selection must be done with them.
-  if (sel_pending) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel, 0));
+  // This chunk's half of the power and psum buffers is rewritten below: the
+  // selection of the chunk that used it last must be done with it.
+  const int b = (int)(ci & 1);
+  float *pw = power.as<float>() + (uint64_t)b * chunk * ldp;
+  double *ps = psum.as<double>() + (uint64_t)b * chunk * npsum;
+  if (sel_pending[b]) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel[b], 0));
   uint64_t k = 0;
   for (uint64_t i0 = 0; i0 < nt; i0 += inner, ++k) {
     const uint64_t ni = std::min(inner, nt - i0);
     PSR_TRY(record(ST_FFT, true, st));
     PSR_TRY(launch_raw_power_ex(fft, series.as<float>() + i0 * ldo, ldo, means.as<float>() + i0,
-                                ni, work.as<float2>(), power.as<float>() + i0 * ldp, ldp,
-                                psum.as<double>() + i0 * npsum, st));
+                                ni, work.as<float2>(), pw + i0 * ldp, ldp, ps + i0 * npsum, st));
     PSR_TRY(record(ST_FFT, false, st));
     cudaEvent_t e = ev_fft[k & 1];
     PSR_CUDA(cudaEventRecord(e, st));
     PSR_CUDA(cudaStreamWaitEvent(aux, e, 0));
     PSR_TRY(record(ST_SPEC, true, aux));
-    PSR_TRY(spectrum_gate(fft, spec, power.as<float>() + i0 * ldp, ldp,
-                          psum.as<double>() + i0 * npsum, npsum, ni, i0, sw, aux));
+    PSR_TRY(spectrum_gate(fft, spec, pw + i0 * ldp, ldp, ps + i0 * npsum, npsum, ni, i0, sw,
+                          aux));
     PSR_TRY(record(ST_SPEC, false, aux));
   }
   const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
   PSR_TRY(record(ST_SPEC, true, aux));
-  PSR_TRY(spectrum_items(fft, spec, power.as<float>(), ldp, nt, sw, aux));
+  PSR_TRY(spectrum_items(fft, spec, pw, ldp, nt, sw, aux));
   PSR_TRY(spectrum_select(fft, spec, trial_dm.as<double>() + t0, nt, sw,
                           kept.as<psr_candidate>() + t0 * maxc, kept_count.as<unsigned>() + t0,
                           aux));
   PSR_TRY(record(ST_SPEC, false, aux));
   PSR_CUDA(cudaMemcpyAsync(chunk_overflow.as<unsigned>() + ci, sw.overflow.p, 4,
                            cudaMemcpyDeviceToDevice, aux));
-  PSR_CUDA(cudaEventRecord(ev_sel, aux));
-  sel_pending = true;
+  PSR_CUDA(cudaEventRecord(ev_sel[b], aux));
+  sel_pending[b] = true;
   return PSR_OK;
 }
 
 int SearchEngine::join(cudaStream_t st) {
-  if (sel_pending) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel, 0));
-  sel_pending = false;
+  for (int b = 0; b < 2; ++b) {
+    if (sel_pending[b]) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel[b], 0));
+    sel_pending[b] = false;
+  }
   return PSR_OK;
 }
 
@@ -155,7 +159,7 @@ SearchEngine::~SearchEngine() {
     for (cudaEvent_t e : ev_begin[s]) cudaEventDestroy(e);
     for (cudaEvent_t e : ev_end[s]) cudaEventDestroy(e);
   }
-  for (cudaEvent_t e : {ev_fft[0], ev_fft[1], ev_sel})
+  for (cudaEvent_t e : {ev_fft[0], ev_fft[1], ev_sel[0], ev_sel[1]})
     if (e) cudaEventDestroy(e);
   if (aux) cudaStreamDestroy(aux);
 }

@@ -6,9 +6,9 @@ namespace psr {
 
 struct SearchEngine {
   // Trials per outer chunk (dedispersion and candidate selection run over
-  // the whole chunk) and per inner chunk (FFT, normalisation and harmonic
-  // sums, sized so the FFT intermediate and the spectra stay in L2).
-  // 0 = automatic.
+  // the whole chunk) and per inner chunk (FFT and normalisation launches;
+  // large launches amortise their tails, so by default the whole chunk
+  // within a 4 GB FFT work buffer).  0 = automatic.
   uint64_t chunk = 0;
   uint64_t inner = 0;
   uint64_t ntrials = 0, n = 0, nch = 0, ldo = 0, ldp = 0, nparts = 0, nchunks = 0;
@@ -32,12 +32,13 @@ struct SearchEngine {
   DevBuf delays, trial_dm, series, parts, sums, means, work, power, psum, kept, kept_count, err,
       chunk_overflow;
   // The gates, harmonic items and selection of a chunk run on `aux`, so that
-  // they overlap the FFTs of the following inner chunks on the caller's
-  // stream.  ev_fft[i % 2]: FFT of inner chunk i done; ev_sel: the chunk's
-  // selection done (its power buffer may be overwritten).
+  // they overlap the FFTs of the following inner chunks and of the next
+  // chunk on the caller's stream.  ev_fft[i % 2]: FFT of inner chunk i done.
+  // The power spectra and their partial sums are double-buffered by chunk
+  // parity: ev_sel[b] = selection of the last chunk in half b done.
   cudaStream_t aux = nullptr;
-  cudaEvent_t ev_fft[2] = {nullptr, nullptr}, ev_sel = nullptr;
-  bool sel_pending = false;
+  cudaEvent_t ev_fft[2] = {nullptr, nullptr}, ev_sel[2] = {nullptr, nullptr};
+  bool sel_pending[2] = {false, false};
 
   // Delay tables, FFT plan and buffers for ntrials trials of length n.
   int prepare(const DeviceObs &o, const double *trials, uint64_t ntrials, uint64_t n,
