@@ -151,6 +151,66 @@ __global__ void k_chan_median(const T *__restrict__ s, uint64_t ns, uint64_t ld,
   }
 }
 
+// 8-bit rows: the median from a 256-bin histogram (one pass).  Each row is
+// split over MH_SPLIT CTAs; every thread counts into its own 16-bit column
+// of a [256][MH_NT] table in shared memory (no atomics, bank = thread / 2),
+// the columns are summed per bin and added to the row's global histogram.
+constexpr int MH_NT = 128;
+constexpr size_t MH_SMEM = 256 * MH_NT * sizeof(uint16_t);
+
+__global__ void __launch_bounds__(MH_NT)
+    k_chan_hist_u8(const uint8_t *__restrict__ s, uint64_t ns, uint64_t ld,
+                   unsigned *__restrict__ hist) {
+  extern __shared__ uint32_t h32[];
+  uint16_t *h16 = reinterpret_cast<uint16_t *>(h32);
+  const int tid = (int)threadIdx.x;
+  for (int i = tid; i < 256 * MH_NT / 2; i += MH_NT) h32[i] = 0u;
+  __syncthreads();
+  const uint8_t *row = s + (uint64_t)blockIdx.y * ld;
+  // this CTA's range [a, b), a a multiple of 16 (rows are 64-byte aligned
+  // and padded by >= 64 bytes, so whole 16-byte loads stay in the row)
+  const uint64_t per = (((ns + gridDim.x - 1) / gridDim.x) + 15) & ~15ull;
+  const uint64_t a = (uint64_t)blockIdx.x * per, b = min(ns, a + per);
+  uint16_t *mine = h16 + tid;
+  for (uint64_t i = a + (uint64_t)tid * 16; i < b; i += (uint64_t)MH_NT * 16) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(row + i));
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    const int m = (int)min((uint64_t)16, b - i);
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      if (k < m) mine[((w[k >> 2] >> (8 * (k & 3))) & 255u) * MH_NT] += 1;
+  }
+  __syncthreads();
+  for (int bin = tid; bin < 256; bin += MH_NT) {
+    const uint16_t *hb = h16 + bin * MH_NT;
+    unsigned t = 0;
+    for (int j = 0; j < MH_NT; ++j) {
+      int k = j + tid;
+      if (k >= MH_NT) k -= MH_NT;
+      t += hb[k];
+    }
+    if (t) atomicAdd(&hist[(uint64_t)blockIdx.y * 256 + bin], t);
+  }
+}
+
+// Element of rank ns / 2 from each row's histogram (one thread per row).
+__global__ void k_hist_median(const unsigned *__restrict__ hist, uint64_t nch, uint64_t ns,
+                              float *__restrict__ med) {
+  const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nch) return;
+  const uint64_t r = ns / 2;
+  uint64_t cum = 0;
+  int d = 255;
+  for (int k = 0; k < 256; ++k) {
+    cum += hist[c * 256 + k];
+    if (cum > r) {
+      d = k;
+      break;
+    }
+  }
+  med[c] = (float)d;
+}
+
 // Exact integer channel totals (for the provably-exact f32 fast path).
 template <class T>
 __global__ void k_chan_total(const T *__restrict__ s, uint64_t ns, uint64_t ld,
@@ -410,7 +470,20 @@ static int rfi_enqueue_t(DeviceObs &o, uint64_t bs, float thr, RfiWork &w, cudaS
                                                         w.vars.as<float>());
   k_block_sums<T><<<(unsigned)((nch * blocks_n + 127) / 128), 128, 0, st>>>(
       s, ns, o.ld, nch, bs, blocks_n, w.bsum.as<float>());
-  k_chan_median<T><<<(unsigned)nch, 512, 0, st>>>(s, ns, o.ld, w.med.as<float>());
+  if constexpr (sizeof(T) == 1) {
+    // per-thread counts stay below 2^16: at most ns / nsplit / MH_NT + 16
+    const uint64_t nsplit = std::max<uint64_t>(16, (ns + 60000ull * MH_NT - 1) / (60000ull * MH_NT));
+    PSR_TRY(w.mhist.ensure(nch * 256 * 4));
+    PSR_CUDA(cudaMemsetAsync(w.mhist.p, 0, nch * 256 * 4, st));
+    PSR_CUDA(cudaFuncSetAttribute(k_chan_hist_u8, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)MH_SMEM));
+    k_chan_hist_u8<<<dim3((unsigned)nsplit, (unsigned)nch), MH_NT, MH_SMEM, st>>>(
+        s, ns, o.ld, w.mhist.as<unsigned>());
+    k_hist_median<<<(unsigned)((nch + 127) / 128), 128, 0, st>>>(w.mhist.as<unsigned>(), nch, ns,
+                                                                 w.med.as<float>());
+  } else {
+    k_chan_median<T><<<(unsigned)nch, 512, 0, st>>>(s, ns, o.ld, w.med.as<float>());
+  }
   unsigned char *fl = w.flags.as<unsigned char>();
   k_channel_decide<<<1, 1024, 0, st>>>(w.means.as<float>(), w.vars.as<float>(), nch, thr,
                                        w.scratch.as<float>(), fl, fl + nch,

@@ -115,7 +115,7 @@ int launch_unpack(const DeviceObs &o, unsigned long long *d_err_index,
 
 // RFI mask (rfi::mask) on the device samples.  Scratch is owned by RfiWork.
 struct RfiWork {
-  DevBuf means, vars, med, bsum, bmeans, chbad, blkbad, scratch, flags, hist;
+  DevBuf means, vars, med, bsum, bmeans, chbad, blkbad, scratch, flags, hist, mhist;
   uint64_t blocks_n = 0;
 };
 struct RfiResult {
