@@ -169,6 +169,10 @@ int psr_rfi_mask(psr_fb *fb, uint64_t block_samples, float threshold,
                  uint64_t *channels, uint64_t *nchannels_bad, uint64_t *blocks,
                  uint64_t blocks_cap, uint64_t *nblocks_bad,
                  double *masked_fraction);
+/* The per-channel means and variances that rfi::mask computes before its
+ * decisions (rfi/src/lib.rs:35-43): f32 sums in the reference's order, bit
+ * for bit, on the device filterbank (not modified).  nchans floats each. */
+int psr_channel_stats(const psr_fb *fb, float *means, float *variances);
 
 /* -------------------------------------------------------- dedisperse */
 /* dedisperse::delays (dedisperse/src/lib.rs:9-34), host FP64, bit-exact. */

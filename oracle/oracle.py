@@ -110,6 +110,17 @@ def median(values) -> float:
     return float(lib().orc_median(_ptr(v, C.c_float), C.c_uint64(v.size)))
 
 
+def channel_stats(data: np.ndarray):
+    """rfi::mask's channel means and variances (reference-order f32 sums)."""
+    d = _f32(data)
+    nch, ns = d.shape
+    m = np.empty(nch, dtype=np.float32)
+    v = np.empty(nch, dtype=np.float32)
+    _check(lib().orc_channel_stats(_ptr(d, C.c_float), C.c_uint64(nch), C.c_uint64(ns),
+                                   _ptr(m, C.c_float), _ptr(v, C.c_float)))
+    return m, v
+
+
 def rfi_mask(data: np.ndarray, block_samples: int, threshold: float):
     """rfi::mask on a copy; returns (masked data, dict)."""
     d = np.array(data, dtype=np.float32, order="C", copy=True)

@@ -1358,6 +1358,24 @@ int orc_decode(const uint8_t *bytes, uint64_t len, int64_t limit,
 
 float orc_median(const float *values, uint64_t n) { return median_f32(values, n); }
 
+// rfi/src/lib.rs:35-43: the channel means and variances of rfi::mask.
+int orc_channel_stats(const float *data, uint64_t nchans, uint64_t nsamples, float *means,
+                      float *variances) {
+  if (nsamples == 0) return fail("channel_stats: empty rows");
+  for (uint64_t c = 0; c < nchans; ++c) {
+    const float *row = data + c * nsamples;
+    const float m = seq_sum_f32(row, nsamples) / (float)nsamples;
+    float s = -0.0f;
+    for (uint64_t t = 0; t < nsamples; ++t) {
+      const float d = row[t] - m;
+      s += d * d;
+    }
+    means[c] = m;
+    variances[c] = s / (float)nsamples;
+  }
+  return 0;
+}
+
 int orc_rfi_mask(float *data, uint64_t nchans, uint64_t nsamples,
                  uint64_t block_samples, float threshold, uint64_t *channels,
                  uint64_t *nchannels_bad, uint64_t *blocks, uint64_t blocks_cap,

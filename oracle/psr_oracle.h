@@ -82,6 +82,8 @@ int orc_decode(const uint8_t *bytes, uint64_t len, int64_t limit,
                orc_header *hdr, uint64_t *nsamples, float *out);
 
 float orc_median(const float *values, uint64_t n);
+int orc_channel_stats(const float *data, uint64_t nchans, uint64_t nsamples, float *means,
+                      float *variances);
 int orc_rfi_mask(float *data, uint64_t nchans, uint64_t nsamples,
                  uint64_t block_samples, float threshold,
                  uint64_t *channels, uint64_t *nchannels_bad,

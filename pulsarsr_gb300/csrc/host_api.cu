@@ -619,6 +619,14 @@ int psr_rfi_mask(psr_fb *fb, uint64_t block_samples, float threshold, uint64_t *
   return PSR_OK;
 }
 
+int psr_channel_stats(const psr_fb *fb, float *means, float *variances) {
+  if (!fb || !means || !variances) {
+    set_error("channel_stats: null argument");
+    return PSR_EINVAL;
+  }
+  return rfi_channel_stats(fb->o, means, variances, fb->stream.s);
+}
+
 int psr_delays(const double *freqs, uint64_t nchans, double tsamp, double dm, uint64_t *out) {
   std::vector<uint64_t> d;
   if (!host_delays(freqs, nchans, tsamp, dm, d)) return PSR_EDEDISPERSE;

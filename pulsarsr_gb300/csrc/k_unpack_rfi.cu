@@ -310,6 +310,192 @@ __global__ void __launch_bounds__(PC_NT)
   }
 }
 
+// Reference-order f32 sums of non-negative terms, s = RN(...RN(RN(-0 + t0) +
+// t1)... + t_{n-1}), bit for bit, in parallel.  While s stays in one binade
+// [2^e, 2^(e+1)) every representable value is a multiple of u = 2^(e-23), so
+// s = K u (2^23 <= K < 2^24) and RN(s + t) = (K + inc(t)) u with inc(t) =
+// t/u rounded to nearest: the integer part of t/u plus one when its fraction
+// exceeds 1/2.  Only an exact half depends on the running K (ties to even),
+// and t >= 0 makes K monotone.  So a 512-term chunk whose increments contain
+// no exact half and keep K + sum(inc) < 2^24 adds sum(inc) at once; any other
+// chunk (a tie, a binade crossing, s still 0 or subnormal) is added term by
+// term in order.
+constexpr int ES_L = 512;  // terms per chunk, 16 per lane
+
+struct SeqInc {
+  unsigned long long sum = 0;
+  bool tie = false;
+  // t = mt 2^et (mt < 2^24); K's unit u = 2^(e - 23)
+  __device__ __forceinline__ void add(float t, int e) {
+    const uint32_t b = __float_as_uint(t);
+    const int be = (int)((b >> 23) & 0xff);
+    if (be == 0 || be == 255) {  // zero adds nothing; subnormal, inf, NaN: in order
+      tie |= (b & 0x7fffffffu) != 0u;
+      return;
+    }
+    const uint32_t mt = (b & 0x7fffffu) | 0x800000u;
+    const int sh = (be - 150) - (e - 23);  // t / u = mt 2^sh
+    if (sh >= 0) {
+      // t >= 2^23 u > 2^e would leave the binade: count it as 2^40 units
+      // (any such term fails the K + sum < 2^24 test; no 64-bit overflow)
+      sum += sh >= 24 ? (1ull << 40) : ((unsigned long long)mt << sh);
+    } else if (sh > -25) {
+      const int r = -sh;
+      const uint32_t rem = mt & ((1u << r) - 1u), half = 1u << (r - 1);
+      sum += (unsigned long long)(mt >> r) + (rem > half ? 1ull : 0ull);
+      tie |= rem == half;
+    }
+  }
+};
+
+// Lane l's 16 consecutive samples of chunk g of a step: one or two aligned
+// 16-byte loads (rows start 64-element aligned; only issued for samples below
+// ns, whose 16-sample run then ends inside the row's padding).
+template <class T>
+struct EsRaw {
+  static constexpr int W = 16 * (int)sizeof(T) / 16;
+  uint4 r[W];
+  __device__ __forceinline__ void load(const T *p, bool ok) {
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+      r[k] = ok ? __ldg(reinterpret_cast<const uint4 *>(p) + k) : make_uint4(0u, 0u, 0u, 0u);
+  }
+  __device__ __forceinline__ float at(int j) const {
+    if constexpr (sizeof(T) == 1) {
+      const uint32_t w = (r[0].x * (j >> 2 == 0)) | (r[0].y * (j >> 2 == 1)) |
+                         (r[0].z * (j >> 2 == 2)) | (r[0].w * (j >> 2 == 3));
+      return (float)((w >> (8 * (j & 3))) & 255u);
+    } else {
+      const uint4 &q = r[j >> 3];
+      const int e = (j >> 1) & 3;
+      const uint32_t w = e == 0 ? q.x : (e == 1 ? q.y : (e == 2 ? q.z : q.w));
+      return (float)((w >> (16 * (j & 1))) & 65535u);
+    }
+  }
+};
+
+constexpr int ES_G = 4;  // chunks per step = warps per CTA
+
+// One CTA of ES_G warps per channel: warp w holds chunk w of every step of
+// ES_G chunks (its samples prefetched a step ahead), computes the chunk's
+// increment sum at the binade of the running s, and the CTA adds the longest
+// tie-free run of chunks that stays in the binade; a chunk that cannot be is
+// added term by term, in order, by thread 0.  Returns s in every thread.
+struct EsShared {
+  float stage[ES_L];
+  unsigned long long tot[ES_G];
+  int tie[ES_G];
+  float s;
+};
+
+template <class T, class Term>
+__device__ float exact_seq_sum_cta(const T *__restrict__ row, uint64_t ns, Term term,
+                                   EsShared &sh) {
+  const int lane = (int)(threadIdx.x & 31), g = (int)(threadIdx.x >> 5);
+  constexpr int PER = ES_L / 32;
+  constexpr uint64_t STEP = (uint64_t)ES_G * ES_L;
+  if (threadIdx.x == 0) sh.s = -0.0f;
+  EsRaw<T> raw, nxt;
+  {
+    const uint64_t i0 = (uint64_t)g * ES_L + (uint64_t)lane * PER;
+    raw.load(row + i0, i0 < ns);
+  }
+  __syncthreads();
+  for (uint64_t c0 = 0; c0 < ns; c0 += STEP) {
+    const uint64_t i0 = c0 + (uint64_t)g * ES_L + (uint64_t)lane * PER;
+    nxt.load(row + i0 + STEP, i0 + STEP < ns);
+    float t[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) t[j] = i0 + j < ns ? term(raw.at(j)) : 0.0f;
+    const int nchunk = (int)min((uint64_t)ES_G, (ns - c0 + ES_L - 1) / ES_L);
+    int g0 = 0;
+    while (g0 < nchunk) {  // g0 and sh.s are uniform across the CTA
+      const float s = sh.s;
+      const uint32_t sb = __float_as_uint(s);
+      const int se = (int)((sb >> 23) & 0xff);
+      int g1 = g0;
+      if (se > 0 && se < 255 && !(sb >> 31)) {
+        const int e = se - 127;
+        SeqInc inc;
+        if (g >= g0) {
+#pragma unroll
+          for (int j = 0; j < PER; ++j) inc.add(t[j], e);
+        }
+        unsigned long long tot = inc.sum;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        const bool tie = __any_sync(0xffffffffu, inc.tie);
+        if (lane == 0) {
+          sh.tot[g] = tot;
+          sh.tie[g] = tie ? 1 : 0;
+        }
+        __syncthreads();
+        unsigned long long acc = (sb & 0x7fffffu) | 0x800000u;
+        bool stop = false;
+#pragma unroll
+        for (int k = 0; k < ES_G; ++k) {
+          if (k >= g0 && k < nchunk && !stop) {
+            if (sh.tie[k] || acc + sh.tot[k] >= (1ull << 24)) {
+              stop = true;
+            } else {
+              acc += sh.tot[k];
+              g1 = k + 1;
+            }
+          }
+        }
+        __syncthreads();  // every thread has read sh.s, sh.tot and sh.tie
+        if (g1 > g0 && threadIdx.x == 0)
+          sh.s = __uint_as_float(((uint32_t)(e + 127) << 23) | ((uint32_t)acc & 0x7fffffu));
+      }
+      if (g1 == g0) {  // chunk g0 term by term
+        if (g == g0)
+#pragma unroll
+          for (int j = 0; j < PER; ++j) sh.stage[lane * PER + j] = t[j];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          float a = sh.s;
+          const int cnt = (int)min((uint64_t)ES_L, ns - (c0 + (uint64_t)g0 * ES_L));
+          for (int i = 0; i < cnt; ++i) a = __fadd_rn(a, sh.stage[i]);
+          sh.s = a;
+        }
+        g1 = g0 + 1;
+      }
+      __syncthreads();  // sh.s updated
+      g0 = g1;
+    }
+    raw = nxt;
+  }
+  return sh.s;
+}
+
+// Channel means and variances (rfi/src/lib.rs:35-43) for integer samples:
+// one warp per channel, the exact parallel reference-order sums above (the
+// mean straight from the exact integer total while it is below 2^24).
+template <class T>
+__global__ void __launch_bounds__(32 * ES_G)
+    k_chan_mean_var_ex(const T *__restrict__ s, uint64_t ns, uint64_t ld,
+                       const unsigned long long *__restrict__ tot, float *__restrict__ means,
+                       float *__restrict__ vars) {
+  __shared__ EsShared sh;
+  const uint64_t c = blockIdx.x;
+  const T *row = s + c * ld;
+  float m;
+  if (tot[c] <= (1ull << 24)) {
+    m = __fdiv_rn((float)tot[c], (float)ns);
+  } else {
+    m = __fdiv_rn(exact_seq_sum_cta(row, ns, [](float x) { return x; }, sh), (float)ns);
+    __syncthreads();  // sh is reused below
+  }
+  const float acc = exact_seq_sum_cta(row, ns, [m](float x) {
+    const float d = __fsub_rn(x, m);
+    return __fmul_rn(d, d);
+  }, sh);
+  if (threadIdx.x == 0) {
+    means[c] = m;
+    vars[c] = __fdiv_rn(acc, (float)ns);
+  }
+}
+
 // Per-(channel, block) sequential f32 sums (rfi/src/lib.rs:62-64).
 template <class T>
 __global__ void k_block_sums(const T *__restrict__ s, uint64_t ns, uint64_t ld,
@@ -466,8 +652,13 @@ static int rfi_enqueue_t(DeviceObs &o, uint64_t bs, float thr, RfiWork &w, cudaS
     dim3 g((unsigned)std::min<uint64_t>((ns + 255) / 256, 64), (unsigned)nch);
     k_chan_total<T><<<g, 256, 0, st>>>(s, ns, o.ld, tot);
   }
-  k_chan_mean_var_pc<T><<<(unsigned)nch, PC_NT, 0, st>>>(s, ns, o.ld, tot, w.means.as<float>(),
-                                                        w.vars.as<float>());
+  if constexpr (sizeof(T) < 4)
+    k_chan_mean_var_ex<T><<<(unsigned)nch, 32 * ES_G, 0, st>>>(s, ns, o.ld, tot, w.means.as<float>(),
+                                                       w.vars.as<float>());
+  else
+    k_chan_mean_var_pc<T><<<(unsigned)nch, PC_NT, 0, st>>>(s, ns, o.ld, tot,
+                                                          w.means.as<float>(),
+                                                          w.vars.as<float>());
   k_block_sums<T><<<(unsigned)((nch * blocks_n + 127) / 128), 128, 0, st>>>(
       s, ns, o.ld, nch, bs, blocks_n, w.bsum.as<float>());
   if constexpr (sizeof(T) == 1) {
@@ -497,6 +688,42 @@ static int rfi_enqueue_t(DeviceObs &o, uint64_t bs, float thr, RfiWork &w, cudaS
   k_fill<T><<<gf, 256, 0, st>>>(s, ns, o.ld, bs, w.chbad.as<unsigned char>(),
                                 w.blkbad.as<unsigned char>(), w.med.as<float>());
   PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+template <class T>
+static int channel_stats_t(const DeviceObs &o, RfiWork &w, cudaStream_t st) {
+  const uint64_t nch = o.nch, ns = o.ns;
+  PSR_TRY(w.means.ensure(nch * 4));
+  PSR_TRY(w.vars.ensure(nch * 4));
+  PSR_TRY(w.hist.ensure(nch * 8 + 8));
+  const T *s = o.samples.as<T>();
+  unsigned long long *tot = w.hist.as<unsigned long long>();
+  PSR_CUDA(cudaMemsetAsync(tot, 0, nch * 8 + 8, st));
+  if constexpr (sizeof(T) < 4) {
+    dim3 g((unsigned)std::min<uint64_t>((ns + 255) / 256, 64), (unsigned)nch);
+    k_chan_total<T><<<g, 256, 0, st>>>(s, ns, o.ld, tot);
+    k_chan_mean_var_ex<T><<<(unsigned)nch, 32 * ES_G, 0, st>>>(s, ns, o.ld, tot, w.means.as<float>(),
+                                                       w.vars.as<float>());
+  } else {
+    k_chan_mean_var_pc<T><<<(unsigned)nch, PC_NT, 0, st>>>(s, ns, o.ld, tot,
+                                                          w.means.as<float>(),
+                                                          w.vars.as<float>());
+  }
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
+
+int rfi_channel_stats(const DeviceObs &o, float *means, float *variances, cudaStream_t st) {
+  RfiWork w;
+  switch (o.kind) {
+    case SAMPLE_U8: PSR_TRY(channel_stats_t<uint8_t>(o, w, st)); break;
+    case SAMPLE_U16: PSR_TRY(channel_stats_t<uint16_t>(o, w, st)); break;
+    default: PSR_TRY(channel_stats_t<float>(o, w, st));
+  }
+  PSR_CUDA(cudaMemcpyAsync(means, w.means.p, o.nch * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(variances, w.vars.p, o.nch * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
   return PSR_OK;
 }
 

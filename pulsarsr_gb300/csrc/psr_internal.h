@@ -126,6 +126,8 @@ int rfi_enqueue(DeviceObs &o, uint64_t block_samples, float threshold,
                 RfiWork &w, cudaStream_t st);
 int rfi_collect(const DeviceObs &o, uint64_t block_samples, RfiWork &w,
                 cudaStream_t st, RfiResult &res);
+// The per-channel means and variances rfi::mask computes, to host arrays.
+int rfi_channel_stats(const DeviceObs &o, float *means, float *variances, cudaStream_t st);
 
 // Exact upper median of n device floats (radix select), result to d_out.
 int launch_median_f32(const float *d_vals, uint64_t n, float *d_out,

@@ -43,3 +43,14 @@ def mask(fb: Filterbank, block_samples: int, threshold: float) -> Mask:
                              C.byref(nbb), C.byref(frac)))
     return Mask([int(x) for x in ch[:nc.value]], [int(x) for x in bl[:nbb.value]],
                 int(block_samples), float(frac.value))
+
+
+def channel_stats(fb: Filterbank):
+    """The per-channel (means, variances) rfi::mask computes
+    (rfi/src/lib.rs:35-43), bit for bit; the filterbank is not modified."""
+    nch = fb.header.nchans
+    m = np.zeros(nch, dtype=np.float32)
+    v = np.zeros(nch, dtype=np.float32)
+    check(lib().psr_channel_stats(fb.handle, m.ctypes.data_as(C.POINTER(C.c_float)),
+                                  v.ctypes.data_as(C.POINTER(C.c_float))))
+    return m, v

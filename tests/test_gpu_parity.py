@@ -136,6 +136,44 @@ def test_rfi_mask_matches_oracle(gpu, oracle, nbits, ns, block):
     assert m.channels  # the planted channels are found
 
 
+@pytest.mark.parametrize("case", ["c2", "u8_big_total", "u16", "dyadic_ties", "constant"])
+def test_channel_stats_bit_exact(gpu, oracle, case):
+    """rfi::mask's channel means and variances: the device's parallel
+    reference-order sums against the oracle's sequential loops, bit for bit.
+    u8_big_total: channel totals above 2^24, so the mean is an inexact f32
+    chain too.  dyadic_ties: 2^16 samples of 0..3, so means and squared
+    deviations have few bits and exact rounding ties occur as the sums grow."""
+    from pulsarsr_gb300 import fbank, rfi, synth
+    from pulsarsr_gb300.synth import pack
+    rng = np.random.default_rng(7)
+    if case == "c2":
+        raw = synth.config_c2(2).to_bytes()
+    else:
+        nbits, ns = {"u8_big_total": (8, 1 << 20), "u16": (16, 60000),
+                     "dyadic_ties": (8, 1 << 16), "constant": (8, 5000)}[case]
+        o = synth.Observation(nchans=24, nbits=nbits, nsamples=ns, tsamp=64e-6, fch1=1450.,
+                              foff=-1.0, seed=11, noise_mean=100., noise_sigma=10.)
+        if case == "u8_big_total":
+            x = np.clip(np.rint(rng.normal(200, 20, (ns, 24))), 0, 255)
+        elif case == "u16":
+            x = np.clip(np.rint(rng.normal(30000, 3000, (ns, 24))), 0, 65535)
+        elif case == "dyadic_ties":
+            x = rng.integers(0, 4, (ns, 24)).astype(np.float64)
+            x[:, 3] = 1.0
+            x[::2, 4] = 3.0
+            x[1::2, 4] = 0.0
+        else:
+            x = np.full((ns, 24), 7.0)
+            x[:, 1] = 0.0
+        raw = o.header() + pack(x.astype(np.float32), nbits)
+    fb = fbank.decode(raw)
+    m, v = rfi.channel_stats(fb)
+    _, d = oracle.decode(raw)
+    om, ov = oracle.channel_stats(d)
+    assert m.tobytes() == om.tobytes()
+    assert v.tobytes() == ov.tobytes()
+
+
 # ------------------------------------------------------------ dedisperse
 @pytest.mark.parametrize("nbits", [4, 8, 32])
 def test_dedisperse_matches_oracle(gpu, oracle, nbits):
