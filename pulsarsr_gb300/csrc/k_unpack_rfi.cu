@@ -374,7 +374,7 @@ struct EsRaw {
   }
 };
 
-constexpr int ES_G = 4;  // chunks per step = warps per CTA
+constexpr int ES_G = 16;  // chunks per step = warps per CTA
 
 // One CTA of ES_G warps per channel: warp w holds chunk w of every step of
 // ES_G chunks (its samples prefetched a step ahead), computes the chunk's
