@@ -77,7 +77,8 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 }
 
 struct StageInfo {
-  long long base[DD_MAXCC];  // absolute sample index of the staged row start
+  long long base[DD_MAXCC];    // absolute sample index of the staged row start
+  int off[DD_MAXCC][DD_DB];    // tile start + delay - staged row start, per trial
 };
 
 // Issue the TMA copies of rows [c0, c0+cc) for trials [d0, d0+DB) of tile t0.
@@ -104,6 +105,10 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
     if (b > rowend) b = rowend;
     if (b > a + rowcap) b = a + rowcap;
     info->base[lane] = a;
+    for (int d = 0; d < DB; ++d) {
+      uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
+      info->off[lane][d] = (int)((long long)t0 - a) + (int)delays[tr * dstride + c];
+    }
     if (b > a) {
       bytes = (unsigned)(b - a);
       mbar_expect_tx(bar, bytes);
@@ -185,15 +190,13 @@ __global__ void __launch_bounds__(DD_NT, 2)
     const int rows = (int)min((uint64_t)cc, (uint64_t)(nch - c0));
     const uint8_t *buf = bufs[b];
     for (int r = 0; r < rows; ++r) {
-      const uint64_t c = c0 + r;
-      const int rel0 = (int)((long long)t0 - info[b].base[r]);  // t0 - staged row start
       const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
+      const int *offs = info[b].off[r];
       int prev = -1;
       uint32_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
 #pragma unroll
       for (int d = 0; d < DB; ++d) {
-        const uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
-        const int off = rel0 + (int)__ldg(&delays[tr * dstride + c]);
+        const int off = offs[d];  // shared-memory broadcast
         if (off != prev) {  // uniform across the CTA
           prev = off;
           const int q = tl + (off >> 4);
