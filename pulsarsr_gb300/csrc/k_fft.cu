@@ -468,7 +468,7 @@ template <int M1, int M2>
 __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
     k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q, int lq,
                 uint32_t N, float *__restrict__ power, uint64_t ldp, double *__restrict__ psum,
-                uint32_t ngroups) {
+                uint32_t ngroups, uint32_t ahead) {
   constexpr int C = cols_for(M2), NT = threads_for(M2, C), H = C / 2;
   constexpr uint32_t M = (uint32_t)M1 * M2;
   extern __shared__ float2 dyn[];
@@ -487,6 +487,26 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
     h = (int)min((uint32_t)H, (uint32_t)(M1 / 2 - kb));
   }
   const int ncols = 2 * h;
+  {
+    // Prefetch into L2 the rows of the CTA one resident wave ahead (linear
+    // index + ahead): CTAs start roughly in index order, so it runs soon.
+    const uint64_t lin = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x + ahead;
+    if (ahead && lin < (uint64_t)gridDim.x * gridDim.y) {
+      const uint32_t gn = (uint32_t)(lin % gridDim.x);
+      const uint64_t tn = lin / gridDim.x;
+      const uint32_t kbn = gn == 0 ? 0u : 1 + (gn - 1) * (uint32_t)H;
+      const int hn = gn == 0 ? 1 : (int)min((uint32_t)H, (uint32_t)(M1 / 2 - kbn));
+      constexpr int LPR = M2 * 8 / 128;  // 128-byte lines per row
+      for (int t = threadIdx.x; t < 2 * hn * LPR; t += NT) {
+        const int ci = t / LPR;
+        const uint32_t k1 = gn == 0 ? (ci == 0 ? 0u : (uint32_t)(M1 / 2))
+                                    : (ci < hn ? kbn + (uint32_t)ci
+                                               : (uint32_t)M1 - (kbn + (uint32_t)(ci - hn)));
+        const float2 *pr = work + tn * M + (uint64_t)k1 * M2 + (t % LPR) * 16;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
+      }
+    }
+  }
   build_wl<M2>(Wl, N, Q, lq);
   const int total = M2 * ncols;
   auto row_of = [&](int ci) -> uint32_t {
@@ -646,8 +666,14 @@ int run_four_step(const FftArgs &a) {
                                   (int)smem));
     const uint32_t ng = 1 + ((uint32_t)M1 / 2 - 1 + C / 2 - 1) / (C / 2);
     dim3 grid(ng, (unsigned)a.ntrials);
-    k_fft_pass2<M1, M2><<<grid, threads_for(M2, C), smem, a.st>>>(a.work, a.Q, a.lq, a.N, a.power,
-                                                                    a.ldp, a.psum, ng);
+    static int nsm2 = 0;
+    if (nsm2 == 0) {
+      int dev = 0;
+      PSR_CUDA(cudaGetDevice(&dev));
+      PSR_CUDA(cudaDeviceGetAttribute(&nsm2, cudaDevAttrMultiProcessorCount, dev));
+    }
+    k_fft_pass2<M1, M2><<<grid, threads_for(M2, C), smem, a.st>>>(
+        a.work, a.Q, a.lq, a.N, a.power, a.ldp, a.psum, ng, 2u * (uint32_t)nsm2);
     PSR_CUDA(cudaGetLastError());
   }
   return PSR_OK;
