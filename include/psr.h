@@ -459,6 +459,11 @@ int psr_batch_load_fb(psr_batch *b, uint64_t i, const psr_fb *fb);
  * (dedispersion block, FFT chunk) pairs and keeps the fastest; chunk/inner
  * (n entries each, may be NULL) receive the choices. */
 int psr_batch_tune(psr_batch *b, uint64_t *chunk, uint64_t *inner);
+/* Pin observation i's dedispersion block (trials per outer chunk, >= 1) and
+ * FFT launch size (trials per inner chunk; 0 = the whole block within a 4 GB
+ * work buffer): the manual counterpart of psr_batch_tune.  No reference
+ * counterpart. */
+int psr_batch_set_chunking(psr_batch *b, uint64_t i, uint64_t chunk, uint64_t inner);
 int psr_batch_run(psr_batch *b);
 int psr_batch_sync(psr_batch *b);
 int psr_batch_candidates(psr_batch *b, uint64_t i, uint64_t *counts, psr_candidate *out,

@@ -61,6 +61,11 @@ class Batch:
                                    inner.ctypes.data_as(C.POINTER(C.c_uint64))))
         return ch, inner
 
+    def set_chunking(self, i: int, chunk: int, inner: int = 0) -> None:
+        """Pin observation i's DM block and FFT launch size (trials)."""
+        check(lib().psr_batch_set_chunking(self._b, C.c_uint64(i), C.c_uint64(chunk),
+                                           C.c_uint64(inner)))
+
     def run(self) -> None:
         check(lib().psr_batch_run(self._b))
 

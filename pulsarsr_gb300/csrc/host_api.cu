@@ -1395,6 +1395,19 @@ int psr_batch_load_fb(psr_batch *b, uint64_t i, const psr_fb *fb) {
 // Autotuner: for every observation, time one whole search at each (DM block,
 // FFT chunk) pair of a small set around the defaults, on the loaded data,
 // and keep the fastest.  Results per observation are in chunk/inner.
+int psr_batch_set_chunking(psr_batch *b, uint64_t i, uint64_t chunk, uint64_t inner) {
+  if (!b || i >= b->obs.size() || chunk == 0) {
+    set_error("batch: observation index out of range or empty DM block");
+    return PSR_EINVAL;
+  }
+  b->drop_graph();
+  psr_session *s = b->obs[i].get();
+  PSR_TRY(reprepare(s, chunk, inner));
+  b->chunk[i] = s->eng.chunk;
+  b->inner[i] = s->eng.inner;
+  return PSR_OK;
+}
+
 int psr_batch_tune(psr_batch *b, uint64_t *chunk_out, uint64_t *inner_out) {
   if (!b) {
     set_error("batch: null handle");
