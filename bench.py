@@ -176,6 +176,22 @@ def measured_traffic(stage):
     return d["dram_bytes_per_launch"] / d["trials_per_launch"]
 
 
+def max_over_ranks(x: float, dist) -> float:
+    """The slowest rank's value (all ranks get it); x itself without a group."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, ms: float, world: int) -> float:
+    """Whole-job rate of `world` replicas that each process units_per_rank
+    units, timed by the slowest rank (weak scaling)."""
+    return world * units_per_rank / (ms / 1e3)
+
+
 def run_ours(args):
     from pulsarsr_gb300 import fbank, search, session
     rank = int(os.environ.get("RANK", "0"))
@@ -224,14 +240,9 @@ def run_ours(args):
         times.append(ev.ms(a, b))
     rt.cudaDeviceSynchronize()
     clk = clocks.stop()
-    ms = statistics.mean(times)
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(statistics.mean(times), dist)
     units = len(trials) * discovery
-    value = world * units / (ms / 1e3)
+    value = replica_throughput(units, ms, world)
     counts, cands = s.candidates()
     # ---- end to end through the public API with host buffers
     e2e = []
