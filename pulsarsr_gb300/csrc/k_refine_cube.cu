@@ -286,7 +286,6 @@ template <class T, class Bins>
 __device__ __forceinline__ void fold_run(const RunRegs<T> &x, float u, float du, int B,
                                          const Bins &bins, OpenBin &ob, RunSums<T> &sums) {
   sums.add(x);
-  const float fB = (float)B;
   if (du < 1.0f) {
     int b = (int)u;
     if (b >= B) b = 0, u = 0.0f;
@@ -367,7 +366,6 @@ __device__ __forceinline__ void fold_run(const RunRegs<uint8_t> &x, float u, flo
     return;
   }
   // Sample-by-sample walk.
-  const float fB = (float)B;
   if (du < 1.0f) {
     float w = w0;
     ob.move_to(b, bins, B);
