@@ -284,9 +284,11 @@ def run_ours(args):
     D = st["dedisperse"][1] // 2
     F = st["fft"][1] // 2
     fft_kernels = 2 if N // 2 > 4096 else 1
-    # unpack + 8 RFI kernels; per outer chunk dedisperse + reduce + select;
-    # per inner chunk the FFT pass(es), scales and harmonic kernels
-    launches = 1 + 8 + D * 3 + F * (fft_kernels + 2)
+    # unpack + 9 RFI kernels (8-bit storage: totals, mean/variance, block sums,
+    # median histograms + pick, channel and block decisions, block means,
+    # fill); per outer chunk dedispersion + part reduction + harmonic items +
+    # selection; per inner chunk the FFT pass(es) and the scales/gates kernel
+    launches = 1 + 9 + D * 4 + F * (fft_kernels + 1)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
