@@ -288,29 +288,27 @@ __global__ void __launch_bounds__(SC_NT)
   }
   __syncthreads();
   {
-    // Thread t sorts chunk t in registers (fully unrolled bitonic network of
-    // 672 compare-exchanges: no shuffles, static register indices).  The
-    // stride-65 layout makes these row reads bank-conflict free.
+    // Thread t sorts chunk t in registers: Batcher's odd-even merge sort
+    // network (543 compare-exchanges for 64 keys), fully unrolled, so every
+    // register index is static and there are no shuffles.  The stride-65
+    // layout makes these row reads bank-conflict free.
     uint32_t x[64];
     uint32_t *row = ch + threadIdx.x * SC_STRIDE;
 #pragma unroll
     for (int i = 0; i < 64; ++i) x[i] = row[i];
+    // (merge step (p, k) compares a with a + k for every a >= k % p with
+    // (a - k % p) mod 2k < k, both in one block of 2p)
 #pragma unroll
-    for (int k = 2; k <= 64; k <<= 1)
+    for (int p = 1; p < 64; p <<= 1)
 #pragma unroll
-      for (int j = k >> 1; j > 0; j >>= 1)
+      for (int k = p; k >= 1; k >>= 1)
 #pragma unroll
-        for (int i = 0; i < 64; ++i) {
-          const int l = i ^ j;
-          if (l > i) {
-            const uint32_t p0 = x[i], p1 = x[l];
-            if ((i & k) == 0) {
-              x[i] = min(p0, p1);
-              x[l] = max(p0, p1);
-            } else {
-              x[i] = max(p0, p1);
-              x[l] = min(p0, p1);
-            }
+        for (int a = 0; a < 64; ++a) {
+          const int c = a + k, j0 = k % p;
+          if (c < 64 && a >= j0 && (a - j0) % (2 * k) < k && a / (2 * p) == c / (2 * p)) {
+            const uint32_t p0 = x[a], p1 = x[c];
+            x[a] = min(p0, p1);
+            x[c] = max(p0, p1);
           }
         }
 #pragma unroll
