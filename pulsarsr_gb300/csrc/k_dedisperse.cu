@@ -389,12 +389,12 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
     const uint64_t ntiles = (n + DD_TT - 1) / DD_TT;
     int rowcap = (int)(((uint64_t)DD_TT + max_spread + 32 + 15) & ~(uint64_t)15);
     int dev = 0;
-    cudaGetDevice(&dev);
+    PSR_CUDA(cudaGetDevice(&dev));
     int smax = 0;
-    cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    PSR_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     // two CTAs per SM: each gets half of the SM's shared memory
     int smsm = 0;
-    cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    PSR_CUDA(cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     size_t budget = std::min((size_t)smax, (size_t)smsm / 2) - 4096;
     const uint64_t glen = std::min<uint64_t>(gch, o.nch);
     int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, glen, budget / (2 * (size_t)rowcap)});

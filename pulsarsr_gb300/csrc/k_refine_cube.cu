@@ -663,17 +663,17 @@ int cube_fold_threads(int B, bool &priv) {
 // < 1 (B <= 256), otherwise runs (analytic for 8-bit data at du < 1/31,
 // walked or scattered otherwise).
 template <class T>
-void launch_cube_fold(dim3 grid, int B, cudaStream_t st, const T *x, uint64_t ld, uint64_t n,
-                      int S, double tsamp, double nu, double nudot, const double *tau,
-                      float *cube, double *chsum) {
+int launch_cube_fold(dim3 grid, int B, cudaStream_t st, const T *x, uint64_t ld, uint64_t n,
+                     int S, double tsamp, double nu, double nudot, const double *tau,
+                     float *cube, double *chsum) {
   const double du = nu * tsamp * (double)B;
   if (du >= 1.0 / 31.0 && du < 1.0 && B <= CB_BO_MAXB) {
     const size_t sm = (size_t)(CB_NT / 32) * CB_TL * sizeof(T) + (size_t)2 * (CB_NT / 32) * B * 4;
-    cudaFuncSetAttribute(k_cube_fold_bo<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
+    PSR_CUDA(cudaFuncSetAttribute(k_cube_fold_bo<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
     k_cube_fold_bo<T><<<grid, CB_NT, sm, st>>>(x, ld, n, S, B, tsamp, nu, nudot, tau, cube,
                                               chsum);
-    return;
+    return PSR_OK;
   }
   // Below 1/31 bins per sample runs rarely change bin: one shared row with
   // 256 threads; above 1 every sample changes bin: private columns.
@@ -685,6 +685,7 @@ void launch_cube_fold(dim3 grid, int B, cudaStream_t st, const T *x, uint64_t ld
   else
     k_cube_fold<T, false><<<grid, nt, (size_t)(B + 1) * 4, st>>>(x, ld, n, S, B, tsamp, nu,
                                                                 nudot, tau, cube, chsum);
+  return PSR_OK;
 }
 
 struct CandDev {
@@ -902,18 +903,21 @@ int build_cube(const DeviceObs &o, uint64_t n, int S, int B, double nu, double n
   PSR_CUDA(cudaMemcpyAsync(w.tau.p, tau.data(), nch * 8, cudaMemcpyHostToDevice, st));
   PSR_CUDA(cudaMemcpyAsync(w.kc.p, kc.data(), nch * 8, cudaMemcpyHostToDevice, st));
   dim3 grid((unsigned)S, (unsigned)nch);
+  const double *tp = w.tau.as<double>();
+  float *cp = w.cube.as<float>();
+  double *sp = w.chsum.as<double>();
   switch (o.kind) {
     case SAMPLE_U8:
-      launch_cube_fold(grid, B, st, o.samples.as<uint8_t>(), o.ld, n, S, o.h.tsamp, nu, nudot,
-                       w.tau.as<double>(), w.cube.as<float>(), w.chsum.as<double>());
+      PSR_TRY(launch_cube_fold(grid, B, st, o.samples.as<uint8_t>(), o.ld, n, S, o.h.tsamp, nu,
+                               nudot, tp, cp, sp));
       break;
     case SAMPLE_U16:
-      launch_cube_fold(grid, B, st, o.samples.as<uint16_t>(), o.ld, n, S, o.h.tsamp, nu, nudot,
-                       w.tau.as<double>(), w.cube.as<float>(), w.chsum.as<double>());
+      PSR_TRY(launch_cube_fold(grid, B, st, o.samples.as<uint16_t>(), o.ld, n, S, o.h.tsamp, nu,
+                               nudot, tp, cp, sp));
       break;
     default:
-      launch_cube_fold(grid, B, st, o.samples.as<float>(), o.ld, n, S, o.h.tsamp, nu, nudot,
-                       w.tau.as<double>(), w.cube.as<float>(), w.chsum.as<double>());
+      PSR_TRY(launch_cube_fold(grid, B, st, o.samples.as<float>(), o.ld, n, S, o.h.tsamp, nu,
+                               nudot, tp, cp, sp));
   }
   PSR_CUDA(cudaGetLastError());
   PSR_TRY(w.R.ensure(w.rows * (uint64_t)(B / 2) * sizeof(float2)));
