@@ -629,6 +629,19 @@ struct FftArgs {
   cudaStream_t st;
 };
 
+// SM count of the current device (cached per device).
+int sm_count(int &n) {
+  static thread_local int dev_cached = -1, n_cached = 0;
+  int dev = 0;
+  PSR_CUDA(cudaGetDevice(&dev));
+  if (dev != dev_cached) {
+    PSR_CUDA(cudaDeviceGetAttribute(&n_cached, cudaDevAttrMultiProcessorCount, dev));
+    dev_cached = dev;
+  }
+  n = n_cached;
+  return PSR_OK;
+}
+
 template <int M>
 int run_small(const FftArgs &a) {
   const size_t smem = (size_t)(M + lay_slots<M, 1>()) * sizeof(float2);
@@ -648,12 +661,8 @@ int run_four_step(const FftArgs &a) {
     PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
     const uint32_t ngroups = (uint32_t)(M2 / C) * (uint32_t)a.ntrials;
-    static int nsm = 0;
-    if (nsm == 0) {
-      int dev = 0;
-      PSR_CUDA(cudaGetDevice(&dev));
-      PSR_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int nsm = 0;
+    PSR_TRY(sm_count(nsm));
     const uint32_t grid = std::min<uint32_t>(ngroups, 2u * (uint32_t)nsm);
     k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(
         a.series, a.lds, a.len, a.means, a.Q, a.lq, a.N, a.tw1, a.work, ngroups);
@@ -666,12 +675,8 @@ int run_four_step(const FftArgs &a) {
                                   (int)smem));
     const uint32_t ng = 1 + ((uint32_t)M1 / 2 - 1 + C / 2 - 1) / (C / 2);
     dim3 grid(ng, (unsigned)a.ntrials);
-    static int nsm2 = 0;
-    if (nsm2 == 0) {
-      int dev = 0;
-      PSR_CUDA(cudaGetDevice(&dev));
-      PSR_CUDA(cudaDeviceGetAttribute(&nsm2, cudaDevAttrMultiProcessorCount, dev));
-    }
+    int nsm2 = 0;
+    PSR_TRY(sm_count(nsm2));
     k_fft_pass2<M1, M2><<<grid, threads_for(M2, C), smem, a.st>>>(
         a.work, a.Q, a.lq, a.N, a.power, a.ldp, a.psum, ng, 2u * (uint32_t)nsm2);
     PSR_CUDA(cudaGetLastError());
