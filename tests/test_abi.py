@@ -121,3 +121,12 @@ def test_max_harmonics_levels(L, oracle):
     for bad in (1, 8, 24, 64):
         with pytest.raises(InvalidArgument, match="valid config"):
             search.periodicity(x, 1e-3, 0.0, search.Config(max_harmonics=bad))
+
+
+def test_batch_and_stats_reject_bad_arguments(L):
+    """Argument checks that run before any device work."""
+    import ctypes as C
+    from pulsarsr_gb300 import _lib
+    assert L.psr_batch_set_chunking(None, C.c_uint64(0), C.c_uint64(16), C.c_uint64(0)) == \
+        _lib.PSR_EINVAL
+    assert L.psr_channel_stats(None, None, None) == _lib.PSR_EINVAL

@@ -136,7 +136,7 @@ def test_rfi_mask_matches_oracle(gpu, oracle, nbits, ns, block):
     assert m.channels  # the planted channels are found
 
 
-@pytest.mark.parametrize("case", ["c2", "u8_big_total", "u16", "dyadic_ties", "constant"])
+@pytest.mark.parametrize("case", ["c2", "u8_big_total", "u16", "dyadic_ties", "constant", "f32"])
 def test_channel_stats_bit_exact(gpu, oracle, case):
     """rfi::mask's channel means and variances: the device's parallel
     reference-order sums against the oracle's sequential loops, bit for bit.
@@ -150,13 +150,16 @@ def test_channel_stats_bit_exact(gpu, oracle, case):
         raw = synth.config_c2(2).to_bytes()
     else:
         nbits, ns = {"u8_big_total": (8, 1 << 20), "u16": (16, 60000),
-                     "dyadic_ties": (8, 1 << 16), "constant": (8, 5000)}[case]
+                     "dyadic_ties": (8, 1 << 16), "constant": (8, 5000),
+                     "f32": (32, 40000)}[case]
         o = synth.Observation(nchans=24, nbits=nbits, nsamples=ns, tsamp=64e-6, fch1=1450.,
                               foff=-1.0, seed=11, noise_mean=100., noise_sigma=10.)
         if case == "u8_big_total":
             x = np.clip(np.rint(rng.normal(200, 20, (ns, 24))), 0, 255)
         elif case == "u16":
             x = np.clip(np.rint(rng.normal(30000, 3000, (ns, 24))), 0, 65535)
+        elif case == "f32":
+            x = rng.normal(-3.0, 2.5, (ns, 24))
         elif case == "dyadic_ties":
             x = rng.integers(0, 4, (ns, 24)).astype(np.float64)
             x[:, 3] = 1.0
@@ -287,6 +290,12 @@ def test_periodicity_32_harmonics_matches_oracle(gpu, oracle, seed):
     c = search.periodicity(x, 64e-6, 3.0, search.Config(**cfg))
     o = oracle.periodicity(x, 64e-6, 3.0, **cfg)
     assert 32 in o["harmonics"].tolist()
+    assert c.tobytes() == o.tobytes()
+    # with birdies over a few of the comb's harmonics
+    f0 = float(o["frequency_hz"][np.argmax(o["harmonics"])])
+    cfg["birdies"] = [(f0 * 3, 0.5), (f0 * 17, 0.5)]
+    c = search.periodicity(x, 64e-6, 3.0, search.Config(**cfg))
+    o = oracle.periodicity(x, 64e-6, 3.0, **cfg)
     assert c.tobytes() == o.tobytes()
 
 
