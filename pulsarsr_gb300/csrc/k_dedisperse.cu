@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(DD_NT, 2)
                 uint64_t n, float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
                 uint64_t ntiles, int cc, int rowcap, int group, int accumulate, unsigned *err) {
   extern __shared__ __align__(128) uint8_t smem[];
-  uint8_t *bufs[2] = {smem, smem + (size_t)cc * rowcap};
+  const size_t bstride = (size_t)cc * rowcap;  // buffer b at smem + b * bstride
   __shared__ uint64_t bars[2];
   __shared__ StageInfo info[2];
   __shared__ unsigned long long wsum[DD_NT / 32][DB];
@@ -148,11 +148,11 @@ __global__ void __launch_bounds__(DD_NT, 2)
   }
   __syncthreads();
   if (tl < 32) {
-    issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, 0, cc, bufs[0], rowcap, &info[0],
-                &bars[0]);
+    issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, 0, cc, smem, rowcap,
+                    &info[0], &bars[0]);
     if (nchunks > 1)
-      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)cc, cc, bufs[1], rowcap,
-                  &info[1], &bars[1]);
+      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)cc, cc,
+                      smem + bstride, rowcap, &info[1], &bars[1]);
   }
 
   uint32_t acc[DB][8];
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(DD_NT, 2)
     }
     const uint64_t c0 = (uint64_t)k * cc;
     const int rows = (int)min((uint64_t)cc, (uint64_t)(nch - c0));
-    const uint8_t *buf = bufs[b];
+    const uint8_t *buf = smem + b * bstride;
     for (int r = 0; r < rows; ++r) {
       const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
       const int *offs = info[b].off[r];
@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(DD_NT, 2)
     __syncthreads();  // every thread is done reading buffer b
     if (tl < 32 && k + 2 < nchunks) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc, cc,
-                  bufs[b], rowcap, &info[b], &bars[b]);
+      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc,
+                      cc, smem + b * bstride, rowcap, &info[b], &bars[b]);
     }
   }
   widen();
