@@ -57,7 +57,12 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   PSR_TRY(kept_count.ensure(ntrials * 4));
   PSR_TRY(err.ensure(16));
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 16, st));
-  nchunks = (ntrials + chunk - 1) / chunk;
+  const uint64_t tail = chunk >= 16 && ntrials > chunk ? chunk / 8 : 0;
+  cstart.clear();
+  for (uint64_t t = 0; t < ntrials - tail; t += chunk) cstart.push_back(t);
+  if (tail) cstart.push_back(ntrials - tail);
+  cstart.push_back(ntrials);
+  nchunks = cstart.size() - 1;
   PSR_TRY(chunk_overflow.ensure(nchunks * 4 + 16));
   if (!aux) PSR_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
   for (cudaEvent_t *e : {&ev_fft[0], &ev_fft[1], &ev_sel[0], &ev_sel[1]})
@@ -67,8 +72,8 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
 }
 
 int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st) {
-  const uint64_t t0 = ci * chunk;
-  const uint64_t nt = std::min(chunk, ntrials - t0);
+  const uint64_t t0 = cstart[ci];
+  const uint64_t nt = cstart[ci + 1] - t0;
   PSR_TRY(record(ST_DEDISP, true, st));
   PSR_TRY(launch_dedisperse_ex(o, delays.as<uint32_t>() + t0 * o.nch, nt, n, series.as<float>(),
                                ldo, parts.as<double>(), sums.as<double>(), means.as<float>(),

@@ -12,6 +12,10 @@ struct SearchEngine {
   uint64_t chunk = 0;
   uint64_t inner = 0;
   uint64_t ntrials = 0, n = 0, nch = 0, ldo = 0, ldp = 0, nparts = 0, nchunks = 0;
+  // Outer chunk ci covers trials [cstart[ci], cstart[ci + 1]).  A search of
+  // more than one chunk ends with a short chunk (chunk / 8 trials): the
+  // spectrum stage of the last chunk has nothing left to overlap with.
+  std::vector<uint64_t> cstart;
   uint64_t max_spread = 0;
   uint32_t npsum = 0;
   FftPlan fft;
