@@ -383,30 +383,43 @@ __global__ void __launch_bounds__(SC_NT)
   const float t1lo = a.t1 > 0.0f ? a.t1 * (1.0f - 4e-7f) : -INFINITY;
   const float t4lo = 4.0f * (1.0f - 4e-7f);
   uint32_t *gq1 = g.q1 + trial * g.qcap, *gq2 = g.q2 + trial * g.qcap;
-  for (int i = threadIdx.x; i < SCG_OWN; i += SC_NT) {
+  // Four consecutive bins per thread (one 16-byte load, one block scale);
+  // the fourth bin's neighbour is the next group's first.
+  for (int i4 = threadIdx.x; i4 < SCG_OWN / 4; i4 += SC_NT) {
+    const int i = 4 * i4;
     const uint64_t k = kb0 + (uint64_t)i;
-    if (k < a.first + 1 || k + 1 > a.end[0]) continue;  // k in [first+1, end_1 - 1]
-    const float e0 = raw[k] * inv_s[i >> 6];
-    bool pass1 = true;
-    if (i + 1 < SCG_OWN) pass1 = fmaxf(e0, raw[k + 1] * inv_s[(i + 1) >> 6]) >= t1lo;
-    if (pass1) {
-      const int slot = atomicAdd(&c1, 1);
-      if (slot < SCG_LQ) {
-        lq1[slot] = (uint16_t)i;
-      } else {
-        const unsigned gi = atomicAdd(&g.n1[trial], 1u);
-        if (gi < g.qcap) gq1[gi] = (uint32_t)k;
-        else atomicOr(a.overflow, 1u);
+    if (k + 3 < a.first + 1 || k + 1 > a.end[0]) continue;  // no bin in [first+1, end_1 - 1]
+    const float4 r4 = *reinterpret_cast<const float4 *>(raw + k);
+    const float inv = inv_s[i >> 6];
+    const float e[4] = {r4.x * inv, r4.y * inv, r4.z * inv, r4.w * inv};
+    const float nx =
+        (i + 4 < SCG_OWN && k + 4 <= a.end[0]) ? raw[k + 4] * inv_s[(i + 4) >> 6] : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint64_t kj = k + (uint64_t)j;
+      if (kj < a.first + 1 || kj + 1 > a.end[0]) continue;
+      const float e0 = e[j];
+      bool pass1 = true;
+      if (i + j + 1 < SCG_OWN) pass1 = fmaxf(e0, j < 3 ? e[j + 1] : nx) >= t1lo;
+      if (pass1) {
+        const int slot = atomicAdd(&c1, 1);
+        if (slot < SCG_LQ) {
+          lq1[slot] = (uint16_t)(i + j);
+        } else {
+          const unsigned gi = atomicAdd(&g.n1[trial], 1u);
+          if (gi < g.qcap) gq1[gi] = (uint32_t)kj;
+          else atomicOr(a.overflow, 1u);
+        }
       }
-    }
-    if (e0 >= t4lo) {
-      const int slot = atomicAdd(&c2, 1);
-      if (slot < SCG_LQ) {
-        lq2[slot] = (uint16_t)i;
-      } else {
-        const unsigned gi = atomicAdd(&g.n2[trial], 1u);
-        if (gi < g.qcap) gq2[gi] = (uint32_t)k;
-        else atomicOr(a.overflow, 1u);
+      if (e0 >= t4lo) {
+        const int slot = atomicAdd(&c2, 1);
+        if (slot < SCG_LQ) {
+          lq2[slot] = (uint16_t)(i + j);
+        } else {
+          const unsigned gi = atomicAdd(&g.n2[trial], 1u);
+          if (gi < g.qcap) gq2[gi] = (uint32_t)kj;
+          else atomicOr(a.overflow, 1u);
+        }
       }
     }
   }
