@@ -266,24 +266,35 @@ __global__ void __launch_bounds__(SC_NT)
     if (lane == 0) floor_s = (float)(s / (double)plen * 1e-6);
   }
   if (threadIdx.x == 0) c1 = c2 = 0;
-  // Stage the bins of all chunks (coalesced, 16 loads in flight per thread);
+  // Stage the bins of all chunks (16-byte loads, four in flight per thread);
   // out-of-range chunks and bin 0 hold the sentinel 0xffffffff.
   constexpr int NV = SC_CH * 64;
-  const long long e_first = c_first * 64;
-  for (int base = 0; base < NV; base += 16 * SC_NT) {
-    uint32_t v[16];
+  constexpr int NV4 = NV / 4;
+  static_assert(NV4 % (4 * SC_NT) == 0, "staging loop covers the chunks exactly");
+  const long long e_first = c_first * 64;  // a multiple of 4: 16-byte aligned loads
+  for (int base = 0; base < NV4; base += 4 * SC_NT) {
+    uint4 v[4];
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int i = base + u * SC_NT + (int)threadIdx.x;
-      const long long e = e_first + i;
-      v[u] = (i < NV && e >= 1 && e < (long long)plen) ? fbits(raw[e]) : 0xffffffffu;
+    for (int u = 0; u < 4; ++u) {
+      const long long e = e_first + 4ll * (base + u * SC_NT + (int)threadIdx.x);
+      if (e >= 1 && e + 3 < (long long)plen) {
+        v[u] = *reinterpret_cast<const uint4 *>(raw + e);
+      } else {
+        uint32_t t[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          t[j] = (e + j >= 1 && e + j < (long long)plen) ? fbits(raw[e + j]) : 0xffffffffu;
+        v[u] = make_uint4(t[0], t[1], t[2], t[3]);
+      }
     }
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int i = base + u * SC_NT + (int)threadIdx.x;
-      if (i < NV) {
-        ch[(i >> 6) * SC_STRIDE + (i & 63)] = v[u];
-      }
+    for (int u = 0; u < 4; ++u) {
+      const int i = 4 * (base + u * SC_NT + (int)threadIdx.x);
+      uint32_t *dst = ch + (i >> 6) * SC_STRIDE + (i & 63);  // one chunk row
+      dst[0] = v[u].x;
+      dst[1] = v[u].y;
+      dst[2] = v[u].z;
+      dst[3] = v[u].w;
     }
   }
   __syncthreads();
@@ -382,6 +393,7 @@ __global__ void __launch_bounds__(SC_NT)
   const uint64_t kb0 = (uint64_t)b0 * 64;
   const float t1lo = a.t1 > 0.0f ? a.t1 * (1.0f - 4e-7f) : -INFINITY;
   const float t4lo = 4.0f * (1.0f - 4e-7f);
+  const float tmin = fminf(t1lo, t4lo);
   uint32_t *gq1 = g.q1 + trial * g.qcap, *gq2 = g.q2 + trial * g.qcap;
   // Four consecutive bins per thread (one 16-byte load, one block scale);
   // the fourth bin's neighbour is the next group's first.
@@ -394,6 +406,11 @@ __global__ void __launch_bounds__(SC_NT)
     const float e[4] = {r4.x * inv, r4.y * inv, r4.z * inv, r4.w * inv};
     const float nx =
         (i + 4 < SCG_OWN && k + 4 <= a.end[0]) ? raw[k + 4] * inv_s[(i + 4) >> 6] : 0.0f;
+    // Most groups pass neither gate: every estimate (and the neighbour's)
+    // below both thresholds queues nothing (the CTA's last group excepted).
+    if (i + 4 < SCG_OWN &&
+        fmaxf(fmaxf(fmaxf(e[0], e[1]), fmaxf(e[2], e[3])), nx) < tmin)
+      continue;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const uint64_t kj = k + (uint64_t)j;
