@@ -70,6 +70,17 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 w) {
 __device__ __forceinline__ float2 mul_mi(float2 d) { return make_float2(d.y, -d.x); }
 
 // W_N^x for x in [0, N) from the quarter table (lq = log2(N/4)).
+// 8-byte asynchronous global -> shared copy (no registers held while in flight).
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 __device__ __forceinline__ float2 twN(const float2 *__restrict__ Q, uint32_t x, int lq) {
   const uint32_t q = x >> lq, r = x & ((1u << lq) - 1u);
   const float2 v = __ldg(&Q[r]);
@@ -507,27 +518,23 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
       }
     }
   }
-  build_wl<M2>(Wl, N, Q, lq);
   const int total = M2 * ncols;
   auto row_of = [&](int ci) -> uint32_t {
     if (g == 0) return ci == 0 ? 0u : (uint32_t)(M1 / 2);
     return ci < h ? kb + (uint32_t)ci : (uint32_t)M1 - (kb + (uint32_t)(ci - h));
   };
   if constexpr (C == 16 && NT == M2) {
-    // thread t loads position t of every row; slot lay<16>(t, ci) = 17 t + ci
+    // thread t copies position t of every row to slot lay<16>(t, ci) = 17 t + ci;
+    // all copies are in flight while the row twiddles are built
     const float2 *src = in + threadIdx.x;
     float2 *dst = sm + 17 * threadIdx.x;
 #pragma unroll
-    for (int c0 = 0; c0 < C; c0 += LB) {
-      float2 v[LB];
-#pragma unroll
-      for (int u = 0; u < LB; ++u)
-        v[u] = c0 + u < ncols ? src[(uint64_t)row_of(c0 + u) * M2] : make_float2(0.0f, 0.0f);
-#pragma unroll
-      for (int u = 0; u < LB; ++u)
-        if (c0 + u < ncols) dst[c0 + u] = v[u];
-    }
+    for (int ci = 0; ci < C; ++ci)
+      if (ci < ncols) cp_async8(dst + ci, src + (uint64_t)row_of(ci) * M2);
+    build_wl<M2>(Wl, N, Q, lq);
+    cp_async_wait_all();
   } else {
+    build_wl<M2>(Wl, N, Q, lq);
 #pragma unroll 1
     for (int base = 0; base < total; base += LB * NT) {
       float2 v[LB];
