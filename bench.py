@@ -309,13 +309,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/f32",
         "data": "synthetic (seeded numpy generator, GBT L-band tutorial shape)",
-        "config": {"workload": f"{'GBT-shaped' if args.config == 'c2' else 'config-1'} search: "
-                               f"{obs.nchans} ch x {obs.nbits}-bit x {obs.nsamples} samples, "
-                               f"tsamp {obs.tsamp * 1e6:.0f} us, {len(trials)} DM trials, "
-                               f"discovery {discovery}, rFFT {N}, RFI on",
-                   "trials": len(trials), "discovery_samples": discovery,
-                   "l2": "flushed (512 MB memset) before every timed step",
-                   "parallelism": f"replicas x{world}"},
+        "config": search_config(args, obs, trials, discovery, world),
         "e2e": {"value": round(world * units / e2e_s, 1), "unit": UNIT,
                 "h2d_bytes_per_step": int(payload.nbytes), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -366,6 +360,18 @@ def cpu_baseline(obs, raw, trials, discovery, args, sample_trials=None):
                       f"({full:.1f}s)"}
 
 
+def search_config(args, obs, trials, discovery, world):
+    """The `config` object of the search lines (both arms)."""
+    N = 2 * (1 << (discovery - 1).bit_length())
+    return {"workload": f"{'GBT-shaped' if args.config == 'c2' else 'config-1'} search: "
+                        f"{obs.nchans} ch x {obs.nbits}-bit x {obs.nsamples} samples, "
+                        f"tsamp {obs.tsamp * 1e6:.0f} us, {len(trials)} DM trials, "
+                        f"discovery {discovery}, rFFT {N}, RFI on",
+            "trials": len(trials), "discovery_samples": discovery,
+            "l2": "flushed (512 MB memset) before every timed step",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -383,9 +389,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": UNIT,
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32/f64 (CPU)", "data": "synthetic",
-            "config": {"workload": "same observation and DM plan as the GPU arm",
-                       "trials": len(trials), "discovery_samples": discovery},
+            "vs_baseline": None, "dtype": "f32/f64 (CPU)",
+            "data": "synthetic (seeded numpy generator, GBT L-band tutorial shape)",
+            "config": search_config(args, obs, trials, discovery,
+                                    int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": info,
             "e2e": {"value": round(v, 1), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
