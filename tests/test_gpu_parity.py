@@ -178,12 +178,15 @@ def test_channel_stats_bit_exact(gpu, oracle, case):
 
 
 # ------------------------------------------------------------ dedisperse
-@pytest.mark.parametrize("nbits", [4, 8, 32])
+NOISE = {1: (0.5, 0.5), 2: (1.5, 1.0), 4: (8., 2.)}  # (mean, sigma) by bit depth; else (100, 10)
+
+
+@pytest.mark.parametrize("nbits", [1, 2, 4, 8, 16, 32])
 def test_dedisperse_matches_oracle(gpu, oracle, nbits):
     from pulsarsr_gb300 import dedisperse, fbank, synth
+    mean, sigma = NOISE.get(nbits, (100., 10.))
     o = synth.Observation(nchans=96, nbits=nbits, nsamples=60000, tsamp=72e-6, fch1=1448.,
-                          foff=-1.0, seed=7, noise_mean=8. if nbits == 4 else 100.,
-                          noise_sigma=2. if nbits == 4 else 10.,
+                          foff=-1.0, seed=7, noise_mean=mean, noise_sigma=sigma,
                           pulsars=[synth.Pulsar(0.0046214, 62.4, 0.03, 0.5)])
     raw = o.to_bytes()
     fb = fbank.decode(raw)
@@ -221,6 +224,34 @@ def test_dedisperse_many_channels_8bit_groups(gpu, oracle):
     for i in range(0, len(trials), 7):
         ref = oracle.apply(d, oracle.delays(freqs, o.tsamp, trials[i]), n)
         assert out[i].tobytes() == ref.tobytes(), i
+
+
+@pytest.mark.parametrize("nbits", [4, 8])
+def test_dedisperse_edge_shapes(gpu, oracle, nbits):
+    """Unordered and repeated trial DMs in one launch, outputs of 2 samples and
+    of one 4096-sample tile +- 1, and a single-channel observation."""
+    from pulsarsr_gb300 import dedisperse, fbank, synth
+    mean, sigma = NOISE.get(nbits, (100., 10.))
+    o = synth.Observation(nchans=96, nbits=nbits, nsamples=12000, tsamp=72e-6, fch1=1448.,
+                          foff=-1.0, seed=21, noise_mean=mean, noise_sigma=sigma)
+    raw = o.to_bytes()
+    fb = fbank.decode(raw)
+    _, d = oracle.decode(raw)
+    freqs = fb.header.frequencies()
+    trials = np.array([300.0, 0.0, 150.0, 150.0, 7.25, 299.0, 0.5])
+    for n in (2, 4095, 4096, 4097):
+        out = dedisperse.apply_trials(fb, trials, n)
+        for i, dm in enumerate(trials):
+            ref = oracle.apply(d, oracle.delays(freqs, o.tsamp, dm), n)
+            assert out[i].tobytes() == ref.tobytes(), (n, i)
+    o1 = synth.Observation(nchans=1, nbits=nbits, nsamples=5000, tsamp=72e-6, fch1=1448.,
+                           foff=-1.0, seed=22, noise_mean=mean, noise_sigma=sigma)
+    raw1 = o1.to_bytes()
+    fb1 = fbank.decode(raw1)
+    _, d1 = oracle.decode(raw1)
+    out = dedisperse.apply_trials(fb1, np.array([0.0, 100.0]), 4999)
+    for i in range(2):
+        assert out[i].tobytes() == d1[0, :4999].astype(np.float32).tobytes(), i
 
 
 def test_dedisperse_errors(gpu):
