@@ -111,6 +111,17 @@ __device__ __forceinline__ double inv_sqrt_div(double x, int hi) {
   }
 }
 
+// Whether (sum - h) / sqrt(h) can reach thr, without the f64 division where
+// it clearly cannot: x * RN(1/sqrt(h)) is within 2^-50 (relative) of the
+// correctly rounded quotient, so below thr by more than |thr| 2^-49 it is
+// below for certain.  Levels with h = 1, 4, 16 scale exactly: always true.
+__device__ __forceinline__ bool may_reach(double x, int hi, double thr) {
+  if ((hi & 1) == 0) return true;
+  constexpr double r1 = 0.7071067811865476;  // RN(1/sqrt(2)); / 2 and / 4 are exact
+  const double r = hi == 1 ? r1 : hi == 3 ? r1 * 0.5 : r1 * 0.25;
+  return __dmul_rn(x, r) >= thr - fabs(thr) * 0x1p-49;
+}
+
 // Full score of harmonic level hi (h = 1 << hi) at bin k (k in [first, end]).
 __device__ double score_at(const HarmArgs &a, const float *raw, const float *sc, uint64_t k,
                            int hi) {
@@ -210,7 +221,9 @@ __device__ void harm_item(const HarmArgs &a, uint64_t trial, const float *raw, c
     // harmonics j = h/2+1 .. h (v[j-1]); for h = 2 also j = 1
 #pragma unroll
     for (int j = (hi == 1 ? 0 : h / 2); j < h; ++j) sum = __dadd_rn(sum, (double)v[j]);
-    const double s = inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
+    const double xs = __dsub_rn(sum, (double)h);
+    if (!may_reach(xs, hi, a.threshold)) continue;
+    const double s = inv_sqrt_div(xs, hi);
     if (s >= a.threshold) {
       const double sm = score_at(a, raw, sc, k - 1, hi);
       const double sp = score_at(a, raw, sc, k + 1, hi);
