@@ -130,3 +130,31 @@ def test_batch_and_stats_reject_bad_arguments(L):
     assert L.psr_batch_set_chunking(None, C.c_uint64(0), C.c_uint64(16), C.c_uint64(0)) == \
         _lib.PSR_EINVAL
     assert L.psr_channel_stats(None, None, None) == _lib.PSR_EINVAL
+
+
+def test_harmonic_division_gate_bound():
+    """The harmonic-item kernel skips the correctly rounded division
+    (sum - h) / RN(sqrt(h)) for h = 2, 8, 32 when x * RN(1/sqrt(2)) / 2^k is
+    below thr - |thr| 2^-49.  Check on IEEE doubles that such a quotient is
+    always below thr, and that the gap between the two is within 2^-50."""
+    rng = np.random.default_rng(3)
+    r1 = 0.7071067811865476
+    for hi, c in ((1, 1.4142135623730951), (3, 2.8284271247461903), (5, 5.656854249492381)):
+        assert c == np.sqrt(np.float64(1 << hi))
+        r = r1 * 2.0 ** (-(hi >> 1))
+        x = np.concatenate([rng.uniform(-50, 400, 400000),
+                            np.exp(rng.uniform(-700, 700, 200000)),
+                            -np.exp(rng.uniform(-700, 700, 50000))])
+        q = x / c
+        a = x * r
+        nz = q != 0
+        assert np.all(np.abs(a[nz] - q[nz]) <= np.abs(q[nz]) * 2.0 ** -50)
+        for thr in (8.0, 0.5, 1e-300, -3.0, 0.0):
+            skip = a < thr - abs(thr) * 2.0 ** -49
+            assert not np.any(q[skip] >= thr), (hi, thr)
+        # quotients straddling the threshold: x chosen so that x / c is within
+        # a few ulps of 8
+        xs = 8.0 * c * (1.0 + rng.integers(-40, 41, 100000) * 2.0 ** -52)
+        qs, as_ = xs / c, xs * r
+        skip = as_ < 8.0 - 8.0 * 2.0 ** -49
+        assert not np.any(qs[skip] >= 8.0)
