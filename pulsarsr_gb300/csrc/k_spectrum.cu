@@ -26,7 +26,7 @@
 namespace psr {
 namespace {
 
-constexpr int SC_NT = 128;               // threads per CTA, one chunk sort each
+constexpr int SC_NT = 256;               // threads per CTA, one chunk sort each
 constexpr int SC_CH = SC_NT;             // chunks staged per CTA
 constexpr int SC_G = SC_CH - 4;          // blocks per CTA (chunks b-2 .. b+2 each)
 constexpr float LN2F = 0.693147180559945309f;
