@@ -314,39 +314,126 @@ __global__ void __launch_bounds__(PC_NT)
 // t1)... + t_{n-1}), bit for bit, in parallel.  While s stays in one binade
 // [2^e, 2^(e+1)) every representable value is a multiple of u = 2^(e-23), so
 // s = K u (2^23 <= K < 2^24) and RN(s + t) = (K + inc(t)) u with inc(t) =
-// t/u rounded to nearest: the integer part of t/u plus one when its fraction
-// exceeds 1/2.  Only an exact half depends on the running K (ties to even),
-// and t >= 0 makes K monotone.  So a 512-term chunk whose increments contain
-// no exact half and keep K + sum(inc) < 2^24 adds sum(inc) at once; any other
-// chunk (a tie, a binade crossing, s still 0 or subnormal) is added term by
-// term in order.
+// t/u rounded to nearest: the integer part q of t/u plus one when its
+// fraction exceeds 1/2.  An exact half (a tie) rounds to even: inc = q +
+// ((K + q) mod 2), so it depends on the running K only through its parity,
+// and leaves K even.  The parity after a run of terms is therefore either
+// P xor c (no tie in the run) or a constant (after its last tie): these maps
+// compose, so a warp scans them across its lanes, and the total of a
+// 512-term chunk is a known sum plus, when it holds a tie, one bit that
+// depends on K's parity at the chunk's start.  t >= 0 makes K monotone; a
+// chunk whose total keeps K + total < 2^24 is added at once.  Chunks with a
+// binade crossing, a subnormal, infinite or NaN term, or s still 0 or
+// subnormal are added term by term in order.
 constexpr int ES_L = 512;  // terms per chunk, 16 per lane
 
-struct SeqInc {
-  unsigned long long sum = 0;
-  bool tie = false;
-  // t = mt 2^et (mt < 2^24); K's unit u = 2^(e - 23)
-  __device__ __forceinline__ void add(float t, int e) {
-    const uint32_t b = __float_as_uint(t);
-    const int be = (int)((b >> 23) & 0xff);
-    if (be == 0 || be == 255) {  // zero adds nothing; subnormal, inf, NaN: in order
-      tie |= (b & 0x7fffffffu) != 0u;
-      return;
-    }
-    const uint32_t mt = (b & 0x7fffffu) | 0x800000u;
-    const int sh = (be - 150) - (e - 23);  // t / u = mt 2^sh
-    if (sh >= 0) {
-      // t >= 2^23 u > 2^e would leave the binade: count it as 2^40 units
-      // (any such term fails the K + sum < 2^24 test; no 64-bit overflow)
-      sum += sh >= 24 ? (1ull << 40) : ((unsigned long long)mt << sh);
-    } else if (sh > -25) {
-      const int r = -sh;
-      const uint32_t rem = mt & ((1u << r) - 1u), half = 1u << (r - 1);
-      sum += (unsigned long long)(mt >> r) + (rem > half ? 1ull : 0ull);
-      tie |= rem == half;
+// One term at unit u = 2^(e - 23): inc = q (+1 above the half), kind 0;
+// kind 1: an exact half (inc = q, the rounding bit comes from K's parity);
+// kind 2: a term the binade arithmetic does not cover.
+__device__ __forceinline__ int es_term(float t, int e, unsigned long long &inc) {
+  const uint32_t b = __float_as_uint(t);
+  const int be = (int)((b >> 23) & 0xff);
+  inc = 0;
+  if (be == 0 || be == 255) return (b & 0x7fffffffu) != 0u ? 2 : 0;  // +-0 adds nothing
+  const uint32_t mt = (b & 0x7fffffu) | 0x800000u;
+  const int sh = (be - 150) - (e - 23);  // t / u = mt 2^sh
+  if (sh >= 0) {
+    // t >= 2^23 u > 2^e would leave the binade: count it as 2^40 units
+    // (any such term fails the K + total < 2^24 test; no 64-bit overflow)
+    inc = sh >= 24 ? (1ull << 40) : ((unsigned long long)mt << sh);
+    return 0;
+  }
+  if (sh <= -25) return 0;  // below half a unit
+  const int r = -sh;
+  const uint32_t rem = mt & ((1u << r) - 1u), half = 1u << (r - 1);
+  inc = (unsigned long long)(mt >> r) + (rem > half ? 1ull : 0ull);
+  return rem == half ? 1 : 0;
+}
+
+// A warp's chunk at unit u: total(P0) = base + (tie ? P0 ^ bit : 0) for K's
+// parity P0 at the chunk's start; special: the chunk must go term by term.
+struct EsChunk {
+  unsigned long long base;
+  int bit;
+  bool tie, special;
+};
+
+template <int PER>
+__device__ __forceinline__ EsChunk es_chunk_warp(const float (&t)[PER], int e, int lane) {
+  // lane map: constant (after a tie in the lane) or xor
+  bool lc = false, lsp = false;
+  uint32_t lv = 0;
+  unsigned long long lsum = 0;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    unsigned long long inc;
+    const int k = es_term(t[j], e, inc);
+    lsum += inc;
+    if (k == 2) {
+      lsp = true;
+    } else if (k == 1) {
+      lc = true;
+      lv = 0;
+    } else {
+      lv ^= (uint32_t)inc & 1u;
     }
   }
-};
+  EsChunk c;
+  c.bit = 0;
+  c.tie = __any_sync(0xffffffffu, lc);
+  c.special = __any_sync(0xffffffffu, lsp);
+  if (!c.tie) {  // (most chunks) the total does not depend on K
+#pragma unroll
+    for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    c.base = lsum;
+    return c;
+  }
+  // inclusive scan of the maps, then the map from the chunk start to this lane
+  bool ic = lc;
+  uint32_t v = lv;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const bool pic = __shfl_up_sync(0xffffffffu, ic, o);
+    const uint32_t pv = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) {
+      v = ic ? v : (pv ^ v);
+      ic = ic || pic;
+    }
+  }
+  bool conc = __shfl_up_sync(0xffffffffu, ic, 1);
+  uint32_t P = __shfl_up_sync(0xffffffffu, v, 1);
+  if (lane == 0) {
+    conc = false;
+    P = 0;
+  }
+  // conc: P is K's parity; otherwise K's parity is P0 ^ P
+  unsigned long long base = 0;
+  int fb = -1;
+#pragma unroll
+  for (int j = 0; j < PER; ++j) {
+    unsigned long long inc;
+    const int k = es_term(t[j], e, inc);
+    if (k == 1) {
+      if (conc) {
+        base += inc + ((P + (uint32_t)inc) & 1u);
+      } else {  // the chunk's first tie: its bit waits for P0
+        base += inc;
+        fb = (int)((P ^ (uint32_t)inc) & 1u);
+      }
+      P = 0;
+      conc = true;
+    } else if (k == 0) {
+      base += inc;
+      P ^= (uint32_t)inc & 1u;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) base += __shfl_xor_sync(0xffffffffu, base, o);
+  const unsigned fm = __ballot_sync(0xffffffffu, fb >= 0);
+  c.base = base;
+  c.bit = fm ? __shfl_sync(0xffffffffu, fb, __ffs(fm) - 1) : 0;
+  return c;
+}
 
 // Lane l's 16 consecutive samples of chunk g of a step: one or two aligned
 // 16-byte loads (rows start 64-element aligned; only issued for samples below
@@ -378,13 +465,14 @@ constexpr int ES_G = 16;  // chunks per step = warps per CTA
 
 // One CTA of ES_G warps per channel: warp w holds chunk w of every step of
 // ES_G chunks (its samples prefetched a step ahead), computes the chunk's
-// increment sum at the binade of the running s, and the CTA adds the longest
-// tie-free run of chunks that stays in the binade; a chunk that cannot be is
-// added term by term, in order, by thread 0.  Returns s in every thread.
+// total at the binade of the running s, and the CTA adds the longest run of
+// chunks that stays in the binade (each tie's rounding bit from the running
+// parity); a chunk that cannot be is added term by term, in order, by
+// thread 0.  Returns s in every thread.
 struct EsShared {
   float stage[ES_L];
   unsigned long long tot[ES_G];
-  int tie[ES_G];
+  int tie[ES_G], bit[ES_G], special[ES_G];
   float s;
 };
 
@@ -416,18 +504,14 @@ __device__ float exact_seq_sum_cta(const T *__restrict__ row, uint64_t ns, Term 
       int g1 = g0;
       if (se > 0 && se < 255 && !(sb >> 31)) {
         const int e = se - 127;
-        SeqInc inc;
-        if (g >= g0) {
-#pragma unroll
-          for (int j = 0; j < PER; ++j) inc.add(t[j], e);
-        }
-        unsigned long long tot = inc.sum;
-#pragma unroll
-        for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-        const bool tie = __any_sync(0xffffffffu, inc.tie);
-        if (lane == 0) {
-          sh.tot[g] = tot;
-          sh.tie[g] = tie ? 1 : 0;
+        if (g >= g0) {  // warp-uniform
+          const EsChunk ck = es_chunk_warp<PER>(t, e, lane);
+          if (lane == 0) {
+            sh.tot[g] = ck.base;
+            sh.tie[g] = ck.tie ? 1 : 0;
+            sh.bit[g] = ck.bit;
+            sh.special[g] = ck.special ? 1 : 0;
+          }
         }
         __syncthreads();
         unsigned long long acc = (sb & 0x7fffffu) | 0x800000u;
@@ -435,10 +519,13 @@ __device__ float exact_seq_sum_cta(const T *__restrict__ row, uint64_t ns, Term 
 #pragma unroll
         for (int k = 0; k < ES_G; ++k) {
           if (k >= g0 && k < nchunk && !stop) {
-            if (sh.tie[k] || acc + sh.tot[k] >= (1ull << 24)) {
+            // a chunk with a tie: its first tie rounds by K's parity here
+            const uint32_t rb = ((uint32_t)acc ^ (uint32_t)sh.bit[k]) & 1u;
+            const unsigned long long tk = sh.tot[k] + (sh.tie[k] ? rb : 0u);
+            if (sh.special[k] || acc + tk >= (1ull << 24)) {
               stop = true;
             } else {
-              acc += sh.tot[k];
+              acc += tk;
               g1 = k + 1;
             }
           }
