@@ -341,7 +341,9 @@ def cpu_baseline(obs, raw, trials, discovery, args, sample_trials=None):
     from oracle import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    nsample = sample_trials or max(2 * threads, 32)
+    # about 10-30 core-seconds of trial work on a 16-core host (320 of the
+    # GBT-shaped plan's 2000 trials), never more than the plan
+    nsample = min(sample_trials or max(2 * threads, 320), len(trials))
     t0 = time.perf_counter()
     h, d = O.decode(raw)
     block = max(int(0.1 / obs.tsamp), 32)
