@@ -158,6 +158,11 @@ typedef struct {
 int psr_fb_synth(const psr_synth_config *cfg, psr_fb **out);
 /* Filterbank.data as f32, channel-major (nchans * nsamples values). */
 int psr_fb_download(const psr_fb *fb, float *out);
+/* Channels [c0, c0 + nchannels) of Filterbank.data (nchannels * nsamples
+ * values): a slice of `data` without copying the rest of a large survey
+ * observation to the host. */
+int psr_fb_download_channels(const psr_fb *fb, uint64_t c0, uint64_t nchannels,
+                             float *out);
 void psr_fb_free(psr_fb *fb);
 
 /* --------------------------------------------------------------- rfi */
@@ -189,9 +194,20 @@ int psr_plan(double dm_min, double dm_max, double step, double *out,
 int psr_dedisperse(const psr_fb *fb, const uint64_t *delays, int64_t length,
                    float *out, uint64_t cap, uint64_t *n_out);
 /* Many trials at once: out is [ntrials][length] (the CLI loop,
- * cli/src/main.rs:462-469, without the periodicity step). */
+ * cli/src/main.rs:462-469, without the periodicity step).  sums (may be
+ * NULL) receives each series' f64 sum, the value periodicity's mean divides
+ * (search/src/lib.rs:36): equal to the reference's sequential sum. */
 int psr_dedisperse_trials(const psr_fb *fb, const double *trials,
-                          uint64_t ntrials, uint64_t length, float *out);
+                          uint64_t ntrials, uint64_t length, float *out,
+                          double *sums);
+
+/* Test hook, no reference counterpart: one dedispersion launch (DM 0, up to
+ * 8192 samples) whose staged kernel arms its TMA barriers but issues no
+ * copy, so every bounded wait runs out after spin_limit polls (1..2^26) with
+ * nothing in flight.  Returns PSR_ETIMEOUT with the message a real give-up
+ * produces, PSR_EINVAL when the filterbank's samples do not take the staged
+ * kernel (f32, or sums that could pass 2^24).  The CUDA context stays usable. */
+int psr_test_stage_timeout(const psr_fb *fb, uint64_t spin_limit);
 
 /* ------------------------------------------------------------ search */
 /* The raw power spectrum of search::periodicity (search/src/lib.rs:35-44):
@@ -221,7 +237,15 @@ int psr_raw_power(const float *series, uint64_t len, float *out);
  *   - Every call on a device shares the one array (series, work, spectrum and
  *     twiddle tables, which are kept between calls of the same FFT size), so
  *     calls that overlap in time on one device, from several threads or
- *     streams, race and corrupt each other's results: serialise them. */
+ *     streams, race and corrupt each other's results: serialise them.
+ *   - The array's address and the kept tables belong to the device's primary
+ *     context (the one the CUDA runtime uses).  After cudaDeviceReset, or
+ *     with another driver-API context current on that device, they are stale:
+ *     do not call this entry point in either situation.
+ *   - The array is reserved when the module is loaded.  With lazy module
+ *     loading (CUDA_MODULE_LOADING=LAZY, the default since CUDA 12.2) that
+ *     is the first call of this entry point on a device; with eager loading
+ *     every process that loads libpsr holds it on every device it uses. */
 #define PSR_RAW_POWER_NOALLOC_MAX_LEN (1u << 20)
 int psr_raw_power_noalloc(const float *series, uint64_t len, float *out, void *stream);
 /* search::periodicity (search/src/lib.rs:33-145) on one host series. */

@@ -7,9 +7,10 @@ has not been built (there is no CPU fallback).
 """
 from ._lib import (CapacityError, CudaError, DedisperseError, FormatError, InvalidArgument,
                    IoError, PsrError, lib)
+from ._lib import TimeoutError_ as WaitTimeout
 
 __all__ = ["PsrError", "FormatError", "IoError", "DedisperseError", "InvalidArgument",
-           "CudaError", "CapacityError", "lib", "version"]
+           "CudaError", "CapacityError", "WaitTimeout", "lib", "version"]
 
 
 def version() -> str:

@@ -297,18 +297,6 @@ int analyze_obs(const DeviceObs &o, const double *trials, uint64_t ntrials,
     e.chunk = 1;
     const double zero_dm = 0.0;
     PSR_TRY(e.prepare(o, &zero_dm, 1, discovery, zc, st));
-    if (o.kind == SAMPLE_F32) {
-      // The mean of periodicity() is a sequential f64 sum (search/src/lib.rs:36),
-      // which only integer samples make order-independent.
-      Dedisperser z;
-      PSR_TRY(z.run(o, zeros, 1, discovery, st));
-      std::vector<float> h(discovery);
-      PSR_CUDA(cudaMemcpyAsync(h.data(), z.row(0), discovery * 4, cudaMemcpyDeviceToHost, st));
-      PSR_CUDA(cudaStreamSynchronize(st));
-      double s = -0.0;
-      for (float v : h) s += (double)v;
-      e.host_sums.assign(1, s);
-    }
     PSR_TRY(e.enqueue(o, st));
     PSR_TRY(e.finish(o, st));
     uint64_t cnt = 0, total = 0;

@@ -556,25 +556,34 @@ int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples) {
   return PSR_OK;
 }
 
+int psr_fb_download_channels(const psr_fb *fb, uint64_t c0, uint64_t nchannels, float *out) {
+  if (!fb || !out || c0 > fb->o.nch || nchannels > fb->o.nch - c0) {
+    set_error("fb_download: null argument or channel range outside the filterbank");
+    return PSR_EINVAL;
+  }
+  const DeviceObs &o = fb->o;
+  if (nchannels == 0) return PSR_OK;
+  cudaStream_t st = fb->stream.s;
+  DevBuf tmp;
+  PSR_TRY(tmp.ensure(o.ns * nchannels * 4));
+  const unsigned g = (unsigned)((o.ns * nchannels + 255) / 256);
+  switch (o.kind) {
+    case SAMPLE_U8: k_to_f32<uint8_t><<<g, 256, 0, st>>>(o.samples.as<uint8_t>() + c0 * o.ld, o.ld, o.ns, nchannels, tmp.as<float>()); break;
+    case SAMPLE_U16: k_to_f32<uint16_t><<<g, 256, 0, st>>>(o.samples.as<uint16_t>() + c0 * o.ld, o.ld, o.ns, nchannels, tmp.as<float>()); break;
+    default: k_to_f32<float><<<g, 256, 0, st>>>(o.samples.as<float>() + c0 * o.ld, o.ld, o.ns, nchannels, tmp.as<float>());
+  }
+  PSR_CUDA(cudaGetLastError());
+  PSR_CUDA(cudaMemcpyAsync(out, tmp.p, o.ns * nchannels * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  return PSR_OK;
+}
+
 int psr_fb_download(const psr_fb *fb, float *out) {
   if (!fb || !out) {
     set_error("fb_download: null argument");
     return PSR_EINVAL;
   }
-  const DeviceObs &o = fb->o;
-  cudaStream_t st = fb->stream.s;
-  DevBuf tmp;
-  PSR_TRY(tmp.ensure(o.ns * o.nch * 4));
-  const unsigned g = (unsigned)((o.ns * o.nch + 255) / 256);
-  switch (o.kind) {
-    case SAMPLE_U8: k_to_f32<uint8_t><<<g, 256, 0, st>>>(o.samples.as<uint8_t>(), o.ld, o.ns, o.nch, tmp.as<float>()); break;
-    case SAMPLE_U16: k_to_f32<uint16_t><<<g, 256, 0, st>>>(o.samples.as<uint16_t>(), o.ld, o.ns, o.nch, tmp.as<float>()); break;
-    default: k_to_f32<float><<<g, 256, 0, st>>>(o.samples.as<float>(), o.ld, o.ns, o.nch, tmp.as<float>());
-  }
-  PSR_CUDA(cudaGetLastError());
-  PSR_CUDA(cudaMemcpyAsync(out, tmp.p, o.ns * o.nch * 4, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaStreamSynchronize(st));
-  return PSR_OK;
+  return psr_fb_download_channels(fb, 0, fb->o.nch, out);
 }
 
 void psr_fb_free(psr_fb *fb) { delete fb; }
@@ -704,7 +713,7 @@ int dedisperse_delays(const DeviceObs &o, const uint64_t *d, int64_t length, flo
   PSR_CUDA(cudaMemcpyAsync(dd.p, tab.data(), o.nch * 4, cudaMemcpyHostToDevice, st));
   const uint64_t ldo = series_ld_(n);
   PSR_TRY(ser.ensure(ldo * 4 + 256));
-  PSR_TRY(parts.ensure(((n + 1023) / 1024 + 8) * 8));
+  PSR_TRY(parts.ensure(dedisperse_part_count(o, n) * 8 + 8));
   PSR_TRY(sums.ensure(8));
   PSR_TRY(means.ensure(8));
   PSR_TRY(err.ensure(8));
@@ -728,7 +737,7 @@ int psr_dedisperse(const psr_fb *fb, const uint64_t *delays, int64_t length, flo
 }
 
 int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntrials,
-                          uint64_t length, float *out) {
+                          uint64_t length, float *out, double *sums_out) {
   if (!fb || !trials || !out || ntrials == 0) {
     set_error("dedisperse_trials: null argument or empty plan");
     return PSR_EINVAL;
@@ -757,6 +766,8 @@ int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntria
                                err.as<unsigned>(), st));
   PSR_CUDA(cudaMemcpy2DAsync(out, length * 4, ser.p, ldo * 4, length * 4, ntrials,
                              cudaMemcpyDeviceToHost, st));
+  if (sums_out)
+    PSR_CUDA(cudaMemcpyAsync(sums_out, sums.p, ntrials * 8, cudaMemcpyDeviceToHost, st));
   unsigned e = 0;
   PSR_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
@@ -765,6 +776,39 @@ int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntria
     return PSR_ETIMEOUT;
   }
   return PSR_OK;
+}
+
+int psr_test_stage_timeout(const psr_fb *fb, uint64_t spin_limit) {
+  if (!fb || spin_limit == 0 || spin_limit > (1ull << 26)) {
+    set_error("test_stage_timeout: a filterbank and a spin limit in [1, 2^26] are required");
+    return PSR_EINVAL;
+  }
+  const DeviceObs &o = fb->o;
+  cudaStream_t st = fb->stream.s;
+  const uint64_t n = std::min<uint64_t>(o.ns, 8192);
+  std::vector<uint32_t> tab(o.nch, 0);
+  DevBuf dd, ser, parts, sums, means, err;
+  PSR_TRY(dd.ensure(o.nch * 4));
+  PSR_CUDA(cudaMemcpyAsync(dd.p, tab.data(), o.nch * 4, cudaMemcpyHostToDevice, st));
+  const uint64_t ldo = series_ld(n);
+  PSR_TRY(ser.ensure(ldo * 4 + 256));
+  PSR_TRY(parts.ensure(dedisperse_part_count(o, n) * 8 + 8));
+  PSR_TRY(sums.ensure(8));
+  PSR_TRY(means.ensure(8));
+  PSR_TRY(err.ensure(8));
+  PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
+  PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), 1, n, ser.as<float>(), ldo,
+                               parts.as<double>(), sums.as<double>(), means.as<float>(), 0,
+                               err.as<unsigned>(), st, (long long)spin_limit, 1));
+  unsigned e = 0;
+  PSR_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  if (!e) {
+    set_error("test_stage_timeout: this filterbank does not take the staged kernel");
+    return PSR_EINVAL;
+  }
+  set_error("dedispersion: a bounded wait for a staged tile gave up");
+  return PSR_ETIMEOUT;
 }
 
 int psr_raw_power(const float *series, uint64_t len, float *out) {
@@ -783,13 +827,7 @@ int psr_raw_power(const float *series, uint64_t len, float *out) {
   PSR_TRY(power.ensure((p.M + 1 + 64) * 4));
   PSR_TRY(psum.ensure(p.pass2_ctas() * 8 + 8));
   PSR_CUDA(cudaMemcpyAsync(ser.p, series, len * 4, cudaMemcpyHostToDevice, s.s));
-  // Mean of the series (f64 sequential in the reference; exact for the
-  // integer-valued and bounded-range series the search produces).
-  double sum = -0.0;
-  for (uint64_t i = 0; i < len; ++i) sum += (double)series[i];
-  const float mean = (float)(sum / (double)len);
-  PSR_CUDA(cudaMemcpyAsync(sums.p, &mean, 4, cudaMemcpyHostToDevice, s.s));
-  PSR_CUDA(cudaStreamSynchronize(s.s));
+  PSR_TRY(launch_series_mean(ser.as<float>(), len, nullptr, sums.as<float>(), s.s));
   PSR_TRY(launch_raw_power_ex(p, ser.as<float>(), ldo, sums.as<float>(), 1, work.as<float2>(),
                               power.as<float>(), ((p.M + 1 + 63) / 64) * 64, psum.as<double>(),
                               s.s));
@@ -814,10 +852,6 @@ int psr_periodicity(const float *series, uint64_t len, double tsamp, double dm,
   e.chunk = 1;
   PSR_TRY(e.prepare(o, &dm, 1, len, to_spec(cfg, tsamp), s.s));
   // The engine computes delays from the DM; with one channel they are zero.
-  // The mean is the reference's sequential f64 sum (search/src/lib.rs:36).
-  double sum = -0.0;
-  for (uint64_t i = 0; i < len; ++i) sum += (double)series[i];
-  e.host_sums.assign(1, sum);
   PSR_TRY(e.enqueue(o, s.s));
   PSR_TRY(e.finish(o, s.s));
   uint64_t counts = 0;

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "psr_internal.h"
 
@@ -30,7 +31,7 @@ constexpr int DD_TT = DD_NT * DD_TPT;   // samples per tile (4096)
 constexpr int DD_DB = 8;                // trials per CTA (16-bit lanes only)
 constexpr int DD_DB8 = 6;               // trials per CTA with 8-bit lanes (registers)
 constexpr int DD_MAXCC = 32;            // rows per stage (one issuing lane each)
-constexpr long long DD_SPIN_LIMIT = 1ll << 26;
+constexpr long long DD_SPIN_LIMIT = 1ll << 26;  // try_wait polls before a wait gives up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -61,8 +62,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
 }
 // Bounded wait: false (and the error word set) if the phase never completes.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity,
-                                                  unsigned *err) {
-  for (long long i = 0; i < DD_SPIN_LIMIT; ++i)
+                                                  unsigned *err, long long limit) {
+  for (long long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   atomicOr(err, 1u);
   return false;
@@ -87,7 +88,8 @@ template <int DB>
 __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns,
                             uint64_t nch, uint64_t dstride, const uint32_t *__restrict__ delays,
                             uint64_t ntrials, uint64_t d0, uint64_t t0, uint64_t c0, int cc,
-                            uint8_t *buf, int rowcap, StageInfo *info, uint64_t *bar) {
+                            uint8_t *buf, int rowcap, StageInfo *info, uint64_t *bar,
+                            int arm_only) {
   const int lane = threadIdx.x & 31;
   unsigned bytes = 0;
   if (lane < cc && c0 + lane < nch) {
@@ -114,7 +116,10 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
       mbar_expect_tx(bar, bytes);
     }
     __syncwarp(__activemask());
-    if (bytes) bulk_g2s(buf + (size_t)lane * rowcap, s + c * ld + a, bytes, bar);
+    // arm_only (a test of the bounded wait): the barrier expects the bytes
+    // but no copy is issued, so its phase never completes and nothing is in
+    // flight when the CTA gives up.
+    if (bytes && !arm_only) bulk_g2s(buf + (size_t)lane * rowcap, s + c * ld + a, bytes, bar);
   }
   __syncwarp();
   if (lane == 0) mbar_arrive(bar);
@@ -129,7 +134,8 @@ __global__ void __launch_bounds__(DD_NT, 2)
     k_dedisp_u8(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
                 uint64_t dstride, const uint32_t *__restrict__ delays, uint64_t ntrials,
                 uint64_t n, float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
-                uint64_t ntiles, int cc, int rowcap, int group, int accumulate, unsigned *err) {
+                uint64_t ntiles, int cc, int rowcap, int group, int accumulate, unsigned *err,
+                long long spin_limit, int arm_only) {
   extern __shared__ __align__(128) uint8_t smem[];
   const size_t bstride = (size_t)cc * rowcap;  // buffer b at smem + b * bstride
   __shared__ uint64_t bars[2];
@@ -149,10 +155,10 @@ __global__ void __launch_bounds__(DD_NT, 2)
   __syncthreads();
   if (tl < 32) {
     issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, 0, cc, smem, rowcap,
-                    &info[0], &bars[0]);
+                    &info[0], &bars[0], arm_only);
     if (nchunks > 1)
       issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)cc, cc,
-                      smem + bstride, rowcap, &info[1], &bars[1]);
+                      smem + bstride, rowcap, &info[1], &bars[1], arm_only);
   }
 
   uint32_t acc[DB][8];
@@ -179,11 +185,16 @@ __global__ void __launch_bounds__(DD_NT, 2)
     }
   };
 
-  bool alive = true;
+  // Chunk k is staged in buffer k & 1, in that barrier's phase (k >> 1).
+  // A wait that gives up ends the whole CTA: the decision is made uniform
+  // by __syncthreads_or before any thread reads the buffer or reaches a
+  // later barrier, so no thread is left waiting on one that left.
+  int failed = -1;
   for (int k = 0; k < nchunks; ++k) {
     const int b = k & 1;
-    if (!mbar_wait_bounded(&bars[b], (unsigned)((k >> 1) & 1), err)) {
-      alive = false;
+    const bool ok = mbar_wait_bounded(&bars[b], (unsigned)((k >> 1) & 1), err, spin_limit);
+    if (__syncthreads_or(!ok)) {
+      failed = k;
       break;
     }
     const uint64_t c0 = (uint64_t)k * cc;
@@ -241,13 +252,20 @@ __global__ void __launch_bounds__(DD_NT, 2)
     if (tl < 32 && k + 2 < nchunks) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc,
-                      cc, smem + b * bstride, rowcap, &info[b], &bars[b]);
+                      cc, smem + b * bstride, rowcap, &info[b], &bars[b], arm_only);
     }
   }
   widen();
-  if (!alive) {
-    // Drain the other buffer's copy (bounded) before leaving.
-    if (tl == 0) mbar_wait_bounded(&bars[0], 0, err), mbar_wait_bounded(&bars[1], 0, err);
+  if (failed >= 0) {
+    // Before leaving, wait (bounded) for the copies still outstanding: chunk
+    // `failed` in its buffer and, if it was issued, chunk failed + 1 in the
+    // other, each in the phase it was issued in.
+    if (tl == 0) {
+      mbar_wait_bounded(&bars[failed & 1], (unsigned)((failed >> 1) & 1), err, spin_limit);
+      if (failed + 1 < nchunks)
+        mbar_wait_bounded(&bars[(failed + 1) & 1], (unsigned)(((failed + 1) >> 1) & 1), err,
+                          spin_limit);
+    }
     return;
   }
 
@@ -314,6 +332,8 @@ __global__ void __launch_bounds__(DG_NT)
                      float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
                      uint64_t ntiles) {
   __shared__ double wsum[DG_NT / 32][DG_DB];
+  __shared__ double wabs[DG_NT / 32][DG_DB];
+  __shared__ int wq[DG_NT / 32][DG_DB];
   const uint64_t t0 = (uint64_t)blockIdx.x * DG_TT;
   const uint64_t d0 = (uint64_t)blockIdx.y * DG_DB;
   float acc[DG_DB][DG_TPT];
@@ -335,9 +355,14 @@ __global__ void __launch_bounds__(DG_NT)
       }
     }
   }
+  // Non-integer samples: besides the sum, each tile records the sum of |x|
+  // and the finest binary quantum among its outputs, from which
+  // k_reduce_parts decides whether every partial sum is exact in f64.
+  constexpr bool kFloat = std::is_same<T, float>::value;
 #pragma unroll
   for (int d = 0; d < DG_DB; ++d) {
-    double local = 0.0;
+    double local = 0.0, labs = 0.0;
+    int lq = kNoQuantum;
     const uint64_t tr = d0 + d;
 #pragma unroll
     for (int i = 0; i < DG_TPT; ++i) {
@@ -345,40 +370,148 @@ __global__ void __launch_bounds__(DG_NT)
       if (t < n) {
         if (tr < ntrials) out[tr * ldo + t] = acc[d][i];
         local += (double)acc[d][i];
+        if (kFloat) {
+          labs += fabs((double)acc[d][i]);
+          lq = min(lq, quantum_exponent(acc[d][i]));
+        }
       }
     }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5][d] = local;
+    for (int o = 16; o; o >>= 1) {
+      local += __shfl_down_sync(0xffffffffu, local, o);
+      if (kFloat) {
+        labs += __shfl_down_sync(0xffffffffu, labs, o);
+        lq = min(lq, __shfl_down_sync(0xffffffffu, lq, o));
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+      wsum[threadIdx.x >> 5][d] = local;
+      if (kFloat) {
+        wabs[threadIdx.x >> 5][d] = labs;
+        wq[threadIdx.x >> 5][d] = lq;
+      }
+    }
   }
   __syncthreads();
   if (threadIdx.x < DG_DB && d0 + threadIdx.x < ntrials) {
-    double t = 0.0;
-    for (int w = 0; w < DG_NT / 32; ++w) t += wsum[w][threadIdx.x];
-    part[(d0 + threadIdx.x) * ntiles + blockIdx.x] = t;
+    double t = 0.0, a = 0.0;
+    int q = kNoQuantum;
+    for (int w = 0; w < DG_NT / 32; ++w) {
+      t += wsum[w][threadIdx.x];
+      if (kFloat) {
+        a += wabs[w][threadIdx.x];
+        q = min(q, wq[w][threadIdx.x]);
+      }
+    }
+    const uint64_t at = (d0 + threadIdx.x) * ntiles + blockIdx.x;
+    part[at] = t;
+    if (kFloat) {
+      part[ntrials * ntiles + at] = a;
+      part[2 * ntrials * ntiles + at] = (double)q;
+    }
   }
 }
 
-// Ordered reduction of per-tile partial sums into the series sum per trial
-// and the f32 mean the FFT subtracts (search/src/lib.rs:36-40).
+// Reduction of per-tile partial sums into the series sum per trial and the
+// f32 mean the FFT subtracts (search/src/lib.rs:36-40).  The reference's
+// mean is a sequential f64 sum starting from -0.0.  Integer samples make
+// every partial sum an exact integer below 2^53, so any order gives it.  For
+// f32 samples (check = true) the tiles also recorded sum |x| and the finest
+// quantum 2^q among the outputs: every partial sum, in any order, is then a
+// multiple of 2^q no larger than sum |x|, so it is exact in f64 while
+// sum |x| < 2^(53+q) (with a margin for the rounding of sum |x| itself).
+// Otherwise the thread re-adds the trial's series sequentially, in the
+// reference's order.
 __global__ void k_reduce_parts(const double *part, uint64_t ntiles, uint64_t ntrials,
-                               uint64_t n, double *sums, float *means) {
+                               uint64_t n, double *sums, float *means, const float *series,
+                               uint64_t ldo, int check) {
   uint64_t tr = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tr >= ntrials) return;
   double s = 0.0;
   for (uint64_t i = 0; i < ntiles; ++i) s += part[tr * ntiles + i];
+  if (check) {
+    double a = 0.0, q = (double)kNoQuantum;
+    for (uint64_t i = 0; i < ntiles; ++i) {
+      a += part[ntrials * ntiles + tr * ntiles + i];
+      q = fmin(q, part[2 * ntrials * ntiles + tr * ntiles + i]);
+    }
+    const bool exact = f64_sums_exact(a, (int)q);
+    if (!exact) {  // the reference's order: t = 0, 1, ..., from -0.0
+      const float *x = series + tr * ldo;
+      s = -0.0;
+      uint64_t t = 0;
+      for (; t + 4 <= n; t += 4) {  // rows start 256-byte aligned (ldo % 64 == 0)
+        const float4 v = *reinterpret_cast<const float4 *>(x + t);
+        s += (double)v.x;
+        s += (double)v.y;
+        s += (double)v.z;
+        s += (double)v.w;
+      }
+      for (; t < n; ++t) s += (double)x[t];
+    }
+  }
   sums[tr] = s;
   means[tr] = (float)(s / (double)n);
 }
 
+// One CTA: the series sum and mean of launch_series_mean.
+constexpr int SM_NT = 1024;
+__global__ void __launch_bounds__(SM_NT)
+    k_series_mean(const float *__restrict__ x, uint64_t n, double *sum_out, float *mean_out) {
+  __shared__ double ss[SM_NT / 32], sa[SM_NT / 32];
+  __shared__ int sq[SM_NT / 32];
+  double s = 0.0, a = 0.0;
+  int q = kNoQuantum;
+  for (uint64_t i = threadIdx.x; i < n; i += SM_NT) {
+    const float v = x[i];
+    s += (double)v;
+    a += fabs((double)v);
+    q = min(q, quantum_exponent(v));
+  }
+  for (int o = 16; o; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    q = min(q, __shfl_down_sync(0xffffffffu, q, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    ss[threadIdx.x >> 5] = s;
+    sa[threadIdx.x >> 5] = a;
+    sq[threadIdx.x >> 5] = q;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  s = 0.0;
+  a = 0.0;
+  q = kNoQuantum;
+  for (int w = 0; w < SM_NT / 32; ++w) {
+    s += ss[w];
+    a += sa[w];
+    q = min(q, sq[w]);
+  }
+  if (!f64_sums_exact(a, q)) {  // the reference's order, from -0.0
+    s = -0.0;
+    for (uint64_t i = 0; i < n; ++i) s += (double)x[i];
+  }
+  if (sum_out) *sum_out = s;
+  *mean_out = (float)(s / (double)n);
+}
+
 }  // namespace
+
+int launch_series_mean(const float *d_x, uint64_t n, double *d_sum, float *d_mean,
+                       cudaStream_t st) {
+  k_series_mean<<<1, SM_NT, 0, st>>>(d_x, n, d_sum, d_mean);
+  PSR_CUDA(cudaGetLastError());
+  return PSR_OK;
+}
 
 uint64_t series_ld(uint64_t n) { return ((n + 63) / 64) * 64; }
 
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part,
                          double *d_sums, float *d_means, uint64_t max_spread, unsigned *d_err,
-                         cudaStream_t st) {
+                         cudaStream_t st, long long spin_limit, int arm_only) {
+  const long long spin = spin_limit > 0 ? spin_limit : DD_SPIN_LIMIT;
   // Integer samples: channel groups small enough that a group's sum fits the
   // 16-bit lanes (nch * max <= 65535 when there is one group); the groups'
   // sums are added in f32, exact while the total stays below 2^24.
@@ -413,20 +546,19 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
           k_dedisp_u8<true, DD_DB8><<<grid, DD_NT, smem, st>>>(
               sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo, d_part, ntiles, ccg, rowcap,
-              group, acc, d_err);
+              group, acc, d_err, spin, arm_only);
         } else {
           dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
           PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false, DD_DB>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
           k_dedisp_u8<false, DD_DB><<<grid, DD_NT, smem, st>>>(
               sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo, d_part, ntiles, ccg, rowcap,
-              1, acc, d_err);
+              1, acc, d_err, spin, arm_only);
         }
         PSR_CUDA(cudaGetLastError());
       }
-      k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles,
-                                                                         ntrials, n, d_sums,
-                                                                         d_means);
+      k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
+          d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, 0);
       PSR_CUDA(cudaGetLastError());
       return PSR_OK;
     }
@@ -450,14 +582,16 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
                                                       ntiles);
   }
   PSR_CUDA(cudaGetLastError());
-  k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(d_part, ntiles, ntrials,
-                                                                     n, d_sums, d_means);
+  k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
+      d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, o.kind == SAMPLE_F32 ? 1 : 0);
   PSR_CUDA(cudaGetLastError());
   return PSR_OK;
 }
 
 uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n) {
-  return std::max((n + DD_TT - 1) / DD_TT, (n + DG_TT - 1) / DG_TT);
+  // f32 samples: sums, sums of |x| and quanta per tile
+  const uint64_t per = o.kind == SAMPLE_F32 ? 3 : 1;
+  return per * std::max((n + DD_TT - 1) / DD_TT, (n + DG_TT - 1) / DG_TT);
 }
 
 }  // namespace psr

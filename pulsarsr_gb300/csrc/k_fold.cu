@@ -125,35 +125,84 @@ __global__ void __launch_bounds__(MOM_NT)
 }
 
 // confirmation::measure (search/src/confirmation.rs:107-141): on/off sums.
-__global__ void k_measure(const float *__restrict__ x, uint64_t n, uint64_t offset, double tsamp,
-                          double period, uint64_t start_bin, uint64_t width_bins, uint64_t bins,
-                          double *__restrict__ part) {
-  __shared__ double red[6][32];
-  double acc[6] = {0, 0, 0, 0, 0, 0};  // n0, s0, q0, n1, s1, q1
+// Each warp covers 32 consecutive samples per step, so the on/off decision
+// of every sample also lands in `bits` (one word per 32 samples) for the
+// sequential pass.  part[block][8] = n0, s0, q0, n1, s1, q1, sum |v|, and the
+// finest quantum exponent among the values (as a double).
+constexpr int MEAS_NT = 256;
+__global__ void __launch_bounds__(MEAS_NT)
+    k_measure(const float *__restrict__ x, uint64_t n, uint64_t offset, double tsamp,
+              double period, uint64_t start_bin, uint64_t width_bins, uint64_t bins,
+              double *__restrict__ part, uint32_t *__restrict__ bits) {
+  __shared__ double red[7][MEAS_NT / 32];
+  __shared__ int redq[MEAS_NT / 32];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};  // n0, s0, q0, n1, s1, q1, sum |v|
+  int qm = kNoQuantum;
   const double dbins = (double)bins;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const double q = __ddiv_rn(__dmul_rn((double)(i + offset), tsamp), period);
-    uint64_t b = (uint64_t)__dmul_rn(__dsub_rn(q, trunc(q)), dbins);
-    if (b > bins - 1) b = bins - 1;
-    const int k = ((b + bins - start_bin) % bins) < width_bins ? 1 : 0;
-    const double v = (double)x[i];
-    acc[3 * k] += 1.0;
-    acc[3 * k + 1] = __dadd_rn(acc[3 * k + 1], v);
-    acc[3 * k + 2] = __dadd_rn(acc[3 * k + 2], __dmul_rn(v, v));
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
+       base += stride) {  // warp-uniform: base is a multiple of 32
+    const uint64_t i = base + lane;
+    int k = 0;
+    if (i < n) {
+      const double q = __ddiv_rn(__dmul_rn((double)(i + offset), tsamp), period);
+      uint64_t b = (uint64_t)__dmul_rn(__dsub_rn(q, trunc(q)), dbins);
+      if (b > bins - 1) b = bins - 1;
+      k = ((b + bins - start_bin) % bins) < width_bins ? 1 : 0;
+      const float xf = x[i];
+      const double v = (double)xf;
+      acc[3 * k] += 1.0;
+      acc[3 * k + 1] = __dadd_rn(acc[3 * k + 1], v);
+      acc[3 * k + 2] = __dadd_rn(acc[3 * k + 2], __dmul_rn(v, v));
+      acc[6] = __dadd_rn(acc[6], fabs(v));
+      qm = min(qm, quantum_exponent(xf));
+    }
+    const unsigned w = __ballot_sync(0xffffffffu, k);
+    if (lane == 0) bits[base >> 5] = w;
   }
 #pragma unroll
-  for (int j = 0; j < 6; ++j) {
+  for (int j = 0; j < 7; ++j) {
     double a = acc[j];
     for (int o = 16; o; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-    if ((threadIdx.x & 31) == 0) red[j][threadIdx.x >> 5] = a;
+    if (lane == 0) red[j][threadIdx.x >> 5] = a;
   }
+  for (int o = 16; o; o >>= 1) qm = min(qm, __shfl_down_sync(0xffffffffu, qm, o));
+  if (lane == 0) redq[threadIdx.x >> 5] = qm;
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < 7) {
     double a = 0.0;
-    for (int w = 0; w < (int)(blockDim.x / 32); ++w) a += red[threadIdx.x][w];
-    part[blockIdx.x * 6 + threadIdx.x] = a;
+    for (int w = 0; w < MEAS_NT / 32; ++w) a += red[threadIdx.x][w];
+    part[blockIdx.x * 8 + threadIdx.x] = a;
+  } else if (threadIdx.x == 7) {
+    int q = kNoQuantum;
+    for (int w = 0; w < MEAS_NT / 32; ++w) q = min(q, redq[w]);
+    part[blockIdx.x * 8 + 7] = (double)q;
   }
+}
+
+// The reference's own order for the on/off sums: one thread adds every
+// sample in turn (each class from 0.0), as measure() does.  Used when the
+// values make a reassociated f64 sum inexact (non-integer series).
+__global__ void k_measure_seq(const float *__restrict__ x, uint64_t n,
+                              const uint32_t *__restrict__ bits, double *__restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s0 = 0.0, q0 = 0.0, s1 = 0.0, q1 = 0.0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const double v = (double)x[i];
+    const double v2 = __dmul_rn(v, v);
+    if ((bits[i >> 5] >> (i & 31)) & 1u) {
+      s1 = __dadd_rn(s1, v);
+      q1 = __dadd_rn(q1, v2);
+    } else {
+      s0 = __dadd_rn(s0, v);
+      q0 = __dadd_rn(q0, v2);
+    }
+  }
+  out[0] = s0;
+  out[1] = q0;
+  out[2] = s1;
+  out[3] = q1;
 }
 
 int32_t key32(float x) {
@@ -298,19 +347,41 @@ int measure_device(const float *d_x, uint64_t n, uint64_t offset, double tsamp, 
                    uint64_t start_bin, uint64_t width_bins, uint64_t bins, psr_measurement *out,
                    cudaStream_t st) {
   const unsigned nb = (unsigned)std::min<uint64_t>((n + 1023) / 1024, 1024);
-  DevBuf part;
-  PSR_TRY(part.ensure((size_t)nb * 6 * 8));
-  k_measure<<<nb, 256, 0, st>>>(d_x, n, offset, tsamp, period, start_bin, width_bins, bins,
-                                part.as<double>());
+  DevBuf part, bits;
+  PSR_TRY(part.ensure((size_t)nb * 8 * 8 + 4 * 8));
+  PSR_TRY(bits.ensure(((n + 31) / 32 + 1) * 4));
+  k_measure<<<nb, MEAS_NT, 0, st>>>(d_x, n, offset, tsamp, period, start_bin, width_bins, bins,
+                                    part.as<double>(), bits.as<uint32_t>());
   PSR_CUDA(cudaGetLastError());
-  std::vector<double> h((size_t)nb * 6);
+  std::vector<double> h((size_t)nb * 8);
   PSR_CUDA(cudaMemcpyAsync(h.data(), part.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
-  double a[6] = {0, 0, 0, 0, 0, 0};
-  for (unsigned b = 0; b < nb; ++b)
-    for (int j = 0; j < 6; ++j) a[j] += h[(size_t)b * 6 + j];
+  double a[7] = {0, 0, 0, 0, 0, 0, 0};
+  int qmin = kNoQuantum;
+  for (unsigned b = 0; b < nb; ++b) {
+    for (int j = 0; j < 7; ++j) a[j] += h[(size_t)b * 8 + j];
+    qmin = std::min(qmin, (int)h[(size_t)b * 8 + 7]);
+  }
   const uint64_t cnt[2] = {(uint64_t)a[0], (uint64_t)a[3]};
-  const double sum[2] = {a[1], a[4]}, sum2[2] = {a[2], a[5]};
+  double sum[2] = {a[1], a[4]}, sum2[2] = {a[2], a[5]};
+  // Integer-valued series (sums of integer samples) give exact partial sums
+  // in any order.  Otherwise the order matters: sums of v are exact while
+  // sum |v| < 2^(53+q), sums of v^2 (multiples of 2^2q) while
+  // sum v^2 < 2^(53+2q); failing either, add in the reference's order.
+  const bool exact = f64_sums_exact(a[6], qmin) &&
+                     (qmin >= kNoQuantum || f64_sums_exact(a[2] + a[5], 2 * qmin));
+  if (!exact) {
+    double *d_seq = part.as<double>() + (size_t)nb * 8;
+    k_measure_seq<<<1, 32, 0, st>>>(d_x, n, bits.as<uint32_t>(), d_seq);
+    PSR_CUDA(cudaGetLastError());
+    double hq[4];
+    PSR_CUDA(cudaMemcpyAsync(hq, d_seq, sizeof(hq), cudaMemcpyDeviceToHost, st));
+    PSR_CUDA(cudaStreamSynchronize(st));
+    sum[0] = hq[0];
+    sum2[0] = hq[1];
+    sum[1] = hq[2];
+    sum2[1] = hq[3];
+  }
   out->on_samples = cnt[1];
   out->off_samples = cnt[0];
   if (cnt[0] < 2 || cnt[1] < 2) {

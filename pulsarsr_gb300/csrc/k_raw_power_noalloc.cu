@@ -178,15 +178,12 @@ extern "C" int psr_raw_power_noalloc(const float *series, uint64_t len, float *o
     PSR_TRY(write_tables(base, N, st));
     d->table_N = N;
   }
-  // Mean as psr_raw_power takes it: f64 sum in series order, divided, to f32.
-  double sum = -0.0;
-  for (uint64_t i = 0; i < len; ++i) sum += (double)series[i];
-  const float mean = (float)(sum / (double)len);
   float *d_ser = reinterpret_cast<float *>(base + NA_SER);
   float *d_mean = reinterpret_cast<float *>(base + NA_MEAN);
   float *d_pow = reinterpret_cast<float *>(base + NA_POW);
   PSR_CUDA(cudaMemcpyAsync(d_ser, series, len * 4, cudaMemcpyHostToDevice, st));
-  PSR_CUDA(cudaMemcpyAsync(d_mean, &mean, 4, cudaMemcpyHostToDevice, st));
+  // The mean as psr_raw_power takes it (one CTA, no scratch of its own).
+  PSR_TRY(launch_series_mean(d_ser, len, nullptr, d_mean, st));
   const uint64_t lds = series_ld(len), ldp = ((M + 1 + 63) / 64) * 64;
   PSR_TRY(launch_raw_power_tables(len, N, reinterpret_cast<const float2 *>(base + NA_Q),
                                   reinterpret_cast<const float2 *>(base + NA_TW1), d_ser, lds,

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include <string>
 #include <vector>
 
@@ -34,6 +36,27 @@ struct Status {
     int rc_ = (expr);                 \
     if (rc_ != PSR_OK) return rc_;    \
   } while (0)
+
+// Binary exponent of the finest quantum of a finite f32 value: x is an
+// integer multiple of 2^quantum_exponent(x); zero constrains nothing.  A
+// set of f32 values with finest quantum 2^q has every partial f64 sum exact,
+// in any order, while the sum of their magnitudes stays below 2^(53+q).
+constexpr int kNoQuantum = 1 << 20;
+#ifdef __CUDACC__
+__device__ __forceinline__ int quantum_exponent(float x) {
+  const uint32_t b = __float_as_uint(x) & 0x7fffffffu;
+  if (b == 0) return kNoQuantum;
+  const int e = (int)(b >> 23);
+  uint32_t m = b & 0x7fffffu;
+  if (e) m |= 0x800000u;
+  return (e ? e : 1) - 150 + (__ffs((int)m) - 1);
+}
+#endif
+// True when sums of magnitude at most `mag` over values whose finest quantum
+// is 2^q are exact in f64 whatever the order (mag itself rounded: a margin).
+__host__ __device__ inline bool f64_sums_exact(double mag, int q) {
+  return q >= kNoQuantum || mag * (1.0 + 0x1p-20) < ldexp(1.0, 53 + q);
+}
 
 // Owning device allocation (sized once, reused).
 struct DevBuf {
@@ -182,11 +205,21 @@ uint64_t series_ld(uint64_t n);
 int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
                      std::vector<uint32_t> &tab, uint64_t &max_spread, uint64_t &max_delay);
 // out[trial][t] (row stride ldo); sums[trial] = f64 series sum, means[trial] =
-// (f32)(sum / n), the value search::periodicity subtracts.
+// (f32)(sum / n), the value search::periodicity subtracts.  The staged
+// (packed integer) kernel's waits give up after spin_limit polls (0 = the
+// default limit) and set *d_err; arm_only = 1 arms its barriers without
+// issuing the copies, so every wait runs out (a test of that path).
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part, double *d_sums,
-                         float *d_means, uint64_t max_spread, unsigned *d_err, cudaStream_t st);
+                         float *d_means, uint64_t max_spread, unsigned *d_err, cudaStream_t st,
+                         long long spin_limit = 0, int arm_only = 0);
 uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
+// The f64 sum of a device series and the f32 mean search::periodicity
+// subtracts (search/src/lib.rs:36), bit-identical to the reference's
+// sequential sum: added in parallel where that is exact, else in order.  One
+// CTA; d_sum may be null.
+int launch_series_mean(const float *d_x, uint64_t n, double *d_sum, float *d_mean,
+                       cudaStream_t st);
 int launch_raw_power_ex(const FftPlan &p, const float *d_series, uint64_t lds,
                         const float *d_means, uint64_t ntrials, float2 *d_work, float *d_power,
                         uint64_t ldp, double *d_psum, cudaStream_t st);

@@ -79,13 +79,6 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
                                ldo, parts.as<double>(), sums.as<double>(), means.as<float>(),
                                max_spread, err.as<unsigned>(), st));
   PSR_TRY(record(ST_DEDISP, false, st));
-  if (!host_sums.empty()) {
-    host_means.resize(host_sums.size());
-    for (size_t i = 0; i < host_sums.size(); ++i)
-      host_means[i] = (float)(host_sums[i] / (double)n);
-    PSR_CUDA(cudaMemcpyAsync(means.p, host_means.data() + t0, nt * 4, cudaMemcpyHostToDevice,
-                             st));
-  }
   // aux runs after everything st has queued so far (the previous chunk's
   // work is ordered on aux already), then resets the candidate queues.
   PSR_CUDA(cudaEventRecord(ev_fft[1], st));

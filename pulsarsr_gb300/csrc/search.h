@@ -21,8 +21,6 @@ struct SearchEngine {
   FftPlan fft;
   SpecConfig spec;
   SpecWork sw;
-  std::vector<double> host_sums;  // series sums supplied by the caller (optional)
-  std::vector<float> host_means;
   // Optional per-stage timing: events recorded around every stage launch on
   // the engine's stream; stage_ms accumulates their elapsed times.
   enum { ST_DEDISP = 0, ST_FFT = 1, ST_SPEC = 2, ST_COUNT = 3 };

@@ -61,10 +61,22 @@ def apply(fb: Filterbank, d, length: int | None = None) -> np.ndarray:
     return out
 
 
-def apply_trials(fb: Filterbank, trials, length: int) -> np.ndarray:
+def apply_trials(fb: Filterbank, trials, length: int, with_sums: bool = False):
+    """Series of every trial DM, [ntrials][length]; with_sums also returns
+    each series' f64 sum (the one periodicity's mean uses)."""
     t = _d(trials)
     out = np.empty((t.size, int(length)), dtype=np.float32)
+    sums = np.empty(t.size, dtype=np.float64)
     check(lib().psr_dedisperse_trials(fb.handle, t.ctypes.data_as(C.POINTER(C.c_double)),
                                       C.c_uint64(t.size), C.c_uint64(length),
-                                      out.ctypes.data_as(C.POINTER(C.c_float))))
-    return out
+                                      out.ctypes.data_as(C.POINTER(C.c_float)),
+                                      sums.ctypes.data_as(C.POINTER(C.c_double))
+                                      if with_sums else None))
+    return (out, sums) if with_sums else out
+
+
+def test_stage_timeout(fb: Filterbank, spin_limit: int = 1000) -> None:
+    """Test hook (psr_test_stage_timeout): one dedispersion launch whose TMA
+    barriers are armed but never fed, so the bounded waits run out; raises
+    WaitTimeout as a real give-up would."""
+    check(lib().psr_test_stage_timeout(fb.handle, C.c_uint64(spin_limit)))

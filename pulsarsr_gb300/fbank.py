@@ -61,8 +61,15 @@ class Filterbank:
         check(lib().psr_fb_download(self._h, out.ctypes.data_as(C.POINTER(C.c_float))))
         return out.reshape(self.header.nchans, self.nsamples)
 
+    def channels(self, c0: int, count: int) -> np.ndarray:
+        """Channels [c0, c0 + count) as f32, shape (count, nsamples) (a host copy)."""
+        out = np.empty((int(count), self.nsamples), dtype=np.float32)
+        check(lib().psr_fb_download_channels(self._h, C.c_uint64(c0), C.c_uint64(count),
+                                             out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
     def channel(self, c: int) -> np.ndarray:
-        return self.data[c]
+        return self.channels(c, 1)[0]
 
     def close(self) -> None:
         if self._h:

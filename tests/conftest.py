@@ -7,10 +7,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-# The PulsarSr reference tree (read-only).  Only CPU tests that pin the oracle
-# against the reference's shipped input files use it; they skip without it.
-REFERENCE_DIR = os.environ.get("PSR_REFERENCE_DIR", "/root/reference")
+# The reference's shipped input files (synthetic.fil, GBT_Lband_PSR.fil):
+# from the PulsarSr tree named by PSR_REFERENCE_DIR, else from the copies
+# tests/golden/stage_inputs.py puts in tests/golden/_ref_data/.  Tests that
+# need them skip when neither has them.
+REFERENCE_DIR = os.environ.get("PSR_REFERENCE_DIR", "")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+STAGED = os.path.join(GOLDEN, "_ref_data")
 
 
 def pytest_configure(config):
@@ -19,10 +22,10 @@ def pytest_configure(config):
 
 
 def reference_file(name: str) -> str:
-    path = os.path.join(REFERENCE_DIR, name)
-    if not os.path.exists(path):
-        pytest.skip(f"reference input {name} not available")
-    return path
+    for d in (REFERENCE_DIR, STAGED):
+        if d and os.path.exists(os.path.join(d, name)):
+            return os.path.join(d, name)
+    pytest.skip(f"reference input {name} not available")
 
 
 @pytest.fixture(scope="session")

@@ -5,9 +5,9 @@ Run once in a checkout where the PulsarSr reference tree is available:
     python tests/golden/make_golden.py /path/to/PulsarSr
 
 It reads only the reference's own saved run outputs (schema-2 reports, the
-DM-62 series metadata and the fold record) and writes compact JSON files
-beside this script.  The input filterbanks themselves are not copied; tests
-that need them look for the reference tree and skip when it is absent.
+DM-62 series metadata, the fold record and the GBT header text) and writes
+compact JSON files beside this script.  The input filterbanks themselves
+are staged separately by stage_inputs.py (git-ignored copies).
 """
 from __future__ import annotations
 
@@ -87,6 +87,12 @@ def main(ref: str) -> None:
         with open(os.path.join(HERE, name), "w") as fh:
             json.dump(obj, fh, separators=(",", ":"))
         print(name, os.path.getsize(os.path.join(HERE, name)))
+    # `psr header` output of the GBT file, byte for byte (pretty JSON text)
+    with open(os.path.join(ref, "output_confirm_gbt", "header.json"), "rb") as fh:
+        text = fh.read()
+    with open(os.path.join(HERE, "gbt_header.json"), "wb") as fh:
+        fh.write(text)
+    print("gbt_header.json", len(text))
 
 
 if __name__ == "__main__":

@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import reference_file
+from conftest import GOLDEN, reference_file
 
 
 @pytest.fixture(scope="module")
@@ -26,7 +26,7 @@ def run(exe, *args, cwd=None):
 def test_header_matches_reference_header_json(psr):
     """psr header prints the reference's output_confirm_gbt/header.json."""
     fil = reference_file("GBT_Lband_PSR.fil")
-    want = open(reference_file("output_confirm_gbt/header.json")).read()
+    want = open(os.path.join(GOLDEN, "gbt_header.json")).read()
     r = run(psr, "header", fil)
     assert r.returncode == 0, r.stderr
     assert r.stdout == want + "\n"

@@ -254,6 +254,33 @@ def test_dedisperse_edge_shapes(gpu, oracle, nbits):
         assert out[i].tobytes() == d1[0, :4999].astype(np.float32).tobytes(), i
 
 
+@pytest.mark.parametrize("nbits", [4, 8])
+def test_stage_wait_gives_up_and_context_recovers(gpu, oracle, nbits):
+    """The staged dedispersion kernel's bounded TMA waits: with its barriers
+    armed and no copy issued (nothing in flight), every CTA gives up together
+    and the host sees PSR_ETIMEOUT; the same context then dedisperses
+    correctly.  f32 samples do not take the staged kernel."""
+    from pulsarsr_gb300 import InvalidArgument, WaitTimeout, dedisperse, fbank, synth
+    mean, sigma = NOISE.get(nbits, (100., 10.))
+    o = synth.Observation(nchans=96, nbits=nbits, nsamples=12000, tsamp=72e-6, fch1=1448.,
+                          foff=-1.0, seed=23, noise_mean=mean, noise_sigma=sigma)
+    raw = o.to_bytes()
+    fb = fbank.decode(raw)
+    _, d = oracle.decode(raw)
+    freqs = fb.header.frequencies()
+    for _ in range(2):
+        with pytest.raises(WaitTimeout, match="bounded wait for a staged tile gave up"):
+            dedisperse.test_stage_timeout(fb, 1000)
+        trials = np.array([0.0, 62.4, 150.0])
+        out = dedisperse.apply_trials(fb, trials, 9000)
+        for i, dm in enumerate(trials):
+            assert out[i].tobytes() == oracle.apply(d, oracle.delays(freqs, o.tsamp, dm),
+                                                    9000).tobytes()
+    fbf, _ = f32_filterbank(np.ones((4, 100), dtype=np.float32))
+    with pytest.raises(InvalidArgument, match="does not take the staged kernel"):
+        dedisperse.test_stage_timeout(fbf, 1000)
+
+
 def test_dedisperse_errors(gpu):
     from pulsarsr_gb300 import DedisperseError, dedisperse, fbank
     fb = fbank.decode(fixture(8, [1, 2, 3, 4]))
@@ -374,10 +401,9 @@ def test_search_trials_match_oracle(gpu, oracle, cfgname):
     assert counts.sum() > 0
 
 
-def test_search_full_c2_sampled_trials(gpu, oracle):
-    """Full 2000-trial GBT-shaped search on the GPU; every 40th trial's list
-    is recomputed by the oracle and must match bit for bit (a trial's list
-    depends on that trial alone)."""
+def test_search_full_c2_every_trial(gpu, oracle):
+    """Full 2000-trial GBT-shaped search on the GPU; the oracle recomputes
+    every trial's list and all 2000 must match bit for bit."""
     from pulsarsr_gb300 import fbank, rfi, search, synth
     obs = synth.config_c2(2)
     raw, trials, disc = search_case(obs, 500.0)
@@ -389,17 +415,107 @@ def test_search_full_c2_sampled_trials(gpu, oracle):
     starts = np.concatenate([[0], np.cumsum(counts)]).astype(int)
     _, d = oracle.decode(raw)
     md, _ = oracle.rfi_mask(d, max(int(0.1 / obs.tsamp), 32), 8.0)
-    pick = np.arange(0, 2000, 40)
-    oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials[pick], disc,
+    oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials, disc,
                                       threads=THREADS, **cfg)
     ostarts = np.concatenate([[0], np.cumsum(oc)]).astype(int)
-    for j, i in enumerate(pick):
+    assert counts.tolist() == oc.tolist()
+    for i in range(trials.size):
         a = cands[starts[i]:starts[i + 1]]
-        b = ocands[ostarts[j]:ostarts[j + 1]]
+        b = ocands[ostarts[i]:ostarts[i + 1]]
         assert a.tobytes() == b.tobytes(), i
     # the injected 4.6214 ms pulsar is among the strongest candidates near DM 62.4
     near = cands[np.abs(cands["dm"] - 62.4) < 2.0]
     assert np.any(np.abs(near["frequency_hz"] - 1 / 0.0046214) < 0.05)
+
+
+# --------------------------------------------------- f32-sample searches
+def f32_obs(seed, noise_mean=100.0, nch=32, ns=1 << 16):
+    """An f32 filterbank shaped like the reference's synthetic.fil (32 ch,
+    65,536 samples at 250 us): non-integer samples, so the periodicity mean
+    (a sequential f64 sum, search/src/lib.rs:36) is order-sensitive."""
+    from pulsarsr_gb300 import synth
+    return synth.Observation(nchans=nch, nbits=32, nsamples=ns, tsamp=2.5e-4, fch1=1500.0,
+                             foff=-200.0 / nch, seed=seed, noise_mean=noise_mean,
+                             noise_sigma=10.0 if noise_mean else 1.0,
+                             pulsars=[synth.Pulsar(0.064, 40.0, 0.05, 0.6)])
+
+
+def sequential_sum(x):
+    """The reference's f64 series sum: one add after another, in order."""
+    return float(np.add.accumulate(np.asarray(x, dtype=np.float64))[-1])
+
+
+def test_f32_series_sums_are_the_sequential_sum(gpu):
+    """Series sums on f32 samples equal the in-order f64 sum bit for bit,
+    also where a reassociated sum would differ: a series whose small terms
+    the sequential sum loses against a large one."""
+    from pulsarsr_gb300 import dedisperse, fbank
+    obs = f32_obs(31)
+    fb = fbank.decode(obs.to_bytes())
+    trials = np.arange(0.0, 120.0 + 1e-9, 8.0)
+    n = 30000
+    x, sums = dedisperse.apply_trials(fb, trials, n, with_sums=True)
+    for i in range(trials.size):
+        assert np.float64(sums[i]).tobytes() == np.float64(sequential_sum(x[i])).tobytes(), i
+    # one channel, zero delay at every DM: the series is the channel itself
+    y = np.full(5000, 2.0 ** -20, dtype=np.float32)
+    y[1::3] *= np.float32(1.5)
+    y[0], y[-1] = 2.0 ** 40, -(2.0 ** 40)
+    fb1, _ = f32_filterbank(y[None, :])
+    x1, s1 = dedisperse.apply_trials(fb1, np.array([0.0, 10.0]), y.size, with_sums=True)
+    assert x1[0].tobytes() == y.tobytes()
+    want = sequential_sum(y)
+    assert want != float(np.sum(y.astype(np.float64)))  # pairwise differs here
+    assert s1.tolist() == [want, want]
+
+
+@pytest.mark.parametrize("noise_mean", [100.0, 0.0])
+def test_search_trials_f32_match_oracle(gpu, oracle, noise_mean):
+    """The trial loop on f32 samples, RFI on: candidate lists bit-identical
+    to the oracle's (mean = the reference's sequential f64 sum)."""
+    from pulsarsr_gb300 import fbank, rfi, search
+    obs = f32_obs(32 if noise_mean else 33, noise_mean)
+    raw = obs.to_bytes()
+    trials = np.arange(0.0, 120.0 + 1e-9, 2.0)
+    disc = 32000
+    cfg = dict(min_hz=10.0, max_hz=2000.0, threshold=8.0, max_candidates=32)
+    block = max(int(0.1 / obs.tsamp), 32)
+    fb = fbank.decode(raw)
+    m = rfi.mask(fb, block, 8.0)
+    counts, cands = search.search_trials(fb, trials, disc, search.Config(**cfg))
+    _, d = oracle.decode(raw)
+    md, om = oracle.rfi_mask(d, block, 8.0)
+    assert (m.channels, m.blocks) == (om["channels"], om["blocks"])
+    oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials, disc,
+                                      threads=THREADS, **cfg)
+    assert counts.tolist() == oc.tolist()
+    assert cands.tobytes() == ocands.tobytes()
+    assert counts.sum() > 0
+
+
+def test_session_f32_matches_oracle(gpu, oracle):
+    """unpack -> RFI -> trial loop in a session on f32 samples, twice."""
+    from pulsarsr_gb300 import fbank, search, session
+    obs = f32_obs(34)
+    raw = obs.to_bytes()
+    hdr = fbank.parse_header(raw)
+    trials = np.arange(0.0, 120.0 + 1e-9, 2.0)
+    disc = 32000
+    cfg = search.Config(min_hz=10.0, max_hz=2000.0, threshold=8.0)
+    block = max(int(0.1 / obs.tsamp), 32)
+    s = session.SearchSession(hdr, obs.nsamples, trials, disc, cfg, block, 8.0)
+    _, d = oracle.decode(raw)
+    md, om = oracle.rfi_mask(d, block, 8.0)
+    oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials, disc,
+                                      threads=THREADS, min_hz=10.0, max_hz=2000.0,
+                                      threshold=8.0, max_candidates=32)
+    for _ in range(2):
+        s.load(raw[hdr.data_offset:])
+        s.run()
+        s.sync()
+        counts, cands = s.candidates()
+        assert counts.tolist() == oc.tolist()
+        assert cands.tobytes() == ocands.tobytes()
 
 
 def test_session_pipeline_matches_oracle(gpu, oracle):

@@ -78,3 +78,23 @@ def test_noalloc_on_a_caller_stream(gpu):
         assert noalloc_power(s, st).tobytes() == want.tobytes()
     finally:
         rt.cudaStreamDestroy(st)
+
+
+@pytest.mark.gpu
+def test_noalloc_allocates_no_device_memory(gpu):
+    """After warm-up calls of every size (which load the modules and their
+    kernels, and so reserve the fixed array), further calls of changing sizes
+    leave the device's free memory unchanged."""
+    rt = _cudart()
+    rng = np.random.default_rng(11)
+    series = [rng.normal(0, 1, n).astype(np.float32) for n in (1000, 300_000, 4097, MAX_LEN, 2)]
+    for s in series:
+        noalloc_power(s)
+    free0, free1, total = C.c_size_t(), C.c_size_t(), C.c_size_t()
+    assert rt.cudaDeviceSynchronize() == 0
+    assert rt.cudaMemGetInfo(C.byref(free0), C.byref(total)) == 0
+    for s in series + series[::-1]:
+        noalloc_power(s)
+    assert rt.cudaDeviceSynchronize() == 0
+    assert rt.cudaMemGetInfo(C.byref(free1), C.byref(total)) == 0
+    assert free1.value == free0.value
