@@ -317,6 +317,17 @@ void psr_refine_options_default(psr_refine_options *out);
 int psr_refine_objective(const psr_fb *fb, uint64_t n, const psr_timing *theta,
                          const psr_refine_options *opt, double variance, double *J,
                          double *grad, double *profile, double *subint_profiles);
+/* The objective psr_refine_gradient optimises by default (exact = 0): the
+ * channels x subints x bins cube folded at `reference`, each (channel,
+ * subint) row shifted by its phase change at the subint centre (band-limited,
+ * in the Fourier domain), J = sum_b (p_b - mean p)^2 / (n v) (by Parseval,
+ * from the harmonics) with v the summed channel variances; J[k] and its adjoint
+ * gradient grad[3k..3k+2] = dJ/d(P, Pdot, DM) at each of npoints points
+ * theta.  No reference counterpart; exposed so the fast path's adjoint can be
+ * checked against finite differences and an FP64 model. */
+int psr_refine_cube_objective(const psr_fb *fb, uint64_t n, const psr_timing *reference,
+                              const psr_timing *theta, uint64_t npoints,
+                              const psr_refine_options *opt, double *J, double *grad);
 /* Gradient refinement (quasi-Newton ascent) of ncand starting points. */
 int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start,
                         uint64_t ncand, const psr_refine_options *opt,

@@ -940,6 +940,31 @@ int psr_refine_objective(const psr_fb *fb, uint64_t n, const psr_timing *theta,
   return PSR_OK;
 }
 
+int psr_refine_cube_objective(const psr_fb *fb, uint64_t n, const psr_timing *reference,
+                              const psr_timing *theta, uint64_t npoints,
+                              const psr_refine_options *opt, double *J, double *grad) {
+  PSR_TRY(refine_length(fb, n));
+  RefineOptions ro;
+  PSR_TRY(refine_options(opt, ro));
+  if (!reference || !theta || !J || npoints == 0) {
+    set_error("refine: null argument");
+    return PSR_EINVAL;
+  }
+  std::vector<double> g(3 * npoints);
+  PSR_TRY(cube_objective(fb->o, n, *reference, theta, npoints, ro, J, g.data(), fb->stream.s));
+  if (grad) {
+    // (nu, nudot) = (1/P, -Pdot/P^2): the chain rule to (P, Pdot).
+    for (uint64_t k = 0; k < npoints; ++k) {
+      const double P = theta[k].period_s, Pd = theta[k].pdot;
+      const double gnu = g[3 * k], gnd = g[3 * k + 1];
+      grad[3 * k] = gnu * (-1.0 / (P * P)) + gnd * (2.0 * Pd / (P * P * P));
+      grad[3 * k + 1] = gnd * (-1.0 / (P * P));
+      grad[3 * k + 2] = g[3 * k + 2];
+    }
+  }
+  return PSR_OK;
+}
+
 int psr_refine_gradient(const psr_fb *fb, uint64_t n, const psr_timing *start, uint64_t ncand,
                         const psr_refine_options *opt, psr_timing *out, double *J,
                         uint64_t *evals) {

@@ -105,9 +105,44 @@ __device__ __forceinline__ void dft4(float2 &v0, float2 &v1, float2 &v2, float2 
   v2 = csub(a, c);
   v3 = csub(b, d);
 }
-// Wl[y] = W_L^y; W_R^y = Wl[y * L / R].
+// The internal twiddles of the radix-8 and radix-16 butterflies, W_16^y for
+// y in {1, 2, 3, 4, 6, 9}, held in registers.  W_L^(y L/16) is the table
+// entry for x = y N/16 whatever L is, so one set serves every sub-FFT size;
+// load_w16 reads them from a sub-FFT's table (values identical to the table
+// lookups they replace).
+struct W16 {
+  float2 w1, w2, w3, w4, w6, w9;
+  template <int Y>
+  __device__ __forceinline__ float2 get() const {
+    static_assert(Y == 1 || Y == 2 || Y == 3 || Y == 4 || Y == 6 || Y == 9, "W_16 power");
+    if constexpr (Y == 1) return w1;
+    else if constexpr (Y == 2) return w2;
+    else if constexpr (Y == 3) return w3;
+    else if constexpr (Y == 4) return w4;
+    else if constexpr (Y == 6) return w6;
+    else return w9;
+  }
+};
 template <int L>
-__device__ __forceinline__ void dft8(float2 *v, const float2 *Wl) {
+__device__ __forceinline__ W16 load_w16(const float2 *Wl) {
+  W16 c{};
+  if constexpr (L >= 16) {
+    c.w1 = Wl[1 * (L / 16)];
+    c.w2 = Wl[2 * (L / 16)];
+    c.w3 = Wl[3 * (L / 16)];
+    c.w4 = Wl[4 * (L / 16)];
+    c.w6 = Wl[6 * (L / 16)];
+    c.w9 = Wl[9 * (L / 16)];
+  } else if constexpr (L == 8) {  // W_8^n2 = W_16^(2 n2)
+    c.w2 = Wl[1];
+    c.w4 = Wl[2];
+    c.w6 = Wl[3];
+  }
+  return c;
+}
+
+// W_R^y = W_16^(y 16/R).
+__device__ __forceinline__ void dft8(float2 *v, const W16 &c) {
   float2 u[4][2];
 #pragma unroll
   for (int n2 = 0; n2 < 4; ++n2) {
@@ -116,8 +151,9 @@ __device__ __forceinline__ void dft8(float2 *v, const float2 *Wl) {
     u[n2][0] = a;
     u[n2][1] = b;
   }
-#pragma unroll
-  for (int n2 = 1; n2 < 4; ++n2) u[n2][1] = cmul(u[n2][1], Wl[n2 * (L / 8)]);
+  u[1][1] = cmul(u[1][1], c.get<2>());
+  u[2][1] = cmul(u[2][1], c.get<4>());
+  u[3][1] = cmul(u[3][1], c.get<6>());
 #pragma unroll
   for (int k1 = 0; k1 < 2; ++k1) {
     float2 a = u[0][k1], b = u[1][k1], c = u[2][k1], d = u[3][k1];
@@ -128,8 +164,7 @@ __device__ __forceinline__ void dft8(float2 *v, const float2 *Wl) {
     v[k1 + 6] = d;
   }
 }
-template <int L>
-__device__ __forceinline__ void dft16(float2 *v, const float2 *Wl) {
+__device__ __forceinline__ void dft16(float2 *v, const W16 &c) {
   float2 u[4][4];
 #pragma unroll
   for (int n2 = 0; n2 < 4; ++n2) {
@@ -140,10 +175,15 @@ __device__ __forceinline__ void dft16(float2 *v, const float2 *Wl) {
     u[n2][2] = c;
     u[n2][3] = d;
   }
-#pragma unroll
-  for (int n2 = 1; n2 < 4; ++n2)
-#pragma unroll
-    for (int k1 = 1; k1 < 4; ++k1) u[n2][k1] = cmul(u[n2][k1], Wl[n2 * k1 * (L / 16)]);
+  u[1][1] = cmul(u[1][1], c.get<1>());
+  u[1][2] = cmul(u[1][2], c.get<2>());
+  u[1][3] = cmul(u[1][3], c.get<3>());
+  u[2][1] = cmul(u[2][1], c.get<2>());
+  u[2][2] = cmul(u[2][2], c.get<4>());
+  u[2][3] = cmul(u[2][3], c.get<6>());
+  u[3][1] = cmul(u[3][1], c.get<3>());
+  u[3][2] = cmul(u[3][2], c.get<6>());
+  u[3][3] = cmul(u[3][3], c.get<9>());
 #pragma unroll
   for (int k1 = 0; k1 < 4; ++k1) {
     float2 a = u[0][k1], b = u[1][k1], c = u[2][k1], d = u[3][k1];
@@ -155,12 +195,40 @@ __device__ __forceinline__ void dft16(float2 *v, const float2 *Wl) {
   }
 }
 
-template <int R, int L>
-__device__ __forceinline__ void dftR(float2 *v, const float2 *Wl) {
+// dft16 of inputs whose v[4..15] are zero (the zero padding): the first
+// level's DFT_4s of (x, 0, 0, 0) return (x, x, x, x), identical to what
+// dft16 computes up to the sign of zero components, which no later
+// operation turns into a non-zero difference.
+__device__ __forceinline__ void dft16_first4(float2 *v, const W16 &c) {
+  float2 u[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) u[n2][0] = u[n2][1] = u[n2][2] = u[n2][3] = v[n2];
+  u[1][1] = cmul(u[1][1], c.get<1>());
+  u[1][2] = cmul(u[1][2], c.get<2>());
+  u[1][3] = cmul(u[1][3], c.get<3>());
+  u[2][1] = cmul(u[2][1], c.get<2>());
+  u[2][2] = cmul(u[2][2], c.get<4>());
+  u[2][3] = cmul(u[2][3], c.get<6>());
+  u[3][1] = cmul(u[3][1], c.get<3>());
+  u[3][2] = cmul(u[3][2], c.get<6>());
+  u[3][3] = cmul(u[3][3], c.get<9>());
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 a = u[0][k1], b = u[1][k1], cc = u[2][k1], d = u[3][k1];
+    dft4(a, b, cc, d);
+    v[k1] = a;
+    v[k1 + 4] = b;
+    v[k1 + 8] = cc;
+    v[k1 + 12] = d;
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void dftR(float2 *v, const W16 &c) {
   if constexpr (R == 2) dft2(v[0], v[1]);
   else if constexpr (R == 4) dft4(v[0], v[1], v[2], v[3]);
-  else if constexpr (R == 8) dft8<L>(v, Wl);
-  else dft16<L>(v, Wl);
+  else if constexpr (R == 8) dft8(v, c);
+  else dft16(v, c);
 }
 
 // One in-place Stockham stage (radix R, Ns = product of earlier radices) on
@@ -173,7 +241,7 @@ __host__ __device__ constexpr int lay_step() {
 }
 
 template <int R, int L, int C, int NT, int Ns>
-__device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
+__device__ __forceinline__ void stage(float2 *sm, const float2 *Wl, const W16 &c16) {
   constexpr int nb = L / R;
   constexpr int total = nb * C;
   constexpr int BPT = (total + NT - 1) / NT;
@@ -198,7 +266,7 @@ __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
           for (int r = 1; r < R; ++r) v[i][r] = cmul(v[i][r], Wl[r * k * (L / (Ns * R))]);
         }
       }
-      dftR<R, L>(v[i], Wl);
+      dftR<R>(v[i], c16);
     }
   }
   __syncthreads();
@@ -222,33 +290,33 @@ __device__ __forceinline__ void stage(float2 *sm, const float2 *Wl) {
 }
 
 template <int L, int C, int NT, int s>
-__device__ __forceinline__ void stages16(float2 *sm, const float2 *Wl) {
+__device__ __forceinline__ void stages16(float2 *sm, const float2 *Wl, const W16 &c) {
   if constexpr (s < ilog2(L) / 4) {
-    stage<16, L, C, NT, (1 << (4 * s))>(sm, Wl);
-    stages16<L, C, NT, s + 1>(sm, Wl);
+    stage<16, L, C, NT, (1 << (4 * s))>(sm, Wl, c);
+    stages16<L, C, NT, s + 1>(sm, Wl, c);
   }
 }
 
 // The stages after the first radix-16 stage (used when stage 0 runs fused
 // with the global loads).
 template <int L, int C, int NT>
-__device__ __forceinline__ void subfft_rest(float2 *sm, const float2 *Wl) {
+__device__ __forceinline__ void subfft_rest(float2 *sm, const float2 *Wl, const W16 &c) {
   constexpr int q = ilog2(L);
   constexpr int NsLast = 1 << (4 * (q / 4));
-  stages16<L, C, NT, 1>(sm, Wl);
-  if constexpr (q % 4 == 1) stage<2, L, C, NT, NsLast>(sm, Wl);
-  else if constexpr (q % 4 == 2) stage<4, L, C, NT, NsLast>(sm, Wl);
-  else if constexpr (q % 4 == 3) stage<8, L, C, NT, NsLast>(sm, Wl);
+  stages16<L, C, NT, 1>(sm, Wl, c);
+  if constexpr (q % 4 == 1) stage<2, L, C, NT, NsLast>(sm, Wl, c);
+  else if constexpr (q % 4 == 2) stage<4, L, C, NT, NsLast>(sm, Wl, c);
+  else if constexpr (q % 4 == 3) stage<8, L, C, NT, NsLast>(sm, Wl, c);
 }
 
 template <int L, int C, int NT>
-__device__ __forceinline__ void subfft(float2 *sm, const float2 *Wl) {
+__device__ __forceinline__ void subfft(float2 *sm, const float2 *Wl, const W16 &c) {
   constexpr int q = ilog2(L);
   constexpr int NsLast = 1 << (4 * (q / 4));
-  stages16<L, C, NT, 0>(sm, Wl);
-  if constexpr (q % 4 == 1) stage<2, L, C, NT, NsLast>(sm, Wl);
-  else if constexpr (q % 4 == 2) stage<4, L, C, NT, NsLast>(sm, Wl);
-  else if constexpr (q % 4 == 3) stage<8, L, C, NT, NsLast>(sm, Wl);
+  stages16<L, C, NT, 0>(sm, Wl, c);
+  if constexpr (q % 4 == 1) stage<2, L, C, NT, NsLast>(sm, Wl, c);
+  else if constexpr (q % 4 == 2) stage<4, L, C, NT, NsLast>(sm, Wl, c);
+  else if constexpr (q % 4 == 3) stage<8, L, C, NT, NsLast>(sm, Wl, c);
 }
 
 template <int L>
@@ -333,7 +401,8 @@ __global__ void __launch_bounds__(threads_for(M, 1))
   build_wl<M>(Wl, N, Q, lq);
   for (int n = threadIdx.x; n < M; n += NT) sm[lay<1>(n, 0)] = load_z(row, len, (uint64_t)n, mean);
   __syncthreads();
-  subfft<M, 1, NT>(sm, Wl);
+  const W16 c16 = load_w16<M>(Wl);
+  subfft<M, 1, NT>(sm, Wl, c16);
   Acc2 acc;
   float *out = power + trial * ldp;
   for (int k = threadIdx.x; k <= M; k += NT) {
@@ -345,32 +414,140 @@ __global__ void __launch_bounds__(threads_for(M, 1))
   block_sum_store<NT>(acc, psum + trial);
 }
 
-// Pass 1: C columns n2 in [n2_0, n2_0 + C) of length M1, then W_M^(n2*k1).
-// Persistent: CTA b takes column groups b, b + gridDim.x, ... (group g =
-// trial g / (M2/C), columns (g % (M2/C)) C ...), builds the twiddle table
-// once, and while it transforms one group prefetches the next group's
-// samples into L2 (one 64-byte run of C complex inputs per row).
+// Pass 1 on one column group: C columns n2 in [n2_0, n2_0 + C) of trial
+// `row` (length M1 over n1), then W_M^(n2*k1), written to out[k1*M2 + n2].
+template <int M1, int M2>
+__device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16 &c16,
+                                         const float *__restrict__ row, uint64_t len,
+                                         float mean, uint32_t n2_0,
+                                         const float2 *__restrict__ tw1,
+                                         float2 *__restrict__ out) {
+  constexpr int C = cols_for(M1), NT = threads_for(M1, C);
+  constexpr int total = M1 * C;
+  const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
+  const uint64_t rows_nz = (nz + M2 - 1) / M2;  // rows n1 holding any of them
+  {
+    // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
+    // (col, j) takes positions j + r*M1/16 of its column and stores its
+    // outputs at 16j + r.  The zero padding (n >= nz) is never loaded, and
+    // butterflies whose inputs r >= 4 all lie in it skip their first level.
+    constexpr int nb = M1 / 16;
+    constexpr int nbt = nb * C;
+    constexpr int BPT = (nbt + NT - 1) / NT;
+#pragma unroll
+    for (int i = 0; i < BPT; ++i) {
+      const int w = (int)threadIdx.x + i * NT;
+      if (nbt % NT == 0 || w < nbt) {
+        const int col = w % C, j = w / C;
+        float2 v[16];
+        if ((uint64_t)(j + 4 * nb) >= rows_nz) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+          }
+          dft16_first4(v, c16);
+        } else {
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+          }
+          dft16(v, c16);
+        }
+        if constexpr (16 % C == 0) {
+          // e = (16j + r) C + col with col < C | 16: the padding of r C +
+          // col is (r C) / 16, so every r is a constant offset
+          float2 *dst = sm + 17 * C * j + col;
+#pragma unroll
+          for (int r = 0; r < 16; ++r) dst[r * C + (r * C) / 16] = v[r];
+        } else {
+#pragma unroll
+          for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  subfft_rest<M1, C, NT>(sm, Wl, c16);
+  // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 +
+  // n2] (values identical to the quarter-table lookup): reads coalesce.
+  if constexpr (NT % C == 0 && 16 % C == 0) {
+    // thread t drains column t % C at rows k1 = t / C + i NT / C: slot
+    // lay<C>(k1, col) = C k1 + col + (C k1) / 16 advances by a constant
+    constexpr int KS = NT / C;  // row step
+    const int col = (int)threadIdx.x % C, k10 = (int)threadIdx.x / C;
+    const uint32_t n2 = n2_0 + (uint32_t)col;
+    const float2 *src = sm + C * k10 + col + (C * k10) / 16;
+    const float2 *tws = tw1 + (uint64_t)k10 * M2 + n2;
+    float2 *dst = out + (uint64_t)k10 * M2 + n2;
+    constexpr int NI = M1 / KS;
+#pragma unroll 1
+    for (int i0 = 0; i0 < NI; i0 += LB) {
+      float2 w[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u)
+        w[u] = i0 + u < NI ? __ldg(tws + (uint64_t)(i0 + u) * KS * M2)
+                           : make_float2(1.0f, 0.0f);
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        if (i0 + u < NI) {
+          const int k1 = k10 + (i0 + u) * KS;
+          float2 v = src[(i0 + u) * lay_step<C, KS>()];
+          if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
+          dst[(uint64_t)(i0 + u) * KS * M2] = v;
+        }
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (int base = 0; base < total; base += LB * NT) {
+      float2 w[LB];
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int idx = base + u * NT + (int)threadIdx.x;
+        w[u] = idx < total ? __ldg(&tw1[(uint64_t)(idx / C) * M2 + n2_0 + (idx % C)])
+                           : make_float2(1.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < LB; ++u) {
+        const int idx = base + u * NT + (int)threadIdx.x;
+        if (idx < total) {
+          const int col = idx % C, k1 = idx / C;
+          const uint32_t n2 = n2_0 + (uint32_t)col;
+          float2 v = sm[lay<C>(k1, col)];
+          if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
+          out[(uint64_t)k1 * M2 + n2] = v;
+        }
+      }
+    }
+  }
+}
+
+// Pass 1: column groups of every trial, persistent: CTA b takes groups b,
+// b + gridDim.x, ... (group g = trial g / (M2/C), columns (g % (M2/C)) C
+// ...), builds the twiddle table once, and while it transforms one group
+// prefetches the next group's samples into L2 (one 64-byte run of C complex
+// inputs per row).
 template <int M1, int M2>
 __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
     k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
                 const float *__restrict__ means, const float2 *__restrict__ Q, int lq,
                 uint32_t N, const float2 *__restrict__ tw1, float2 *__restrict__ work,
                 uint32_t ngroups) {
-  constexpr int C = cols_for(M1), NT = threads_for(M1, C);
+  constexpr int C = cols_for(M1);
   constexpr uint32_t M = (uint32_t)M1 * M2;
   constexpr uint32_t GPT = M2 / C;  // column groups per trial
   extern __shared__ float2 dyn[];
   float2 *Wl = dyn;       // M1 entries
   float2 *sm = dyn + M1;  // lay_slots<M1, C>() entries
   build_wl<M1>(Wl, N, Q, lq);
-  const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
-  constexpr int total = M1 * C;
+  const uint64_t nz = (len + 1) / 2;
   __syncthreads();  // Wl
+  const W16 c16 = load_w16<M1>(Wl);
   for (uint32_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
     const uint64_t trial = grp / GPT;
     const uint32_t n2_0 = (grp % GPT) * (uint32_t)C;
-    const float *row = series + trial * lds;
-    const float mean = means[trial];
     {
       // (only inputs the next group loads: complex index < nz)
       const uint32_t nx = grp + gridDim.x;
@@ -380,115 +557,24 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
       }
     }
-    {
-      // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
-      // (col, j) takes positions j + r*M1/16 of its column and stores its
-      // outputs at 16j + r.  The zero padding (n >= nz) is never loaded.
-      constexpr int nb = M1 / 16;
-      constexpr int nbt = nb * C;
-      constexpr int BPT = (nbt + NT - 1) / NT;
-#pragma unroll
-      for (int i = 0; i < BPT; ++i) {
-        const int w = (int)threadIdx.x + i * NT;
-        if (nbt % NT == 0 || w < nbt) {
-          const int col = w % C, j = w / C;
-          float2 v[16];
-#pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
-            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
-          }
-          dft16<M1>(v, Wl);
-          if constexpr (16 % C == 0) {
-            // e = (16j + r) C + col with col < C | 16: the padding of r C +
-            // col is (r C) / 16, so every r is a constant offset
-            float2 *dst = sm + 17 * C * j + col;
-#pragma unroll
-            for (int r = 0; r < 16; ++r) dst[r * C + (r * C) / 16] = v[r];
-          } else {
-#pragma unroll
-            for (int r = 0; r < 16; ++r) sm[lay<C>(16 * j + r, col)] = v[r];
-          }
-        }
-      }
-    }
-    __syncthreads();
-    subfft_rest<M1, C, NT>(sm, Wl);
-    float2 *out = work + trial * (uint64_t)M;
-    // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 +
-    // n2] (values identical to the quarter-table lookup): reads coalesce.
-    if constexpr (NT % C == 0 && 16 % C == 0) {
-      // thread t drains column t % C at rows k1 = t / C + i NT / C: slot
-      // lay<C>(k1, col) = C k1 + col + (C k1) / 16 advances by a constant
-      constexpr int KS = NT / C;  // row step
-      const int col = (int)threadIdx.x % C, k10 = (int)threadIdx.x / C;
-      const uint32_t n2 = n2_0 + (uint32_t)col;
-      const float2 *src = sm + C * k10 + col + (C * k10) / 16;
-      const float2 *tws = tw1 + (uint64_t)k10 * M2 + n2;
-      float2 *dst = out + (uint64_t)k10 * M2 + n2;
-      constexpr int NI = M1 / KS;
-#pragma unroll 1
-      for (int i0 = 0; i0 < NI; i0 += LB) {
-        float2 w[LB];
-#pragma unroll
-        for (int u = 0; u < LB; ++u)
-          w[u] = i0 + u < NI ? __ldg(tws + (uint64_t)(i0 + u) * KS * M2)
-                             : make_float2(1.0f, 0.0f);
-#pragma unroll
-        for (int u = 0; u < LB; ++u) {
-          if (i0 + u < NI) {
-            const int k1 = k10 + (i0 + u) * KS;
-            float2 v = src[(i0 + u) * lay_step<C, KS>()];
-            if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
-            dst[(uint64_t)(i0 + u) * KS * M2] = v;
-          }
-        }
-      }
-    } else {
-#pragma unroll 1
-      for (int base = 0; base < total; base += LB * NT) {
-        float2 w[LB];
-#pragma unroll
-        for (int u = 0; u < LB; ++u) {
-          const int idx = base + u * NT + (int)threadIdx.x;
-          w[u] = idx < total ? __ldg(&tw1[(uint64_t)(idx / C) * M2 + n2_0 + (idx % C)])
-                             : make_float2(1.0f, 0.0f);
-        }
-#pragma unroll
-        for (int u = 0; u < LB; ++u) {
-          const int idx = base + u * NT + (int)threadIdx.x;
-          if (idx < total) {
-            const int col = idx % C, k1 = idx / C;
-            const uint32_t n2 = n2_0 + (uint32_t)col;
-            float2 v = sm[lay<C>(k1, col)];
-            if (n2 * (uint32_t)k1 != 0) v = cmul(v, w[u]);
-            out[(uint64_t)k1 * M2 + n2] = v;
-          }
-        }
-      }
-    }
+    p1_group<M1, M2>(sm, Wl, c16, series + trial * lds, len, means[trial], n2_0, tw1,
+                     work + trial * (uint64_t)M);
     __syncthreads();  // the next group's stage 0 overwrites sm
   }
 }
 
-// Pass 2: row sub-FFTs of length M2 for a group of rows and their mirrors,
-// then the real post-processing and |X|^2.  Group 0 holds rows 0 and M1/2;
-// group g >= 1 holds rows kb..kb+h-1 (kb = 1 + (g-1)*H) and M1-kb..M1-kb-h+1.
+// Pass 2 on one row group of one trial: the row sub-FFTs of length M2, then
+// the real post-processing and |X|^2.  Group 0 holds rows 0 and M1/2; group
+// g >= 1 holds rows kb..kb+h-1 (kb = 1 + (g-1)*H) and M1-kb..M1-kb-h+1.
 // Unused columns of the last group are transformed but never read.
+// The row twiddle table Wl is built while the rows are in flight.
 template <int M1, int M2>
-__global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
-    k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q, int lq,
-                uint32_t N, float *__restrict__ power, uint64_t ldp, double *__restrict__ psum,
-                uint32_t ngroups, uint32_t ahead) {
+__device__ __forceinline__ void p2_group(float2 *sm, float2 *Wl, uint32_t N,
+                                         const float2 *__restrict__ in, uint32_t g,
+                                         const float2 *__restrict__ Q, int lq,
+                                         float *__restrict__ out, double *__restrict__ psum_out) {
   constexpr int C = cols_for(M2), NT = threads_for(M2, C), H = C / 2;
   constexpr uint32_t M = (uint32_t)M1 * M2;
-  extern __shared__ float2 dyn[];
-  float2 *Wl = dyn;       // M2 entries
-  float2 *sm = dyn + M2;  // lay_slots<M2, C>() entries
-  const uint64_t trial = blockIdx.y;
-  const uint32_t g = blockIdx.x;
-  const float2 *in = work + trial * (uint64_t)M;
-  float *out = power + trial * ldp;
   int h;
   uint32_t kb = 0;
   if (g == 0) {
@@ -498,34 +584,13 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
     h = (int)min((uint32_t)H, (uint32_t)(M1 / 2 - kb));
   }
   const int ncols = 2 * h;
-  {
-    // Prefetch into L2 the rows of the CTA one resident wave ahead (linear
-    // index + ahead): CTAs start roughly in index order, so it runs soon.
-    const uint64_t lin = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x + ahead;
-    if (ahead && lin < (uint64_t)gridDim.x * gridDim.y) {
-      const uint32_t gn = (uint32_t)(lin % gridDim.x);
-      const uint64_t tn = lin / gridDim.x;
-      const uint32_t kbn = gn == 0 ? 0u : 1 + (gn - 1) * (uint32_t)H;
-      const int hn = gn == 0 ? 1 : (int)min((uint32_t)H, (uint32_t)(M1 / 2 - kbn));
-      constexpr int LPR = M2 * 8 / 128;  // 128-byte lines per row
-      for (int t = threadIdx.x; t < 2 * hn * LPR; t += NT) {
-        const int ci = t / LPR;
-        const uint32_t k1 = gn == 0 ? (ci == 0 ? 0u : (uint32_t)(M1 / 2))
-                                    : (ci < hn ? kbn + (uint32_t)ci
-                                               : (uint32_t)M1 - (kbn + (uint32_t)(ci - hn)));
-        const float2 *pr = work + tn * M + (uint64_t)k1 * M2 + (t % LPR) * 16;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
-      }
-    }
-  }
   const int total = M2 * ncols;
   auto row_of = [&](int ci) -> uint32_t {
     if (g == 0) return ci == 0 ? 0u : (uint32_t)(M1 / 2);
     return ci < h ? kb + (uint32_t)ci : (uint32_t)M1 - (kb + (uint32_t)(ci - h));
   };
   if constexpr (C == 16 && NT == M2) {
-    // thread t copies position t of every row to slot lay<16>(t, ci) = 17 t + ci;
-    // all copies are in flight while the row twiddles are built
+    // thread t copies position t of every row to slot lay<16>(t, ci) = 17 t + ci
     const float2 *src = in + threadIdx.x;
     float2 *dst = sm + 17 * threadIdx.x;
 #pragma unroll
@@ -552,7 +617,8 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
     }
   }
   __syncthreads();
-  subfft<M2, C, NT>(sm, Wl);
+  const W16 c16 = load_w16<M2>(Wl);
+  subfft<M2, C, NT>(sm, Wl, c16);
   Acc2 acc;
   if (g == 0) {
     for (uint32_t idx = threadIdx.x; idx < 2 * M2; idx += NT) {
@@ -617,7 +683,44 @@ __global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
     if (h == H) rows(std::integral_constant<int, H>{});
     else rows(std::integral_constant<int, 0>{});
   }
-  block_sum_store<NT>(acc, psum + trial * ngroups + g);
+  block_sum_store<NT>(acc, psum_out);
+}
+
+// Pass 2: one CTA per row group of every trial.
+template <int M1, int M2>
+__global__ void __launch_bounds__(threads_for(M2, cols_for(M2)), 2)
+    k_fft_pass2(const float2 *__restrict__ work, const float2 *__restrict__ Q, int lq,
+                uint32_t N, float *__restrict__ power, uint64_t ldp, double *__restrict__ psum,
+                uint32_t ngroups, uint32_t ahead) {
+  constexpr int C = cols_for(M2), NT = threads_for(M2, C), H = C / 2;
+  constexpr uint32_t M = (uint32_t)M1 * M2;
+  extern __shared__ float2 dyn[];
+  float2 *Wl = dyn;       // M2 entries
+  float2 *sm = dyn + M2;  // lay_slots<M2, C>() entries
+  const uint64_t trial = blockIdx.y;
+  const uint32_t g = blockIdx.x;
+  {
+    // Prefetch into L2 the rows of the CTA one resident wave ahead (linear
+    // index + ahead): CTAs start roughly in index order, so it runs soon.
+    const uint64_t lin = (uint64_t)blockIdx.y * gridDim.x + blockIdx.x + ahead;
+    if (ahead && lin < (uint64_t)gridDim.x * gridDim.y) {
+      const uint32_t gn = (uint32_t)(lin % gridDim.x);
+      const uint64_t tn = lin / gridDim.x;
+      const uint32_t kbn = gn == 0 ? 0u : 1 + (gn - 1) * (uint32_t)H;
+      const int hn = gn == 0 ? 1 : (int)min((uint32_t)H, (uint32_t)(M1 / 2 - kbn));
+      constexpr int LPR = M2 * 8 / 128;  // 128-byte lines per row
+      for (int t = threadIdx.x; t < 2 * hn * LPR; t += NT) {
+        const int ci = t / LPR;
+        const uint32_t k1 = gn == 0 ? (ci == 0 ? 0u : (uint32_t)(M1 / 2))
+                                    : (ci < hn ? kbn + (uint32_t)ci
+                                               : (uint32_t)M1 - (kbn + (uint32_t)(ci - hn)));
+        const float2 *pr = work + tn * M + (uint64_t)k1 * M2 + (t % LPR) * 16;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
+      }
+    }
+  }
+  p2_group<M1, M2>(sm, Wl, N, work + trial * (uint64_t)M, g, Q, lq, power + trial * ldp,
+                   psum + trial * ngroups + g);
 }
 
 struct FftArgs {

@@ -1012,6 +1012,36 @@ void set_direction(Opt &s) {
 
 }  // namespace
 
+int cube_objective(const DeviceObs &o, uint64_t n, const psr_timing &ref, const psr_timing *theta,
+                   uint64_t K, const RefineOptions &opt, double *Jout, double *gout,
+                   cudaStream_t st) {
+  const int B = (int)opt.bins, S = (int)opt.subints;
+  if (B > CB_MAXB || B < 8 || S < 1 || K == 0) {
+    set_error("cube_objective: 8..1024 bins, >= 1 subint and >= 1 point required");
+    return PSR_EINVAL;
+  }
+  const double nu_r = 1.0 / ref.period_s, nudot_r = -ref.pdot * nu_r * nu_r;
+  CubeWork w;
+  PSR_TRY(build_cube(o, n, S, B, nu_r, nudot_r, ref.dm, w, st));
+  std::vector<CandDev> cand(K);
+  for (uint64_t k = 0; k < K; ++k) {
+    cand[k].nu = 1.0 / theta[k].period_s;
+    cand[k].nudot = -theta[k].pdot * cand[k].nu * cand[k].nu;
+    cand[k].dm = theta[k].dm;
+  }
+  std::vector<double> J, grad;
+  PSR_TRY(eval_cube(o, n, S, B, nu_r, nudot_r, ref.dm, cand, w, J, grad, st));
+  for (uint64_t k = 0; k < K; ++k) {
+    Jout[k] = J[k];
+    if (gout) {
+      gout[3 * k] = grad[3 * k];
+      gout[3 * k + 1] = grad[3 * k + 1];
+      gout[3 * k + 2] = grad[3 * k + 2];
+    }
+  }
+  return PSR_OK;
+}
+
 int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, uint64_t K,
                       const RefineOptions &opt, psr_timing *out, double *Jout, uint64_t *evals,
                       CubeCache &cache, cudaStream_t st) {

@@ -50,6 +50,12 @@ struct CubeCache {
   ~CubeCache();
 };
 
+// The cube objective J at K points theta, with the cube folded at `ref`,
+// and its adjoint gradient in (nu, nudot, DM) (3 values per point).
+int cube_objective(const DeviceObs &o, uint64_t n, const psr_timing &ref, const psr_timing *theta,
+                   uint64_t K, const RefineOptions &opt, double *J, double *grad,
+                   cudaStream_t st);
+
 // Cube-based refinement of K nearby starting points (k_refine_cube.cu).
 int refine_cube_group(const DeviceObs &o, uint64_t n, const psr_timing *start, uint64_t K,
                       const RefineOptions &opt, psr_timing *out, double *J, uint64_t *evals,

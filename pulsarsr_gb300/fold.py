@@ -96,6 +96,22 @@ def refine_objective(fb, n: int, period: float, pdot: float, dm: float, bins: in
     return J.value, grad, prof, cells.reshape(subints, bins)
 
 
+def refine_cube_objective(fb, n: int, reference, points, bins: int = 128, subints: int = 64):
+    """The cube objective of refine_gradient's default path: the cube folded
+    at `reference` (P, Pdot, DM), J and dJ/d(P, Pdot, DM) at each point;
+    returns (J array, gradient array of shape (npoints, 3))."""
+    ref = Timing(*reference)
+    pts = np.ascontiguousarray(np.array([tuple(x) for x in points], dtype=TIMING_DTYPE))
+    J = np.zeros(pts.size)
+    grad = np.zeros((pts.size, 3))
+    opt = RefineOptions.make(bins, subints)
+    check(lib().psr_refine_cube_objective(fb.handle, C.c_uint64(n), C.byref(ref),
+                                          pts.ctypes.data_as(C.c_void_p), C.c_uint64(pts.size),
+                                          C.byref(opt), J.ctypes.data_as(C.POINTER(C.c_double)),
+                                          grad.ctypes.data_as(C.POINTER(C.c_double))))
+    return J, grad
+
+
 def refine_gradient(fb, n: int, starts, bins: int = 128, subints: int = 64,
                     max_evals: int = 40, tol_bins: float = 1e-3, exact: bool = False,
                     dm_window: float = 0.0):

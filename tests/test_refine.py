@@ -90,11 +90,14 @@ def test_device_objective_and_adjoint_match_fp64(gpu, oracle, obs_data):
         Jd, gd, pd, cells = fold.refine_objective(fb, N, P, PD, D, 128, 64, variance=vfix)
         Jo, go, po = oracle.refine_objective(data, freqs, TSAMP, N, P, PD, D, 128, 64,
                                              variance=vfix)
-        # f32 sums over 64 channels against f64: relative 1e-5 per sample.
-        assert np.isclose(Jd, Jo, rtol=1e-4), (Jd, Jo)
+        # The device sums 64 channels per sample in f32 (about 2^-24 relative
+        # each) and accumulates cells and adjoint terms in f64: measured on a
+        # GB300, J within 6e-9 and every gradient component within 2e-6 of
+        # the FP64 oracle; the bounds leave a 10x margin.
+        assert np.isclose(Jd, Jo, rtol=1e-7), (Jd, Jo)
         assert np.allclose(pd, po, rtol=1e-4, atol=1e-3 * np.abs(po).max())
         assert np.allclose(cells.sum(axis=0), pd, rtol=1e-9, atol=1e-6)
-        assert np.allclose(gd, go, rtol=2e-3, atol=1e-3 * np.abs(go).max()), (gd, go)
+        assert np.allclose(gd, go, rtol=2e-5, atol=1e-7 * np.abs(go).max()), (gd, go)
 
 
 @pytest.mark.gpu
