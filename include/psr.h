@@ -156,6 +156,22 @@ typedef struct {
   uint64_t npulsars;   /* at most 64 */
 } psr_synth_config;
 int psr_fb_synth(const psr_synth_config *cfg, psr_fb **out);
+/* Seeded interference added in place to a device filterbank (no reference
+ * counterpart; the survey-scale workload's narrowband and burst RFI):
+ * nb_channels distinct channels get nb_amplitude * (0.5 + 0.5 sin(2 pi nb_hz t
+ * + phase_c)), and nbursts broadband bursts of burst_samples samples add
+ * burst_amplitude to every channel; amplitudes are in sample units, integer
+ * samples are rounded and clamped again. */
+typedef struct {
+  uint64_t seed;
+  uint64_t nb_channels;
+  double nb_amplitude;
+  double nb_hz;
+  uint64_t nbursts;      /* at most 1024 */
+  uint64_t burst_samples;
+  double burst_amplitude;
+} psr_synth_rfi;
+int psr_fb_inject_rfi(psr_fb *fb, const psr_synth_rfi *rfi);
 /* Filterbank.data as f32, channel-major (nchans * nsamples values). */
 int psr_fb_download(const psr_fb *fb, float *out);
 /* Channels [c0, c0 + nchannels) of Filterbank.data (nchannels * nsamples

@@ -88,7 +88,7 @@ struct Dedisperser {
     PSR_CUDA(cudaMemcpyAsync(dd.p, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice, st));
     PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), ntr, n, out.as<float>(), ldo,
                                  parts.as<double>(), sums.as<double>(), means.as<float>(),
-                                 spread, err.as<unsigned>(), st));
+                                 spread, err.as<unsigned>(), st, 0, 0, false));
     unsigned e = 0;
     PSR_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, st));
     PSR_CUDA(cudaStreamSynchronize(st));

@@ -546,6 +546,14 @@ int psr_fb_synth(const psr_synth_config *cfg, psr_fb **out) {
   return PSR_OK;
 }
 
+int psr_fb_inject_rfi(psr_fb *fb, const psr_synth_rfi *rfi) {
+  if (!fb || !rfi) {
+    set_error("invalid interference configuration");
+    return PSR_EINVAL;
+  }
+  return inject_rfi(fb->o, *rfi, fb->stream.s);
+}
+
 int psr_fb_info(const psr_fb *fb, psr_header *header, uint64_t *nsamples) {
   if (!fb) {
     set_error("fb_info: null handle");
@@ -720,7 +728,7 @@ int dedisperse_delays(const DeviceObs &o, const uint64_t *d, int64_t length, flo
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
   PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), 1, n, ser.as<float>(), ldo,
                                parts.as<double>(), sums.as<double>(), means.as<float>(), spread,
-                               err.as<unsigned>(), st));
+                               err.as<unsigned>(), st, 0, 0, false));
   PSR_CUDA(cudaMemcpyAsync(out, ser.p, n * 4, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
   return PSR_OK;
@@ -763,7 +771,7 @@ int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntria
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
   PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), ntrials, length, ser.as<float>(), ldo,
                                parts.as<double>(), sums.as<double>(), means.as<float>(), spread,
-                               err.as<unsigned>(), st));
+                               err.as<unsigned>(), st, 0, 0, sums_out != nullptr));
   PSR_CUDA(cudaMemcpy2DAsync(out, length * 4, ser.p, ldo * 4, length * 4, ntrials,
                              cudaMemcpyDeviceToHost, st));
   if (sums_out)

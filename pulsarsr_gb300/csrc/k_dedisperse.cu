@@ -510,7 +510,7 @@ uint64_t series_ld(uint64_t n) { return ((n + 63) / 64) * 64; }
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part,
                          double *d_sums, float *d_means, uint64_t max_spread, unsigned *d_err,
-                         cudaStream_t st, long long spin_limit, int arm_only) {
+                         cudaStream_t st, long long spin_limit, int arm_only, bool want_means) {
   const long long spin = spin_limit > 0 ? spin_limit : DD_SPIN_LIMIT;
   // Integer samples: channel groups small enough that a group's sum fits the
   // 16-bit lanes (nch * max <= 65535 when there is one group); the groups'
@@ -557,9 +557,11 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
         }
         PSR_CUDA(cudaGetLastError());
       }
-      k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
-          d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, 0);
-      PSR_CUDA(cudaGetLastError());
+      if (want_means) {
+        k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
+            d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, 0);
+        PSR_CUDA(cudaGetLastError());
+      }
       return PSR_OK;
     }
   }
@@ -582,9 +584,11 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
                                                       ntiles);
   }
   PSR_CUDA(cudaGetLastError());
-  k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
-      d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, o.kind == SAMPLE_F32 ? 1 : 0);
-  PSR_CUDA(cudaGetLastError());
+  if (want_means) {
+    k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
+        d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, o.kind == SAMPLE_F32 ? 1 : 0);
+    PSR_CUDA(cudaGetLastError());
+  }
   return PSR_OK;
 }
 

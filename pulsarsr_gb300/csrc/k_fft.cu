@@ -195,34 +195,6 @@ __device__ __forceinline__ void dft16(float2 *v, const W16 &c) {
   }
 }
 
-// dft16 of inputs whose v[4..15] are zero (the zero padding): the first
-// level's DFT_4s of (x, 0, 0, 0) return (x, x, x, x), identical to what
-// dft16 computes up to the sign of zero components, which no later
-// operation turns into a non-zero difference.
-__device__ __forceinline__ void dft16_first4(float2 *v, const W16 &c) {
-  float2 u[4][4];
-#pragma unroll
-  for (int n2 = 0; n2 < 4; ++n2) u[n2][0] = u[n2][1] = u[n2][2] = u[n2][3] = v[n2];
-  u[1][1] = cmul(u[1][1], c.get<1>());
-  u[1][2] = cmul(u[1][2], c.get<2>());
-  u[1][3] = cmul(u[1][3], c.get<3>());
-  u[2][1] = cmul(u[2][1], c.get<2>());
-  u[2][2] = cmul(u[2][2], c.get<4>());
-  u[2][3] = cmul(u[2][3], c.get<6>());
-  u[3][1] = cmul(u[3][1], c.get<3>());
-  u[3][2] = cmul(u[3][2], c.get<6>());
-  u[3][3] = cmul(u[3][3], c.get<9>());
-#pragma unroll
-  for (int k1 = 0; k1 < 4; ++k1) {
-    float2 a = u[0][k1], b = u[1][k1], cc = u[2][k1], d = u[3][k1];
-    dft4(a, b, cc, d);
-    v[k1] = a;
-    v[k1 + 4] = b;
-    v[k1 + 8] = cc;
-    v[k1 + 12] = d;
-  }
-}
-
 template <int R>
 __device__ __forceinline__ void dftR(float2 *v, const W16 &c) {
   if constexpr (R == 2) dft2(v[0], v[1]);
@@ -425,12 +397,10 @@ __device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16
   constexpr int C = cols_for(M1), NT = threads_for(M1, C);
   constexpr int total = M1 * C;
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
-  const uint64_t rows_nz = (nz + M2 - 1) / M2;  // rows n1 holding any of them
   {
     // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
     // (col, j) takes positions j + r*M1/16 of its column and stores its
-    // outputs at 16j + r.  The zero padding (n >= nz) is never loaded, and
-    // butterflies whose inputs r >= 4 all lie in it skip their first level.
+    // outputs at 16j + r.  The zero padding (n >= nz) is never loaded.
     constexpr int nb = M1 / 16;
     constexpr int nbt = nb * C;
     constexpr int BPT = (nbt + NT - 1) / NT;
@@ -440,21 +410,12 @@ __device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16
       if (nbt % NT == 0 || w < nbt) {
         const int col = w % C, j = w / C;
         float2 v[16];
-        if ((uint64_t)(j + 4 * nb) >= rows_nz) {
 #pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
-            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
-          }
-          dft16_first4(v, c16);
-        } else {
-#pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
-            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
-          }
-          dft16(v, c16);
+        for (int r = 0; r < 16; ++r) {
+          const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+          v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
         }
+        dft16(v, c16);
         if constexpr (16 % C == 0) {
           // e = (16j + r) C + col with col < C | 16: the padding of r C +
           // col is (r C) / 16, so every r is a constant offset

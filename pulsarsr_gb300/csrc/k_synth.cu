@@ -12,6 +12,7 @@
 // the same seed always gives the same data.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -171,6 +172,34 @@ int synth_obs(const psr_synth_config &cfg, DeviceObs &o, cudaStream_t st) {
 }
 
 namespace {
+// Interference added in place: channel c of `band` (1 = narrowband) gets
+// nb_amp * (0.5 + 0.5 sin(2 pi nb_hz t tsamp + phi_c)) on every sample; every
+// channel gets burst_amp inside each burst window [start_k, start_k + width).
+// Values are rounded and clamped again for integer bit depths.
+template <class T>
+__global__ void __launch_bounds__(SY_NT)
+    k_inject_rfi(T *__restrict__ out, uint64_t ld, uint64_t ns, double tsamp,
+                 const uint8_t *__restrict__ band, const float *__restrict__ phi, float nb_amp,
+                 double nb_hz, const uint64_t *__restrict__ starts, int nbursts, uint64_t width,
+                 float burst_amp, float hi) {
+  const uint64_t c = blockIdx.y;
+  const bool nb = band[c] != 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * SY_NT + threadIdx.x; t < ns;
+       t += (uint64_t)gridDim.x * SY_NT) {
+    float add = 0.0f;
+    if (nb) {
+      const double x = nb_hz * tsamp * (double)t;
+      add += nb_amp * (0.5f + 0.5f * sinpif(2.0f * (float)(x - floor(x)) + phi[c]));
+    }
+    for (int k = 0; k < nbursts; ++k)
+      if (t >= starts[k] && t - starts[k] < width) add += burst_amp;
+    if (add == 0.0f) continue;
+    float v = (float)out[c * ld + t] + add;
+    if (hi > 0.0f) v = fminf(fmaxf(rintf(v), 0.0f), hi);
+    out[c * ld + t] = (T)v;
+  }
+}
+
 // payload[t * nch + c] = samples[c * ld + t] for 8-bit samples: 32 x 32
 // tiles through shared memory (coalesced reads along t, writes along c).
 __global__ void k_pack_u8(const uint8_t *__restrict__ samples, uint64_t ld, uint64_t ns,
@@ -188,6 +217,64 @@ __global__ void k_pack_u8(const uint8_t *__restrict__ samples, uint64_t ld, uint
   }
 }
 }  // namespace
+
+int inject_rfi(DeviceObs &o, const psr_synth_rfi &r, cudaStream_t st) {
+  if (r.nb_channels > o.nch || r.nbursts > 1024 || !(r.nb_amplitude >= 0.0) ||
+      !(r.burst_amplitude >= 0.0) || !std::isfinite(r.nb_hz) ||
+      (r.nbursts && (r.burst_samples == 0 || r.burst_samples > o.ns))) {
+    set_error("invalid interference configuration");
+    return PSR_EINVAL;
+  }
+  // Seeded choices: narrowband channels (distinct), their tone phases and
+  // the burst start samples.
+  std::vector<uint8_t> band(o.nch, 0);
+  std::vector<float> phi(o.nch, 0.0f);
+  uint64_t picked = 0, i = 0;
+  while (picked < r.nb_channels) {
+    const uint64_t c = host_mix64(r.seed ^ host_mix64(0xBA5Eull + i++)) % o.nch;
+    if (!band[c]) {
+      band[c] = 1;
+      ++picked;
+    }
+  }
+  for (uint64_t c = 0; c < o.nch; ++c)
+    phi[c] = (float)((host_mix64(r.seed ^ host_mix64(0xF00Dull + c)) >> 40) *
+                     (2.0 / 16777216.0));
+  std::vector<uint64_t> starts(r.nbursts + 1, 0);
+  for (uint64_t k = 0; k < r.nbursts; ++k)
+    starts[k] = host_mix64(r.seed ^ host_mix64(0xB0B0ull + k)) % (o.ns - r.burst_samples + 1);
+  DevBuf dband, dphi, dstarts;
+  PSR_TRY(dband.ensure(o.nch));
+  PSR_TRY(dphi.ensure(o.nch * 4));
+  PSR_TRY(dstarts.ensure(starts.size() * 8));
+  PSR_CUDA(cudaMemcpyAsync(dband.p, band.data(), o.nch, cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(dphi.p, phi.data(), o.nch * 4, cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaMemcpyAsync(dstarts.p, starts.data(), starts.size() * 8, cudaMemcpyHostToDevice,
+                           st));
+  const float hi = o.kind == SAMPLE_U8 ? (float)((1u << (o.h.nbits < 8 ? o.h.nbits : 8)) - 1)
+                   : o.kind == SAMPLE_U16 ? 65535.0f : 0.0f;
+  dim3 grid((unsigned)std::min<uint64_t>((o.ns + SY_NT - 1) / SY_NT, 64), (unsigned)o.nch);
+  const float nba = (float)r.nb_amplitude, ba = (float)r.burst_amplitude;
+  switch (o.kind) {
+    case SAMPLE_U8:
+      k_inject_rfi<uint8_t><<<grid, SY_NT, 0, st>>>(
+          o.samples.as<uint8_t>(), o.ld, o.ns, o.h.tsamp, dband.as<uint8_t>(), dphi.as<float>(),
+          nba, r.nb_hz, dstarts.as<uint64_t>(), (int)r.nbursts, r.burst_samples, ba, hi);
+      break;
+    case SAMPLE_U16:
+      k_inject_rfi<uint16_t><<<grid, SY_NT, 0, st>>>(
+          o.samples.as<uint16_t>(), o.ld, o.ns, o.h.tsamp, dband.as<uint8_t>(), dphi.as<float>(),
+          nba, r.nb_hz, dstarts.as<uint64_t>(), (int)r.nbursts, r.burst_samples, ba, hi);
+      break;
+    default:
+      k_inject_rfi<float><<<grid, SY_NT, 0, st>>>(
+          o.samples.as<float>(), o.ld, o.ns, o.h.tsamp, dband.as<uint8_t>(), dphi.as<float>(),
+          nba, r.nb_hz, dstarts.as<uint64_t>(), (int)r.nbursts, r.burst_samples, ba, 0.0f);
+  }
+  PSR_CUDA(cudaGetLastError());
+  PSR_CUDA(cudaStreamSynchronize(st));
+  return PSR_OK;
+}
 
 int pack_payload_u8(const DeviceObs &src, uint8_t *d_payload, cudaStream_t st) {
   if (src.kind != SAMPLE_U8 || src.h.nbits != 8) {

@@ -122,6 +122,8 @@ struct DeviceObs {
 
 // Seeded synthetic observation generated on the device (k_synth.cu).
 int synth_obs(const psr_synth_config &cfg, DeviceObs &o, cudaStream_t st);
+// Seeded interference added in place (narrowband channels, broadband bursts).
+int inject_rfi(DeviceObs &o, const psr_synth_rfi &r, cudaStream_t st);
 // Time-major 8-bit payload (as read from a file) of a device observation.
 int pack_payload_u8(const DeviceObs &src, uint8_t *d_payload, cudaStream_t st);
 
@@ -209,10 +211,12 @@ int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
 // (packed integer) kernel's waits give up after spin_limit polls (0 = the
 // default limit) and set *d_err; arm_only = 1 arms its barriers without
 // issuing the copies, so every wait runs out (a test of that path).
+// With want_means = false (series only folded, not searched) the sums and
+// means are left unset.
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part, double *d_sums,
                          float *d_means, uint64_t max_spread, unsigned *d_err, cudaStream_t st,
-                         long long spin_limit = 0, int arm_only = 0);
+                         long long spin_limit = 0, int arm_only = 0, bool want_means = true);
 uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
 // The f64 sum of a device series and the f32 mean search::periodicity
 // subtracts (search/src/lib.rs:36), bit-identical to the reference's

@@ -184,3 +184,23 @@ def device(nchans: int, nbits: int, nsamples: int, tsamp: float, fch1: float, fo
     h = C.c_void_p()
     check(lib().psr_fb_synth(C.byref(cfg), C.byref(h)))
     return Filterbank(h.value)
+
+
+def inject_rfi(fb, seed: int, nb_channels: int = 0, nb_amplitude: float = 0.0,
+               nb_hz: float = 0.0, nbursts: int = 0, burst_samples: int = 0,
+               burst_amplitude: float = 0.0) -> None:
+    """Seeded interference added in place to a device filterbank
+    (psr_fb_inject_rfi): nb_channels narrowband channels modulated at nb_hz,
+    and nbursts broadband bursts; amplitudes in sample units."""
+    import ctypes as C
+
+    from ._lib import check, lib
+
+    class _R(C.Structure):
+        _fields_ = [("seed", C.c_uint64), ("nb_channels", C.c_uint64),
+                    ("nb_amplitude", C.c_double), ("nb_hz", C.c_double),
+                    ("nbursts", C.c_uint64), ("burst_samples", C.c_uint64),
+                    ("burst_amplitude", C.c_double)]
+
+    r = _R(seed, nb_channels, nb_amplitude, nb_hz, nbursts, burst_samples, burst_amplitude)
+    check(lib().psr_fb_inject_rfi(fb.handle, C.byref(r)))

@@ -428,6 +428,29 @@ def test_search_full_c2_every_trial(gpu, oracle):
     assert np.any(np.abs(near["frequency_hz"] - 1 / 0.0046214) < 0.05)
 
 
+def test_injected_rfi_is_masked_like_the_oracle(gpu, oracle):
+    """Seeded narrowband channels and broadband bursts added on the device
+    (the survey workload's interference): the mask flags them, and mask,
+    fraction and filled data equal the oracle's on the same samples."""
+    from pulsarsr_gb300 import rfi, synth
+    fb = synth.device(128, 8, 1 << 17, 64e-6, 1600.0, -400.0 / 128, seed=8, noise_mean=128.0,
+                      noise_sigma=16.0, gain_spread=0.1)
+    clean = fb.data
+    synth.inject_rfi(fb, 8, nb_channels=3, nb_amplitude=48.0, nb_hz=50.0, nbursts=2,
+                     burst_samples=781, burst_amplitude=32.0)
+    d = fb.data
+    changed = np.flatnonzero(np.any(d != clean, axis=1))
+    nb = [c for c in changed if np.mean(d[c] != clean[c]) > 0.5]
+    assert len(nb) == 3
+    block = max(int(0.1 / 64e-6), 32)
+    m = rfi.mask(fb, block, 8.0)
+    od, om = oracle.rfi_mask(d, block, 8.0)
+    assert set(nb) <= set(m.channels) and len(m.blocks) >= 2
+    assert (m.channels, m.blocks, m.masked_fraction) == (om["channels"], om["blocks"],
+                                                          om["masked_fraction"])
+    assert np.array_equal(fb.data, od)
+
+
 # --------------------------------------------------- f32-sample searches
 def f32_obs(seed, noise_mean=100.0, nch=32, ns=1 << 16):
     """An f32 filterbank shaped like the reference's synthetic.fil (32 ch,
