@@ -787,7 +787,7 @@ def run_batch(args):
     b.sync()
     ms_default = timed(max(args.steps // 3, 2))
     t0 = time.perf_counter()
-    chunk, inner = b.tune()
+    chunk, inner, subbands = b.tune()
     t_tune = time.perf_counter() - t0
     b.run()
     b.sync()
@@ -810,12 +810,52 @@ def run_batch(args):
                            zip(*np.unique(chunk, return_counts=True))},
         "tuned_fft_chunk": {str(int(k)): int(v) for k, v in
                             zip(*np.unique(inner, return_counts=True))},
-        "cpu_estimate": {"value": round(8.25e7 * 96 * units / adds, 1), "kind": "extrapolated",
-                         "basis": "oracle on 16 host cores for the 96-channel GBT-shaped "
-                                  "search (8.25e7 DM-trial*samples/s), scaled by channels"},
+        "tuned_subbands": {str(int(k)): int(v) for k, v in
+                           zip(*np.unique(subbands, return_counts=True))},
         "clocks": clk,
     }
+    if not args.no_cpu:
+        line["cpu_baseline"] = batch_cpu_sample(specs, obs)
     print(json.dumps(line))
+
+
+def batch_cpu_sample(specs, obs, every=16, ntrials=32):
+    """The oracle on the host cores for the batch: every `every`-th
+    observation regenerated with the same generator, RFI-masked, and
+    `ntrials` of its trial DMs spread over its plan searched on all threads;
+    the rate is the sampled DM-trial*samples over the summed time (a subset,
+    stated as such)."""
+    from oracle import oracle as O
+    O.build()
+    from pulsarsr_gb300 import synth
+    threads = os.cpu_count() or 1
+    units, secs, picked = 0, 0.0, []
+    for i in range(0, len(specs), every):
+        nch, ns, tsamp, fch1, foff, ps = specs[i]
+        o = obs[i]
+        fb = synth.device(nch, 8, ns, tsamp, fch1, foff, seed=300 + i, noise_mean=128.0,
+                          noise_sigma=16.0, pulsars=ps)
+        d = fb.data
+        fb.close()
+        freqs = fch1 + np.arange(nch) * foff
+        t0 = time.perf_counter()
+        m, _ = O.rfi_mask(d, o["rfi_block"], 8.0)
+        t_rfi = time.perf_counter() - t0
+        del d
+        tr = o["trials"]
+        pick = tr[np.linspace(0, len(tr) - 1, min(ntrials, len(tr))).round().astype(int)]
+        t0 = time.perf_counter()
+        O.search_trials(m, freqs, tsamp, pick, o["discovery"], threads=threads, min_hz=1.0,
+                        max_hz=2000.0, threshold=8.0, max_candidates=32)
+        t_tr = time.perf_counter() - t0
+        # the whole observation: RFI once plus every trial at the sampled rate
+        secs += t_rfi + t_tr * len(tr) / len(pick)
+        units += len(tr) * o["discovery"]
+        picked.append(f"{nch}ch x {ns} ({len(pick)} of {len(tr)} trials)")
+    return {"value": round(units / secs, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(picked)} of the {len(specs)} observations: "
+                      f"{'; '.join(picked)}; each RFI-masked once, the trial time extrapolated "
+                      f"from the sampled trials to its plan; {threads} threads"}
 
 
 def main():

@@ -216,6 +216,14 @@ int psr_dedisperse(const psr_fb *fb, const uint64_t *delays, int64_t length,
 int psr_dedisperse_trials(const psr_fb *fb, const double *trials,
                           uint64_t ntrials, uint64_t length, float *out,
                           double *sums);
+/* Tuning, no reference counterpart: how the many-trial dedispersion of
+ * psr_dedisperse_trials, searches and sessions treats samples stored in 8
+ * bits (<= 8-bit data).  0: every channel added to every trial; 4 or 8:
+ * channels in subbands of that width, each subband's partial sum formed once
+ * per distinct intra-subband delay pattern of 8 consecutive trials and added
+ * shifted to every trial that shares it (identical results); -1 (initial):
+ * the library default.  Process-wide; affects searches prepared afterwards. */
+int psr_set_dedisp_subbands(int subbands);
 
 /* Test hook, no reference counterpart: one dedispersion launch (DM 0, up to
  * 8192 samples) whose staged kernel arms its TMA barriers but issues no
@@ -506,10 +514,13 @@ int psr_batch_load(psr_batch *b, uint64_t i, const uint8_t *payload, uint64_t nb
 /* Load observation i from an 8-bit device filterbank of the same shape (its
  * samples packed into the time-major payload on the device). */
 int psr_batch_load_fb(psr_batch *b, uint64_t i, const psr_fb *fb);
-/* Autotuner: times whole searches of every loaded observation at a few
- * (dedispersion block, FFT chunk) pairs and keeps the fastest; chunk/inner
- * (n entries each, may be NULL) receive the choices. */
-int psr_batch_tune(psr_batch *b, uint64_t *chunk, uint64_t *inner);
+/* Autotuner: per shape class (channels, bit depth, FFT size, trial count to
+ * the nearest power of two), times whole searches of the class's first
+ * loaded observation at each candidate tiling (DM block and half of it;
+ * whole-block or 64-trial FFT launches; for 8-bit samples, channel-by-channel
+ * or 8-channel subband dedispersion) and applies the fastest to the class.
+ * chunk/inner/subbands (n entries each, may be NULL) receive the choices. */
+int psr_batch_tune(psr_batch *b, uint64_t *chunk, uint64_t *inner, int *subbands);
 /* Pin observation i's dedispersion block (trials per outer chunk, >= 1) and
  * FFT launch size (trials per inner chunk; 0 = the whole block within a 4 GB
  * work buffer): the manual counterpart of psr_batch_tune.  No reference

@@ -55,11 +55,15 @@ class Batch:
         check(lib().psr_batch_load_fb(self._b, C.c_uint64(i), fb.handle))
 
     def tune(self):
+        """psr_batch_tune: per shape class, the fastest (DM block, FFT launch
+        size, subband width); returns the three per-observation arrays."""
         ch = np.zeros(self.n, dtype=np.uint64)
         inner = np.zeros(self.n, dtype=np.uint64)
+        sub = np.zeros(self.n, dtype=np.int32)
         check(lib().psr_batch_tune(self._b, ch.ctypes.data_as(C.POINTER(C.c_uint64)),
-                                   inner.ctypes.data_as(C.POINTER(C.c_uint64))))
-        return ch, inner
+                                   inner.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                   sub.ctypes.data_as(C.POINTER(C.c_int))))
+        return ch, inner, sub
 
     def set_chunking(self, i: int, chunk: int, inner: int = 0) -> None:
         """Pin observation i's DM block and FFT launch size (trials)."""

@@ -769,9 +769,12 @@ int psr_dedisperse_trials(const psr_fb *fb, const double *trials, uint64_t ntria
   PSR_TRY(means.ensure(ntrials * 4));
   PSR_TRY(err.ensure(8));
   PSR_CUDA(cudaMemsetAsync(err.p, 0, 8, st));
+  SubbandPlan sbp;
+  const int G = o.kind == SAMPLE_U8 ? dedisp_subbands_default(o) : 0;
+  PSR_TRY(build_subband_plan(tab, o.nch, {0, ntrials}, G, sbp, st));
   PSR_TRY(launch_dedisperse_ex(o, dd.as<uint32_t>(), ntrials, length, ser.as<float>(), ldo,
                                parts.as<double>(), sums.as<double>(), means.as<float>(), spread,
-                               err.as<unsigned>(), st, 0, 0, sums_out != nullptr));
+                               err.as<unsigned>(), st, 0, 0, sums_out != nullptr, &sbp, 0));
   PSR_CUDA(cudaMemcpy2DAsync(out, length * 4, ser.p, ldo * 4, length * 4, ntrials,
                              cudaMemcpyDeviceToHost, st));
   if (sums_out)
@@ -1403,9 +1406,10 @@ uint64_t chunk_for_budget(const psr_batch_obs *obs, uint64_t n, double budget) {
   return (uint64_t)std::max(16.0, std::min(256.0, std::floor(c)));
 }
 
-int reprepare(psr_session *s, uint64_t chunk, uint64_t inner) {
+int reprepare(psr_session *s, uint64_t chunk, uint64_t inner, int subbands = -2) {
   s->eng.chunk = chunk;
   s->eng.inner = inner;
+  if (subbands > -2) s->eng.subbands = subbands;
   PSR_TRY(s->eng.prepare(s->o, s->trials.data(), s->trials.size(), s->discovery, s->spec,
                          s->stream.s));
   PSR_CUDA(cudaStreamSynchronize(s->stream.s));
@@ -1459,9 +1463,6 @@ int psr_batch_load_fb(psr_batch *b, uint64_t i, const psr_fb *fb) {
   return PSR_OK;
 }
 
-// Autotuner: for every observation, time one whole search at each (DM block,
-// FFT chunk) pair of a small set around the defaults, on the loaded data,
-// and keep the fastest.  Results per observation are in chunk/inner.
 int psr_batch_set_chunking(psr_batch *b, uint64_t i, uint64_t chunk, uint64_t inner) {
   if (!b || i >= b->obs.size() || chunk == 0) {
     set_error("batch: observation index out of range or empty DM block");
@@ -1475,48 +1476,77 @@ int psr_batch_set_chunking(psr_batch *b, uint64_t i, uint64_t chunk, uint64_t in
   return PSR_OK;
 }
 
-int psr_batch_tune(psr_batch *b, uint64_t *chunk_out, uint64_t *inner_out) {
+// Autotuner.  Observations fall into shape classes (channels, bit depth, FFT
+// size, trial count to the nearest power of two); the first observation of a
+// class is searched whole at each candidate tiling, on its loaded data, and
+// the fastest is applied to the whole class.  Candidates: the budgeted DM
+// block and half of it (outer chunk), whole-block or 64-trial FFT launches
+// (inner chunk), and for 8-bit samples channel-by-channel or 8-channel
+// subband dedispersion.
+int psr_batch_tune(psr_batch *b, uint64_t *chunk_out, uint64_t *inner_out, int *subbands_out) {
   if (!b) {
     set_error("batch: null handle");
     return PSR_EINVAL;
   }
   b->drop_graph();
-  for (size_t i = 0; i < b->obs.size(); ++i) {
+  struct Pick {
+    uint64_t chunk, inner;
+    int subbands;
+  };
+  std::map<std::tuple<uint64_t, int64_t, uint64_t, int>, Pick> classes;
+  cudaEvent_t e0, e1;
+  PSR_CUDA(cudaEventCreate(&e0));
+  PSR_CUDA(cudaEventCreate(&e1));
+  int rc = PSR_OK;
+  for (size_t i = 0; i < b->obs.size() && rc == PSR_OK; ++i) {
     psr_session *s = b->obs[i].get();
-    const uint64_t c0 = b->chunk[i];
-    std::vector<std::pair<uint64_t, uint64_t>> cand;
-    for (uint64_t c : {c0, std::max<uint64_t>(16, c0 / 2)})
-      for (uint64_t inner : {(uint64_t)0, (uint64_t)16, (uint64_t)64})
-        cand.emplace_back(c, inner);
-    double best = 1e300;
-    std::pair<uint64_t, uint64_t> pick{c0, 0};
-    cudaEvent_t e0, e1;
-    PSR_CUDA(cudaEventCreate(&e0));
-    PSR_CUDA(cudaEventCreate(&e1));
-    for (const auto &c : cand) {
-      PSR_TRY(reprepare(s, c.first, c.second));
-      PSR_TRY(psr_session_run(s));  // warm (first use of the new buffers)
-      PSR_TRY(psr_session_sync(s));
-      PSR_CUDA(cudaEventRecord(e0, s->stream.s));
-      PSR_TRY(psr_session_run(s));
-      PSR_CUDA(cudaEventRecord(e1, s->stream.s));
-      PSR_TRY(psr_session_sync(s));
-      float ms = 0.0f;
-      PSR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best) {
-        best = ms;
-        pick = {s->eng.chunk, s->eng.inner};
+    int lt = 0;
+    while ((1ull << lt) < s->trials.size()) ++lt;
+    const auto key = std::make_tuple(s->o.nch, s->o.h.nbits, s->eng.fft.M, lt);
+    auto it = classes.find(key);
+    if (it == classes.end()) {
+      const uint64_t c0 = b->chunk[i];
+      std::vector<Pick> cand;
+      for (uint64_t c : {c0, std::max<uint64_t>(16, c0 / 2)})
+        for (uint64_t inner : {(uint64_t)0, (uint64_t)64})
+          for (int g : {0, 8})
+            if (g == 0 || s->o.h.nbits == 8) cand.push_back(Pick{c, inner, g});
+      double best = 1e300;
+      Pick pick = cand[0];
+      for (const Pick &c : cand) {
+        if ((rc = reprepare(s, c.chunk, c.inner, c.subbands)) != PSR_OK) break;
+        if ((rc = psr_session_run(s)) != PSR_OK || (rc = psr_session_sync(s)) != PSR_OK) break;
+        if (cudaEventRecord(e0, s->stream.s) != cudaSuccess ||
+            (rc = psr_session_run(s)) != PSR_OK ||
+            cudaEventRecord(e1, s->stream.s) != cudaSuccess ||
+            (rc = psr_session_sync(s)) != PSR_OK) {
+          if (rc == PSR_OK) rc = PSR_ECUDA;
+          break;
+        }
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+          rc = PSR_ECUDA;
+          break;
+        }
+        if (ms < best) {
+          best = ms;
+          pick = Pick{s->eng.chunk, s->eng.inner, c.subbands};
+        }
       }
+      it = classes.emplace(key, pick).first;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    PSR_TRY(reprepare(s, pick.first, pick.second));
-    b->chunk[i] = pick.first;
-    b->inner[i] = pick.second;
-    if (chunk_out) chunk_out[i] = pick.first;
-    if (inner_out) inner_out[i] = pick.second;
+    if (rc != PSR_OK) break;
+    const Pick &p = it->second;
+    rc = reprepare(s, p.chunk, p.inner, p.subbands);
+    b->chunk[i] = p.chunk;
+    b->inner[i] = p.inner;
+    if (chunk_out) chunk_out[i] = p.chunk;
+    if (inner_out) inner_out[i] = p.inner;
+    if (subbands_out) subbands_out[i] = p.subbands;
   }
-  return PSR_OK;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
 }
 
 int psr_batch_run(psr_batch *b) {

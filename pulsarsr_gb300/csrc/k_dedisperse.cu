@@ -18,7 +18,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cstring>
 #include <type_traits>
+#include <vector>
 
 #include "psr_internal.h"
 
@@ -319,6 +323,256 @@ __global__ void __launch_bounds__(DD_NT, 2)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Subband reuse (u8 samples, 16-bit lanes).  Channels are taken in subbands
+// of G adjacent channels.  For one block of SB_TB consecutive trials, the
+// delays of a subband's channels relative to its smallest delay form a
+// pattern; trials that share a pattern share the subband's partial series
+// up to a shift.  The plan (host, per block and subband) lists the distinct
+// patterns.  Stage A forms each pattern's partial sum over the tile (plus
+// the shift range) once in shared memory; stage B adds it, shifted, into
+// every trial that uses it.  A subband whose patterns do not repeat enough to
+// pay for stage A is added channel by channel (direct).  Every sum is an
+// integer below 2^16 in its lane, so the result is bit-identical to the
+// reference's channel-ordered f32 sum.
+constexpr int SB_TB = 8;    // trials per CTA
+constexpr int SB_PMAX = 4;  // patterns per subband held in shared memory
+constexpr int SB_GMAX = 8;
+
+struct SbEntry {
+  int32_t dref_min;               // smallest subband reference delay in the block
+  uint8_t npat, pad0, pad1, pad2;  // npat = 0: direct
+  uint8_t pid[SB_TB];             // pattern of each trial
+  uint16_t roff[SB_TB];           // reference delay - dref_min, per trial
+  uint16_t lo[SB_PMAX], hi[SB_PMAX];  // roff range of each pattern's trials
+  uint16_t rel[SB_PMAX][SB_GMAX];     // channel delay - reference delay
+};
+static_assert(sizeof(SbEntry) == 112, "plan entry layout");
+
+// acc (16-bit lanes: acc[i] = samples 2i | 2i+1 << 16) += the 16 bytes of
+// `row` starting at byte `off` (thread's own 16 samples: off includes 16 tl).
+__device__ __forceinline__ void add_bytes16(const uint4 *row16, int off, uint32_t *acc) {
+  const int q = off >> 4, o = off & 15;
+  const uint4 lo = row16[q], hi = row16[q + 1];
+  uint32_t w0 = lo.x, w1 = lo.y, w2 = lo.z, w3 = lo.w, w4 = hi.x, w5 = hi.y, w6 = hi.z,
+           w7 = hi.w;
+  if (o & 8) {
+    w0 = w2; w1 = w3; w2 = w4; w3 = w5; w4 = w6; w5 = w7;
+  }
+  if (o & 4) {
+    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5;
+  }
+  const unsigned sh = (unsigned)(o & 3) * 8u;
+  const uint32_t x0 = __funnelshift_r(w0, w1, sh), x1 = __funnelshift_r(w1, w2, sh),
+                 x2 = __funnelshift_r(w2, w3, sh), x3 = __funnelshift_r(w3, w4, sh);
+  acc[0] += __byte_perm(x0, 0, 0x4140);
+  acc[1] += __byte_perm(x0, 0, 0x4342);
+  acc[2] += __byte_perm(x1, 0, 0x4140);
+  acc[3] += __byte_perm(x1, 0, 0x4342);
+  acc[4] += __byte_perm(x2, 0, 0x4140);
+  acc[5] += __byte_perm(x2, 0, 0x4342);
+  acc[6] += __byte_perm(x3, 0, 0x4140);
+  acc[7] += __byte_perm(x3, 0, 0x4342);
+}
+
+// acc += 16 u16 samples of `pb` starting at sample j (any j >= 0).
+__device__ __forceinline__ void add_u16x16(const uint16_t *pb, int j, uint32_t *acc) {
+  const int w = j >> 1;  // first word
+  const uint4 *p4 = reinterpret_cast<const uint4 *>(pb) + (w >> 2);
+  const uint4 a = p4[0], b = p4[1], c = p4[2];
+  uint32_t x[12] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+  const int e = w & 3;  // words x[e .. e+8] are needed
+  if (e & 2) {
+#pragma unroll
+    for (int i = 0; i < 10; ++i) x[i] = x[i + 2];
+  }
+  if (e & 1) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) x[i] = x[i + 1];
+  }
+  const unsigned sh = (unsigned)(j & 1) * 16u;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc[i] += __funnelshift_r(x[i], x[i + 1], sh);
+}
+
+template <int G>
+__global__ void __launch_bounds__(DD_NT, 2)
+    k_dedisp_sb(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
+                uint64_t dstride, const uint32_t *__restrict__ delays, uint64_t ntrials,
+                uint64_t n, float *__restrict__ out, uint64_t ldo, double *__restrict__ part,
+                uint64_t ntiles, int cc, int rowcap, int accumulate, unsigned *err,
+                long long spin_limit, const SbEntry *__restrict__ plan, uint64_t nsub_total,
+                uint64_t sb0, uint64_t block0, int sbstride) {
+  static_assert(G <= SB_GMAX, "subband width");
+  extern __shared__ __align__(128) uint8_t smem[];
+  const size_t bstride = (size_t)cc * rowcap;
+  uint16_t *pbuf = reinterpret_cast<uint16_t *>(smem + 2 * bstride);
+  __shared__ uint64_t bars[2];
+  __shared__ StageInfo info[2];
+  __shared__ unsigned long long wsum[DD_NT / 32][SB_TB];
+  // the plan entries of each staged chunk's subbands, copied with its rows
+  __shared__ __align__(16) SbEntry ents[2][DD_MAXCC / 4];
+
+  const uint64_t t0 = (uint64_t)blockIdx.x * DD_TT;
+  const uint64_t d0 = (uint64_t)blockIdx.y * SB_TB;
+  const int tl = threadIdx.x;
+  const int nchunks = (int)((nch + cc - 1) / cc);
+  const SbEntry *pl = plan + (block0 + blockIdx.y) * nsub_total + sb0;
+
+  if (tl == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // Entries of chunk k: subbands [k cc / G, ...) of this block, contiguous in
+  // the plan; lane 0 copies them on the chunk's barrier before the rows'
+  // copies complete it.
+  auto stage_entries = [&](int k, int b) {
+    if (tl == 0) {
+      const uint64_t e0 = ((uint64_t)k * cc) / G;
+      const uint64_t ne = (min((uint64_t)cc, nch - (uint64_t)k * cc) + G - 1) / G;
+      const unsigned bytes = (unsigned)(ne * sizeof(SbEntry));
+      mbar_expect_tx(&bars[b], bytes);
+      bulk_g2s(&ents[b][0], pl + e0, bytes, &bars[b]);
+    }
+  };
+  if (tl < 32) {
+    stage_entries(0, 0);
+    issue_stage<SB_TB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, 0, cc, smem, rowcap,
+                       &info[0], &bars[0], 0);
+    if (nchunks > 1) {
+      stage_entries(1, 1);
+      issue_stage<SB_TB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)cc, cc,
+                         smem + bstride, rowcap, &info[1], &bars[1], 0);
+    }
+  }
+  uint32_t acc[SB_TB][8];
+#pragma unroll
+  for (int d = 0; d < SB_TB; ++d)
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[d][i] = 0;
+
+  int failed = -1;
+  bool pending = false;  // the pattern buffers hold partials some thread may still read
+  for (int k = 0; k < nchunks; ++k) {
+    const int b = k & 1;
+    const bool ok = mbar_wait_bounded(&bars[b], (unsigned)((k >> 1) & 1), err, spin_limit);
+    if (__syncthreads_or(!ok)) {
+      failed = k;
+      break;
+    }
+    const uint64_t c0 = (uint64_t)k * cc;
+    const int rows = (int)min((uint64_t)cc, (uint64_t)(nch - c0));
+    const uint8_t *buf = smem + b * bstride;
+    for (int j0 = 0; j0 < rows; j0 += G) {
+      const int gr = min(G, rows - j0);
+      const SbEntry &ent = ents[b][j0 / G];
+      const int npat = ent.npat;
+      if (npat == 0) {
+        for (int r = j0; r < j0 + gr; ++r) {
+          const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
+#pragma unroll
+          for (int d = 0; d < SB_TB; ++d) add_bytes16(row16, info[b].off[r][d] + 16 * tl, acc[d]);
+        }
+        continue;
+      }
+      // Stage A: pattern partials over [lo, hi + tile) of the reference delay,
+      // once every thread is done reading the previous subband's partials.
+      if (pending) __syncthreads();
+      for (int p = 0; p < npat; ++p) {
+        const int lo = ent.lo[p];
+        const int ngr = (DD_TT + (ent.hi[p] - lo) + 15) >> 4;
+        uint16_t *dst = pbuf + (size_t)p * sbstride;
+        for (int g = tl; g < ngr; g += DD_NT) {
+          uint32_t a[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          for (int r = 0; r < gr; ++r) {
+            const long long abs0 = (long long)t0 + ent.dref_min + lo + 16 * g + ent.rel[p][r];
+            const int off = (int)(abs0 - info[b].base[j0 + r]);
+            add_bytes16(reinterpret_cast<const uint4 *>(buf + (size_t)(j0 + r) * rowcap), off, a);
+          }
+          uint4 *d4 = reinterpret_cast<uint4 *>(dst + 16 * g);
+          d4[0] = make_uint4(a[0], a[1], a[2], a[3]);
+          d4[1] = make_uint4(a[4], a[5], a[6], a[7]);
+        }
+      }
+      __syncthreads();
+      // Stage B: every trial adds its pattern's partial at its shift.
+#pragma unroll
+      for (int d = 0; d < SB_TB; ++d) {
+        const int p = ent.pid[d];
+        add_u16x16(pbuf + (size_t)p * sbstride, ent.roff[d] - ent.lo[p] + 16 * tl, acc[d]);
+      }
+      pending = true;
+    }
+    __syncthreads();  // every thread is done reading buffer b (rows, entries, partials)
+    pending = false;
+    if (tl < 32 && k + 2 < nchunks) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      stage_entries(k + 2, b);
+      issue_stage<SB_TB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0,
+                         (uint64_t)(k + 2) * cc, cc, smem + b * bstride, rowcap, &info[b],
+                         &bars[b], 0);
+    }
+  }
+  if (failed >= 0) {
+    if (tl == 0) {
+      mbar_wait_bounded(&bars[failed & 1], (unsigned)((failed >> 1) & 1), err, spin_limit);
+      if (failed + 1 < nchunks)
+        mbar_wait_bounded(&bars[(failed + 1) & 1], (unsigned)(((failed + 1) >> 1) & 1), err,
+                          spin_limit);
+    }
+    return;
+  }
+
+  const uint64_t tb = t0 + (uint64_t)tl * DD_TPT;
+#pragma unroll
+  for (int d = 0; d < SB_TB; ++d) {
+    const uint64_t tr = d0 + d;
+    float v[16];
+    unsigned long long local = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      uint32_t lo = acc[d][i] & 0xffffu, hi = acc[d][i] >> 16;
+      bool in0 = tb + 2 * i < n, in1 = tb + 2 * i + 1 < n;
+      v[2 * i] = (float)lo;
+      v[2 * i + 1] = (float)hi;
+      local += (in0 ? lo : 0u) + (in1 ? hi : 0u);
+    }
+    if (tr < ntrials) {
+      float *dst = out + tr * ldo + tb;
+      if (tb + 16 <= n) {
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          float4 w = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+          if (accumulate) {
+            const float4 o = d4[i];
+            w.x += o.x;
+            w.y += o.y;
+            w.z += o.z;
+            w.w += o.w;
+          }
+          d4[i] = w;
+        }
+      } else {
+        for (int i = 0; i < 16; ++i)
+          if (tb + i < n) dst[i] = accumulate ? dst[i] + v[i] : v[i];
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((tl & 31) == 0) wsum[tl >> 5][d] = local;
+  }
+  __syncthreads();
+  if (tl < SB_TB && d0 + tl < ntrials) {
+    unsigned long long t = 0;
+    for (int w = 0; w < DD_NT / 32; ++w) t += wsum[w][tl];
+    double *pp = &part[(d0 + tl) * ntiles + blockIdx.x];
+    *pp = accumulate ? *pp + (double)t : (double)t;
+  }
+}
+
 // Reference-order f32 accumulation (one output per thread per trial).
 constexpr int DG_TPT = 4;
 constexpr int DG_NT = 256;
@@ -507,11 +761,178 @@ int launch_series_mean(const float *d_x, uint64_t n, double *d_sum, float *d_mea
 
 uint64_t series_ld(uint64_t n) { return ((n + 63) / 64) * 64; }
 
+// The subband kernel over channel groups (sums of a group stay below 2^16;
+// groups start at multiples of G).  PSR_EINVAL (no error recorded) when the
+// sample range or the shared memory does not fit this path.
+int launch_dedisperse_sb(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
+                         uint64_t n, float *d_out, uint64_t ldo, double *d_part,
+                         uint64_t max_spread, unsigned *d_err, cudaStream_t st, long long spin,
+                         const SubbandPlan &sb, uint64_t chunk_index) {
+  const int G = sb.G;
+  const double maxv = o.max_value();
+  const uint64_t gch = maxv > 0.0 ? (uint64_t)(65535.0 / maxv) : 0;
+  const uint64_t glen = std::min<uint64_t>((gch / G) * G, ((o.nch + G - 1) / G) * G);
+  if (glen < (uint64_t)G || (double)o.nch * maxv >= 16777216.0) return PSR_EINVAL;
+  const uint64_t ntiles = (n + DD_TT - 1) / DD_TT;
+  const int rowcap = (int)(((uint64_t)DD_TT + max_spread + 64 + 15) & ~(uint64_t)15);
+  const int sbstride = (int)(((uint64_t)DD_TT + max_spread + 40 + 7) & ~(uint64_t)7);
+  int dev = 0;
+  PSR_CUDA(cudaGetDevice(&dev));
+  int smax = 0, smsm = 0;
+  PSR_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  PSR_CUDA(cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  const size_t budget = std::min((size_t)smax, (size_t)smsm / 2) - 4096;
+  const size_t pbytes = (size_t)SB_PMAX * sbstride * 2;
+  if (budget <= pbytes) return PSR_EINVAL;
+  int cc = (int)std::min<uint64_t>((uint64_t)DD_MAXCC, (budget - pbytes) / (2 * (size_t)rowcap));
+  cc = (cc / G) * G;
+  if (cc < G) return PSR_EINVAL;
+  const size_t smem = 2 * (size_t)cc * rowcap + pbytes;
+  const SbEntry *plan = sb.entries.as<SbEntry>();
+  auto kern = G == 4 ? k_dedisp_sb<4> : k_dedisp_sb<8>;
+  if (G != 4 && G != 8) return PSR_EINVAL;
+  PSR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)ntiles, (unsigned)((ntrials + SB_TB - 1) / SB_TB));
+  for (uint64_t c0 = 0; c0 < o.nch; c0 += glen) {
+    const uint64_t ng = std::min(glen, o.nch - c0);
+    const int ccg = (int)std::min<uint64_t>((uint64_t)cc, ((ng + G - 1) / G) * G);
+    kern<<<grid, DD_NT, smem, st>>>(o.samples.as<uint8_t>() + c0 * o.ld, o.ld, o.ns, ng, o.nch,
+                                    d_delays + c0, ntrials, n, d_out, ldo, d_part, ntiles, ccg,
+                                    rowcap, c0 > 0 ? 1 : 0, d_err, spin, plan, sb.nsub, c0 / G,
+                                    sb.block0[chunk_index], sbstride);
+    PSR_CUDA(cudaGetLastError());
+  }
+  return PSR_OK;
+}
+
+namespace {
+std::atomic<int> g_subbands{-1};
+}
+int dedisp_subbands_default(const DeviceObs &o) {
+  const int g = g_subbands.load();
+  if (g >= 0) return g;
+  // Measured on a GB300: subbands of 8 save about 5% on 8-bit samples at
+  // 4096 channels but cost about 8% at 64-1024 channels; on <= 4-bit samples
+  // the byte-lane kernel is faster.  Batches tune it per shape class.
+  return o.kind == SAMPLE_U8 && o.h.nbits == 8 && o.nch >= 2048 ? 8 : 0;
+}
+
+// Cost of one (block, subband) in thread instructions per 16 samples, for
+// the choice between stage A/B and direct adds: a shifted 16-byte add is
+// about 33, a shifted 16-sample u16 add about 37, plus two barriers.
+bool subband_pays(int npat, int ge, int tbe) {
+  return npat * ge * 33 + tbe * 37 + 40 < tbe * ge * 33;
+}
+
+int build_subband_plan(const std::vector<uint32_t> &tab, uint64_t nch,
+                       const std::vector<uint64_t> &cstart, int G, SubbandPlan &plan,
+                       cudaStream_t st) {
+  plan.G = 0;
+  plan.nsub = 0;
+  plan.block0.clear();
+  plan.reused = plan.direct = 0;
+  if ((G != 4 && G != 8) || cstart.size() < 2) return PSR_OK;
+  const uint64_t nsub = (nch + G - 1) / G;
+  std::vector<uint64_t> block0;
+  uint64_t nblocks = 0;
+  for (size_t ci = 0; ci + 1 < cstart.size(); ++ci) {
+    block0.push_back(nblocks);
+    nblocks += (cstart[ci + 1] - cstart[ci] + SB_TB - 1) / SB_TB;
+  }
+  std::vector<SbEntry> ent(nblocks * nsub);
+  uint64_t nsb = 0, ndirect = 0;
+  for (size_t ci = 0; ci + 1 < cstart.size(); ++ci) {
+    const uint64_t ta = cstart[ci], tz = cstart[ci + 1];
+    for (uint64_t b = 0; ta + b * SB_TB < tz; ++b) {
+      const uint64_t tb0 = ta + b * SB_TB;
+      const int tbe = (int)std::min<uint64_t>(SB_TB, tz - tb0);
+      for (uint64_t j = 0; j < nsub; ++j) {
+        SbEntry e{};
+        const uint64_t ca = j * G;
+        const int ge = (int)std::min<uint64_t>(G, nch - ca);
+        uint32_t dref[SB_TB];
+        int32_t dmin = INT32_MAX, dmaxr = 0;
+        for (int d = 0; d < SB_TB; ++d) {
+          // trials past the chunk repeat its last trial, as the kernel's staging does
+          const uint64_t tr = tb0 + (uint64_t)std::min(d, tbe - 1);
+          uint32_t m = 0xffffffffu;
+          for (int c = 0; c < ge; ++c) m = std::min(m, tab[tr * nch + ca + c]);
+          dref[d] = m;
+          dmin = std::min(dmin, (int32_t)m);
+          dmaxr = std::max(dmaxr, (int32_t)m);
+        }
+        bool ok = dmaxr - dmin < 65536;
+        int npat = 0;
+        for (int d = 0; d < SB_TB && ok; ++d) {
+          const uint64_t tr = tb0 + (uint64_t)std::min(d, tbe - 1);
+          uint16_t rel[SB_GMAX] = {0};
+          for (int c = 0; c < ge; ++c) {
+            const uint32_t r = tab[tr * nch + ca + c] - dref[d];
+            if (r > 65535u) ok = false;
+            rel[c] = (uint16_t)r;
+          }
+          int p = 0;
+          while (p < npat && std::memcmp(e.rel[p], rel, sizeof(rel)) != 0) ++p;
+          if (p == npat) {
+            if (npat == SB_PMAX) {
+              ok = false;
+              break;
+            }
+            std::memcpy(e.rel[p], rel, sizeof(rel));
+            e.lo[p] = 0xffff;
+            e.hi[p] = 0;
+            ++npat;
+          }
+          const uint16_t ro = (uint16_t)(dref[d] - (uint32_t)dmin);
+          e.pid[d] = (uint8_t)p;
+          e.roff[d] = ro;
+          e.lo[p] = std::min(e.lo[p], ro);
+          e.hi[p] = std::max(e.hi[p], ro);
+        }
+        if (ok && subband_pays(npat, ge, tbe)) {
+          e.npat = (uint8_t)npat;
+          e.dref_min = dmin;
+          ++nsb;
+        } else {
+          e = SbEntry{};
+          ++ndirect;
+        }
+        ent[(block0[ci] + b) * nsub + j] = e;
+      }
+    }
+  }
+  PSR_TRY(plan.entries.ensure(ent.size() * sizeof(SbEntry)));
+  PSR_CUDA(cudaMemcpyAsync(plan.entries.p, ent.data(), ent.size() * sizeof(SbEntry),
+                           cudaMemcpyHostToDevice, st));
+  PSR_CUDA(cudaStreamSynchronize(st));
+  plan.G = G;
+  plan.nsub = nsub;
+  plan.block0 = block0;
+  plan.reused = nsb;
+  plan.direct = ndirect;
+  return PSR_OK;
+}
+
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part,
                          double *d_sums, float *d_means, uint64_t max_spread, unsigned *d_err,
-                         cudaStream_t st, long long spin_limit, int arm_only, bool want_means) {
+                         cudaStream_t st, long long spin_limit, int arm_only, bool want_means,
+                         const SubbandPlan *sb, uint64_t chunk_index) {
   const long long spin = spin_limit > 0 ? spin_limit : DD_SPIN_LIMIT;
+  if (sb && sb->G && !arm_only && o.kind == SAMPLE_U8 && chunk_index < sb->block0.size()) {
+    int rc = launch_dedisperse_sb(o, d_delays, ntrials, n, d_out, ldo, d_part, max_spread,
+                                  d_err, st, spin, *sb, chunk_index);
+    if (rc == PSR_OK) {
+      if (want_means) {
+        const uint64_t ntiles = (n + DD_TT - 1) / DD_TT;
+        k_reduce_parts<<<(unsigned)((ntrials + 127) / 128), 128, 0, st>>>(
+            d_part, ntiles, ntrials, n, d_sums, d_means, d_out, ldo, 0);
+        PSR_CUDA(cudaGetLastError());
+      }
+      return PSR_OK;
+    }
+    if (rc != PSR_EINVAL) return rc;  // EINVAL: this shape does not fit; take the kernels below
+  }
   // Integer samples: channel groups small enough that a group's sum fits the
   // 16-bit lanes (nch * max <= 65535 when there is one group); the groups'
   // sums are added in f32, exact while the total stays below 2^24.
@@ -599,3 +1020,12 @@ uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n) {
 }
 
 }  // namespace psr
+
+extern "C" int psr_set_dedisp_subbands(int subbands) {
+  if (subbands != -1 && subbands != 0 && subbands != 4 && subbands != 8) {
+    psr::set_error("set_dedisp_subbands: -1, 0, 4 or 8");
+    return PSR_EINVAL;
+  }
+  psr::g_subbands.store(subbands);
+  return PSR_OK;
+}

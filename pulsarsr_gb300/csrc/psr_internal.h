@@ -211,12 +211,31 @@ int make_delay_table(const DeviceObs &o, const double *trials, uint64_t ntrials,
 // (packed integer) kernel's waits give up after spin_limit polls (0 = the
 // default limit) and set *d_err; arm_only = 1 arms its barriers without
 // issuing the copies, so every wait runs out (a test of that path).
+// Subband-reuse plan of the staged dedispersion kernel for one DM plan
+// split into outer chunks (k_dedisperse.cu): per block of 8 consecutive
+// trials of a chunk and subband of G adjacent channels, the distinct
+// intra-subband delay patterns.  G = 0: no plan.
+struct SubbandPlan {
+  int G = 0;
+  uint64_t nsub = 0;
+  DevBuf entries;
+  std::vector<uint64_t> block0;  // first block of each outer chunk
+  uint64_t reused = 0, direct = 0;  // (block, subband) pairs by mode
+};
+// The subband width searches use when not told otherwise: the process-wide
+// setting of psr_set_dedisp_subbands, else the per-sample-kind default.
+int dedisp_subbands_default(const DeviceObs &o);
+int build_subband_plan(const std::vector<uint32_t> &tab, uint64_t nch,
+                       const std::vector<uint64_t> &cstart, int G, SubbandPlan &plan,
+                       cudaStream_t st);
 // With want_means = false (series only folded, not searched) the sums and
-// means are left unset.
+// means are left unset.  With a subband plan (8-bit-storage samples), chunk
+// chunk_index of the plan runs the subband-reuse kernel.
 int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t ntrials,
                          uint64_t n, float *d_out, uint64_t ldo, double *d_part, double *d_sums,
                          float *d_means, uint64_t max_spread, unsigned *d_err, cudaStream_t st,
-                         long long spin_limit = 0, int arm_only = 0, bool want_means = true);
+                         long long spin_limit = 0, int arm_only = 0, bool want_means = true,
+                         const SubbandPlan *sb = nullptr, uint64_t chunk_index = 0);
 uint64_t dedisperse_part_count(const DeviceObs &o, uint64_t n);
 // The f64 sum of a device series and the f32 mean search::periodicity
 // subtracts (search/src/lib.rs:36), bit-identical to the reference's

@@ -63,6 +63,8 @@ int SearchEngine::prepare(const DeviceObs &o, const double *trials, uint64_t ntr
   if (tail) cstart.push_back(ntrials - tail);
   cstart.push_back(ntrials);
   nchunks = cstart.size() - 1;
+  const int G = subbands >= 0 ? subbands : dedisp_subbands_default(o);
+  PSR_TRY(build_subband_plan(tab, o.nch, cstart, o.kind == SAMPLE_U8 ? G : 0, sbplan, st));
   PSR_TRY(chunk_overflow.ensure(nchunks * 4 + 16));
   if (!aux) PSR_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
   for (cudaEvent_t *e : {&ev_fft[0], &ev_fft[1], &ev_sel[0], &ev_sel[1]})
@@ -77,7 +79,7 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
   PSR_TRY(record(ST_DEDISP, true, st));
   PSR_TRY(launch_dedisperse_ex(o, delays.as<uint32_t>() + t0 * o.nch, nt, n, series.as<float>(),
                                ldo, parts.as<double>(), sums.as<double>(), means.as<float>(),
-                               max_spread, err.as<unsigned>(), st));
+                               max_spread, err.as<unsigned>(), st, 0, 0, true, &sbplan, ci));
   PSR_TRY(record(ST_DEDISP, false, st));
   // aux runs after everything st has queued so far (the previous chunk's
   // work is ordered on aux already), then resets the candidate queues.

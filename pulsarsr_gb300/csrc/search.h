@@ -11,6 +11,11 @@ struct SearchEngine {
   // within a 4 GB FFT work buffer).  0 = automatic.
   uint64_t chunk = 0;
   uint64_t inner = 0;
+  // Dedispersion subband width for 8-bit-storage samples: 0 = channel by
+  // channel, 4 or 8 = subband reuse, -1 = the library default
+  // (dedisp_subbands_default()).
+  int subbands = -1;
+  SubbandPlan sbplan;
   uint64_t ntrials = 0, n = 0, nch = 0, ldo = 0, ldp = 0, nparts = 0, nchunks = 0;
   // Outer chunk ci covers trials [cstart[ci], cstart[ci + 1]).  A search of
   // more than one chunk ends with a short chunk (chunk / 8 trials): the

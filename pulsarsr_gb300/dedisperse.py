@@ -80,3 +80,10 @@ def test_stage_timeout(fb: Filterbank, spin_limit: int = 1000) -> None:
     barriers are armed but never fed, so the bounded waits run out; raises
     WaitTimeout as a real give-up would."""
     check(lib().psr_test_stage_timeout(fb.handle, C.c_uint64(spin_limit)))
+
+
+def set_subbands(subbands: int) -> None:
+    """Process-wide dedispersion tuning for samples stored in 8 bits
+    (psr_set_dedisp_subbands): 0 = channel by channel, 4 or 8 = subband
+    reuse, -1 = the library default.  Results are identical either way."""
+    check(lib().psr_set_dedisp_subbands(C.c_int(subbands)))

@@ -254,6 +254,63 @@ def test_dedisperse_edge_shapes(gpu, oracle, nbits):
         assert out[i].tobytes() == d1[0, :4999].astype(np.float32).tobytes(), i
 
 
+@pytest.mark.parametrize("subbands", [0, 4, 8])
+@pytest.mark.parametrize("nbits,nch", [(4, 96), (8, 96), (8, 601), (2, 37)])
+def test_dedisperse_subband_reuse_matches_oracle(gpu, oracle, subbands, nbits, nch):
+    """Channel-by-channel and subband-reuse dedispersion (subbands of 4 or 8
+    channels, each distinct intra-subband delay pattern of 8 consecutive
+    trials summed once): bit-identical to the oracle for contiguous,
+    fine-stepped trial DMs (where patterns repeat), a count that is not a
+    multiple of 8, channel counts that are not multiples of the subband
+    width, and 601 8-bit channels (three channel groups)."""
+    from pulsarsr_gb300 import dedisperse, fbank, synth
+    mean, sigma = NOISE.get(nbits, (100., 10.))
+    o = synth.Observation(nchans=nch, nbits=nbits, nsamples=30000, tsamp=64e-6, fch1=1500.,
+                          foff=-300.0 / nch, seed=40 + nbits, noise_mean=mean, noise_sigma=sigma,
+                          pulsars=[synth.Pulsar(0.0123, 150.0, 0.04, 0.5)])
+    raw = o.to_bytes()
+    fb = fbank.decode(raw)
+    _, d = oracle.decode(raw)
+    freqs = fb.header.frequencies()
+    plan = dedisperse.plan(0, 400, dedisperse.dm_step(freqs, o.tsamp))
+    trials = np.concatenate([plan[100:145], plan[-21:]])
+    n = 30000 - int(dedisperse.delays(freqs, o.tsamp, trials.max()).max())
+    dedisperse.set_subbands(subbands)
+    try:
+        out, sums = dedisperse.apply_trials(fb, trials, n, with_sums=True)
+    finally:
+        dedisperse.set_subbands(-1)
+    for i, dm in enumerate(trials):
+        ref = oracle.apply(d, oracle.delays(freqs, o.tsamp, dm), n)
+        assert out[i].tobytes() == ref.tobytes(), (subbands, i)
+        assert sums[i] == float(np.add.accumulate(ref.astype(np.float64))[-1])
+
+
+@pytest.mark.parametrize("subbands", [0, 4])
+def test_search_subband_reuse_matches_oracle(gpu, oracle, subbands):
+    """The GBT-shaped search's first 256 trial DMs with either dedispersion:
+    candidate lists bit-identical to the oracle's."""
+    from pulsarsr_gb300 import dedisperse, fbank, rfi, search, synth
+    obs = synth.config_c2(2)
+    raw, trials, disc = search_case(obs, 500.0)
+    trials = trials[:256]
+    cfg = dict(min_hz=15.0, max_hz=2000.0, threshold=8.0, max_candidates=32)
+    block = max(int(0.1 / obs.tsamp), 32)
+    fb = fbank.decode(raw)
+    rfi.mask(fb, block, 8.0)
+    dedisperse.set_subbands(subbands)
+    try:
+        counts, cands = search.search_trials(fb, trials, disc, search.Config(**cfg))
+    finally:
+        dedisperse.set_subbands(-1)
+    _, d = oracle.decode(raw)
+    md, _ = oracle.rfi_mask(d, block, 8.0)
+    oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials, disc,
+                                      threads=THREADS, **cfg)
+    assert counts.tolist() == oc.tolist()
+    assert cands.tobytes() == ocands.tobytes()
+
+
 @pytest.mark.parametrize("nbits", [4, 8])
 def test_stage_wait_gives_up_and_context_recovers(gpu, oracle, nbits):
     """The staged dedispersion kernel's bounded TMA waits: with its barriers
