@@ -386,21 +386,60 @@ __global__ void __launch_bounds__(threads_for(M, 1))
   block_sum_store<NT>(acc, psum + trial);
 }
 
+// z[n] from a staged pair of series values (as load_z reads them).
+__device__ __forceinline__ float2 staged_z(float2 p, uint64_t len, uint64_t n, float mean) {
+  const uint64_t i0 = 2 * n;
+  if (i0 + 1 < len) return make_float2(__fsub_rn(p.x, mean), __fsub_rn(p.y, mean));
+  if (i0 < len) return make_float2(__fsub_rn(p.x, mean), 0.0f);
+  return make_float2(0.0f, 0.0f);
+}
+
+// 16-byte asynchronous global -> shared copy, cached in L2 only.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src)
+               : "memory");
+}
+
+// Copies the non-zero rows n1 < ceil(nz / M2) of column group n2_0 of `row`
+// into stg[n1 * C + c] (float pairs), 16 bytes per thread and step; chunks
+// starting at or past len are left alone (stage 0 never reads them).
+template <int M1, int M2>
+__device__ __forceinline__ void p1_stage_rows(float2 *stg, const float *__restrict__ row,
+                                              uint64_t len, uint32_t n2_0) {
+  constexpr int C = cols_for(M1), NT = threads_for(M1, C);
+  static_assert(C % 2 == 0, "16-byte chunks of complex pairs");
+  const uint64_t nz = (len + 1) / 2;
+  const int rows = (int)((nz + M2 - 1) / M2);
+  const int nchunk = rows * (C / 2);
+  for (int q = threadIdx.x; q < nchunk; q += NT) {
+    const int n1 = q / (C / 2), part = q % (C / 2);
+    const uint64_t f = 2 * ((uint64_t)n1 * M2 + n2_0) + 4 * (uint64_t)part;
+    if (f < len) cp_async16(stg + n1 * C + 2 * part, row + f);
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 // Pass 1 on one column group: C columns n2 in [n2_0, n2_0 + C) of trial
 // `row` (length M1 over n1), then W_M^(n2*k1), written to out[k1*M2 + n2].
-template <int M1, int M2>
+// stg (if not null) holds the group's non-zero rows (p1_stage_rows);
+// after_stage0() runs once every thread is done with stg.
+template <int M1, int M2, class Hook>
 __device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16 &c16,
                                          const float *__restrict__ row, uint64_t len,
                                          float mean, uint32_t n2_0,
                                          const float2 *__restrict__ tw1,
-                                         float2 *__restrict__ out) {
+                                         float2 *__restrict__ out, const float2 *stg,
+                                         Hook after_stage0) {
   constexpr int C = cols_for(M1), NT = threads_for(M1, C);
   constexpr int total = M1 * C;
   const uint64_t nz = (len + 1) / 2;  // complex inputs that can be non-zero
   {
-    // Stage 0 (radix 16, Ns = 1) straight from global memory: butterfly
-    // (col, j) takes positions j + r*M1/16 of its column and stores its
-    // outputs at 16j + r.  The zero padding (n >= nz) is never loaded.
+    // Stage 0 (radix 16, Ns = 1) straight from global memory (or the staged
+    // rows): butterfly (col, j) takes positions j + r*M1/16 of its column and
+    // stores its outputs at 16j + r.  The zero padding (n >= nz) is never
+    // loaded.
     constexpr int nb = M1 / 16;
     constexpr int nbt = nb * C;
     constexpr int BPT = (nbt + NT - 1) / NT;
@@ -410,10 +449,19 @@ __device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16
       if (nbt % NT == 0 || w < nbt) {
         const int col = w % C, j = w / C;
         float2 v[16];
+        if (stg) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) {
-          const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
-          v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+          for (int r = 0; r < 16; ++r) {
+            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+            v[r] = n < nz ? staged_z(stg[(j + r * nb) * C + col], len, n, mean)
+                          : make_float2(0.0f, 0.0f);
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            const uint64_t n = (uint64_t)(j + r * nb) * M2 + n2_0 + col;
+            v[r] = n < nz ? load_z(row, len, n, mean) : make_float2(0.0f, 0.0f);
+          }
         }
         dft16(v, c16);
         if constexpr (16 % C == 0) {
@@ -430,6 +478,7 @@ __device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16
     }
   }
   __syncthreads();
+  after_stage0();
   subfft_rest<M1, C, NT>(sm, Wl, c16);
   // W_M^(n2*k1) comes from a table laid out like the output, Tw1[k1*M2 +
   // n2] (values identical to the quarter-table lookup): reads coalesce.
@@ -490,7 +539,10 @@ __device__ __forceinline__ void p1_group(float2 *sm, const float2 *Wl, const W16
 // ...), builds the twiddle table once, and while it transforms one group
 // prefetches the next group's samples into L2 (one 64-byte run of C complex
 // inputs per row).
-template <int M1, int M2>
+// STAGED: the next group's non-zero rows are copied into shared memory
+// (cp.async) while the CTA transforms the current group, instead of
+// prefetched into L2, so stage 0 reads shared memory.
+template <int M1, int M2, bool STAGED>
 __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
     k_fft_pass1(const float *__restrict__ series, uint64_t lds, uint64_t len,
                 const float *__restrict__ means, const float2 *__restrict__ Q, int lq,
@@ -502,6 +554,16 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
   extern __shared__ float2 dyn[];
   float2 *Wl = dyn;       // M1 entries
   float2 *sm = dyn + M1;  // lay_slots<M1, C>() entries
+  // staged rows after sm, rounded up to 16 bytes (the launch adds one slot)
+  float2 *stg = STAGED ? reinterpret_cast<float2 *>(
+                             (reinterpret_cast<uintptr_t>(sm + lay_slots<M1, C>()) + 15) &
+                             ~(uintptr_t)15)
+                       : nullptr;
+  if constexpr (STAGED) {
+    if (blockIdx.x < ngroups)
+      p1_stage_rows<M1, M2>(stg, series + (uint64_t)(blockIdx.x / GPT) * lds, len,
+                            (blockIdx.x % GPT) * (uint32_t)C);
+  }
   build_wl<M1>(Wl, N, Q, lq);
   const uint64_t nz = (len + 1) / 2;
   __syncthreads();  // Wl
@@ -509,17 +571,26 @@ __global__ void __launch_bounds__(threads_for(M1, cols_for(M1)), 2)
   for (uint32_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
     const uint64_t trial = grp / GPT;
     const uint32_t n2_0 = (grp % GPT) * (uint32_t)C;
-    {
+    const uint32_t nx = grp + gridDim.x;
+    if constexpr (STAGED) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncthreads();  // this group's rows are in stg
+      p1_group<M1, M2>(sm, Wl, c16, series + trial * lds, len, means[trial], n2_0, tw1,
+                       work + trial * (uint64_t)M, stg, [&]() {
+                         if (nx < ngroups)
+                           p1_stage_rows<M1, M2>(stg, series + (uint64_t)(nx / GPT) * lds, len,
+                                                 (nx % GPT) * (uint32_t)C);
+                       });
+    } else {
       // (only inputs the next group loads: complex index < nz)
-      const uint32_t nx = grp + gridDim.x;
       const uint64_t pn = (uint64_t)threadIdx.x * M2 + (nx % GPT) * (uint32_t)C;
       if (nx < ngroups && pn < nz) {
         const float *pr = series + (uint64_t)(nx / GPT) * lds + 2 * pn;
         asm volatile("prefetch.global.L2 [%0];" ::"l"(pr));
       }
+      p1_group<M1, M2>(sm, Wl, c16, series + trial * lds, len, means[trial], n2_0, tw1,
+                       work + trial * (uint64_t)M, nullptr, []() {});
     }
-    p1_group<M1, M2>(sm, Wl, c16, series + trial * lds, len, means[trial], n2_0, tw1,
-                     work + trial * (uint64_t)M);
     __syncthreads();  // the next group's stage 0 overwrites sm
   }
 }
@@ -700,6 +771,10 @@ struct FftArgs {
   cudaStream_t st;
 };
 
+// Largest pass-1 dynamic shared memory that keeps two CTAs per SM with the
+// staged rows (GB300: 228 KB per SM, 1 KB reserved per CTA, static arrays).
+size_t g_pass1_stage_max = 110 * 1024;
+
 // SM count of the current device (cached per device).
 int sm_count(int &n) {
   static thread_local int dev_cached = -1, n_cached = 0;
@@ -729,14 +804,25 @@ int run_four_step(const FftArgs &a) {
   {
     constexpr int C = cols_for(M1);
     const size_t smem = (size_t)(M1 + lay_slots<M1, C>()) * sizeof(float2);
-    PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    const uint32_t ngroups = (uint32_t)(M2 / C) * (uint32_t)a.ntrials;
+    // staged rows: ceil(nz / M2) <= M1 / 2 rows of C complex values (plus the
+    // slot that aligns them to 16 bytes)
+    const uint64_t rows = ((a.len + 1) / 2 + M2 - 1) / M2;
+    const size_t smem_st = smem + (rows * C + 1) * sizeof(float2);
     int nsm = 0;
     PSR_TRY(sm_count(nsm));
+    const uint32_t ngroups = (uint32_t)(M2 / C) * (uint32_t)a.ntrials;
     const uint32_t grid = std::min<uint32_t>(ngroups, 2u * (uint32_t)nsm);
-    k_fft_pass1<M1, M2><<<grid, threads_for(M1, C), smem, a.st>>>(
-        a.series, a.lds, a.len, a.means, a.Q, a.lq, a.N, a.tw1, a.work, ngroups);
+    if (C % 2 == 0 && smem_st <= g_pass1_stage_max) {
+      PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_st));
+      k_fft_pass1<M1, M2, true><<<grid, threads_for(M1, C), smem_st, a.st>>>(
+          a.series, a.lds, a.len, a.means, a.Q, a.lq, a.N, a.tw1, a.work, ngroups);
+    } else {
+      PSR_CUDA(cudaFuncSetAttribute(k_fft_pass1<M1, M2, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_fft_pass1<M1, M2, false><<<grid, threads_for(M1, C), smem, a.st>>>(
+          a.series, a.lds, a.len, a.means, a.Q, a.lq, a.N, a.tw1, a.work, ngroups);
+    }
     PSR_CUDA(cudaGetLastError());
   }
   {
