@@ -261,7 +261,7 @@ int obs_from_bytes(const uint8_t *bytes, uint64_t len, int64_t limit, DeviceObs 
   PSR_TRY(o.payload.ensure(o.payload_bytes + 16));
   PSR_CUDA(cudaMemcpyAsync(o.payload.p, bytes + o.h.data_offset, o.payload_bytes,
                            cudaMemcpyHostToDevice, st));
-  PSR_TRY(o.alloc());
+  PSR_TRY(o.alloc(st));
   return PSR_OK;
 }
 
@@ -306,7 +306,7 @@ int obs_from_f32(const float *data, uint64_t nch, uint64_t ns, double tsamp, Dev
   o.ns = ns;
   o.nch = nch;
   o.kind = SAMPLE_F32;
-  PSR_TRY(o.alloc());
+  PSR_TRY(o.alloc(st));
   PSR_CUDA(cudaMemcpy2DAsync(o.samples.p, o.ld * 4, data, ns * 4, ns * 4, nch,
                              cudaMemcpyHostToDevice, st));
   return PSR_OK;
@@ -494,8 +494,8 @@ int psr_fb_read(const char *path, int64_t limit, psr_fb **out) {
   o.kind = kind_for_bits(o.h.nbits);
   o.payload_bytes = (ns * bpf + 7) / 8;
   PSR_TRY(o.payload.ensure(o.payload_bytes + 16));
-  PSR_TRY(o.alloc());
   cudaStream_t st = fb->stream.s;
+  PSR_TRY(o.alloc(st));
   constexpr uint64_t CHUNK = 64ull << 20;
   uint8_t *stage[2] = {nullptr, nullptr};
   cudaEvent_t done[2] = {nullptr, nullptr};
@@ -1198,7 +1198,7 @@ int session_create(const psr_header *header, uint64_t nsamples, const double *tr
   o.kind = kind_for_bits(header->nbits);
   o.payload_bytes = (nsamples * o.nch * (uint64_t)header->nbits + 7) / 8;
   PSR_TRY(o.payload.ensure(o.payload_bytes + 16));
-  PSR_TRY(o.alloc());
+  PSR_TRY(o.alloc(s->stream.s));
   s->rfi_block = rfi_block_samples;
   s->rfi_threshold = rfi_threshold;
   s->trials.assign(trials, trials + ntrials);

@@ -134,7 +134,7 @@ int synth_obs(const psr_synth_config &cfg, DeviceObs &o, cudaStream_t st) {
   o.ns = cfg.nsamples;
   o.nch = nch;
   o.kind = kind_for_bits(cfg.nbits);
-  PSR_TRY(o.alloc());
+  PSR_TRY(o.alloc(st));
   DevBuf dgain, dps, ddelay;
   PSR_TRY(dgain.ensure(nch * 4));
   PSR_TRY(dps.ensure(ps.size() * sizeof(SynthPulsarDev) + 16));

@@ -681,11 +681,13 @@ __global__ void k_fill(T *__restrict__ s, uint64_t ns, uint64_t ld, uint64_t bs,
 
 }  // namespace
 
-int DeviceObs::alloc() {
+int DeviceObs::alloc(cudaStream_t st) {
   ld = ((ns + 64 + 63) / 64) * 64;
   size_t bytes = (size_t)ld * nch * sample_bytes(kind) + 256;
   PSR_TRY(samples.ensure(bytes));
-  PSR_CUDA(cudaMemset(samples.p, 0, bytes));
+  // on the stream that fills the samples next: a plain cudaMemset runs on the
+  // legacy default stream, which does not order against non-blocking streams
+  PSR_CUDA(cudaMemsetAsync(samples.p, 0, bytes, st));
   return PSR_OK;
 }
 

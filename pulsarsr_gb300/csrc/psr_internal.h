@@ -111,7 +111,7 @@ struct DeviceObs {
   DevBuf samples;
   DevBuf payload;   // packed bytes as read (time-major)
   uint64_t payload_bytes = 0;
-  int alloc();      // samples for (nch, ns, kind)
+  int alloc(cudaStream_t st);  // samples for (nch, ns, kind), zeroed on st
   // Maximum sample value (integer kinds) used for exactness decisions.
   double max_value() const {
     if (kind == SAMPLE_U8) return (double)((1u << (h.nbits < 8 ? h.nbits : 8)) - 1);
