@@ -687,13 +687,29 @@ __device__ __forceinline__ void p2_group(float2 *sm, float2 *Wl, uint32_t N,
         float2 wk[PB];
         uint32_t kk[PB];
         int pp[PB], k2s[PB];
+        // Full groups: k2 = t / HC + u NT / HC with t / HC < NT / HC and
+        // 4 NT / HC = M2 / 2, so bin k = kb + p + M1 k2 (kb + p < M1 / 2) lies in
+        // the first quarter of the quarter-table's cycle for u < 4 and in the
+        // second for u >= 4: the quadrant rule of twN, fixed per u.
+        constexpr bool QFIX = HC > 0 && PB == 8 && 4 * (NT / (HC > 0 ? HC : 1)) == M2 / 2 &&
+                              (HC > 0 ? NT % HC == 0 : false) && M2 * HC == PB * NT;
 #pragma unroll
         for (int u = 0; u < PB; ++u) {
           const int idx = base + u * NT + (int)threadIdx.x;
           pp[u] = HC > 0 ? idx % HC : idx % hh;
           k2s[u] = HC > 0 ? idx / HC : idx / hh;
           kk[u] = kb + (uint32_t)pp[u] + M1 * (uint32_t)k2s[u];
-          wk[u] = idx < tot2 ? twN(Q, kk[u], lq) : make_float2(1.0f, 0.0f);
+          if constexpr (QFIX) {
+            if (u < 4) {
+              const float2 v = __ldg(&Q[kk[u]]);
+              wk[u] = make_float2(v.x, -v.y);
+            } else {
+              const float2 v = __ldg(&Q[kk[u] - (1u << lq)]);
+              wk[u] = make_float2(-v.y, -v.x);
+            }
+          } else {
+            wk[u] = idx < tot2 ? twN(Q, kk[u], lq) : make_float2(1.0f, 0.0f);
+          }
         }
 #pragma unroll
         for (int u = 0; u < PB; ++u) {
