@@ -307,6 +307,24 @@ __device__ __forceinline__ float post_power(float2 a, float2 zb, float2 w) {
   return __fadd_rn(__fmul_rn(xr, xr), __fmul_rn(xi, xi));
 }
 
+// Both bins of a mirrored pair at once: pk from a = zk, b = conj(zm) with
+// W_N^k = w, and pm from a = zm, b = conj(zk) with W_N^(M-k) = (-w.re, w.im).
+// The mirror's e, o and t are exactly (e.re, -e.im), (-o.re, o.im) and
+// (t.re, -t.im) (round to nearest is symmetric in sign and the fma products
+// are the same), so pm equals post_power(zm, zk, (-w.re, w.im)) bit for bit.
+__device__ __forceinline__ void post_power_pair(float2 zk, float2 zm, float2 w, float &pk,
+                                                float &pm) {
+  const float2 b = make_float2(zm.x, -zm.y);
+  const float2 e = cadd(zk, b), o = csub(zk, b);
+  const float2 t = cmul(o, w);
+  const float xr = __fmul_rn(0.5f, __fadd_rn(e.x, t.y));
+  const float xi = __fmul_rn(0.5f, __fsub_rn(e.y, t.x));
+  pk = __fadd_rn(__fmul_rn(xr, xr), __fmul_rn(xi, xi));
+  const float yr = __fmul_rn(0.5f, __fsub_rn(e.x, t.y));
+  const float yi = __fmul_rn(0.5f, __fadd_rn(e.y, t.x));  // -(mirror's xi)
+  pm = __fadd_rn(__fmul_rn(yr, yr), __fmul_rn(yi, yi));
+}
+
 __device__ __forceinline__ float2 load_z(const float *__restrict__ row, uint64_t len, uint64_t n,
                                          float mean) {
   const uint64_t i0 = 2 * n;
@@ -718,8 +736,8 @@ __device__ __forceinline__ void p2_group(float2 *sm, float2 *Wl, uint32_t N,
             const uint32_t k = kk[u];
             const float2 zk = sm[lay<C>(k2s[u], pp[u])];
             const float2 zm = sm[lay<C>(M2 - 1 - k2s[u], hh + pp[u])];
-            const float pk = post_power(zk, zm, wk[u]);
-            const float pm = post_power(zm, zk, make_float2(-wk[u].x, wk[u].y));
+            float pk, pm;
+            post_power_pair(zk, zm, wk[u], pk, pm);
             out[k] = pk;
             out[M - k] = pm;
             acc.add(pk);
