@@ -7,11 +7,12 @@
 // reference's channel-ordered f32 sum is exact and any summation order gives
 // the bit-identical value.  The fast kernel stages a tile of every channel
 // row into shared memory with TMA bulk copies (cp.async.bulk + mbarrier,
-// double buffered), and each thread accumulates 16 consecutive samples for a
-// block of trials in packed 2 x u16 lanes (samples of <= 4 bits first in
-// 4 x u8 lanes, widened once per group of channels).  Consecutive trials whose
-// delay for a channel is unchanged reuse the aligned sample words
-// (warp-uniform test).
+// double buffered), and each thread accumulates four sample words (16
+// samples, words tl + 256 k of the tile) for a block of trials in packed
+// 2 x u16 lanes (samples of <= 4 bits first in 4 x u8 lanes, widened once per
+// group of channels).  Consecutive trials whose delay for a channel falls in
+// the same aligned word reuse the loaded words (CTA-uniform test) and only
+// shift them again.
 //
 // Everything else (f32 samples, or integer sums that could exceed 2^16) uses
 // a kernel that adds channels in reference order in f32.
@@ -33,7 +34,7 @@ constexpr int DD_NT = 256;              // threads per CTA
 constexpr int DD_TPT = 16;              // samples per thread
 constexpr int DD_TT = DD_NT * DD_TPT;   // samples per tile (4096)
 constexpr int DD_DB = 8;                // trials per CTA (16-bit lanes only)
-constexpr int DD_DB8 = 6;               // trials per CTA with 8-bit lanes (registers)
+constexpr int DD_DB8 = 8;               // trials per CTA with 8-bit lanes (128 registers)
 constexpr int DD_MAXCC = 32;            // rows per stage (one issuing lane each)
 constexpr long long DD_SPIN_LIMIT = 1ll << 26;  // try_wait polls before a wait gives up
 
@@ -205,31 +206,39 @@ __global__ void __launch_bounds__(DD_NT, 2)
     const int rows = (int)min((uint64_t)cc, (uint64_t)(nch - c0));
     const uint8_t *buf = smem + b * bstride;
     for (int r = 0; r < rows; ++r) {
-      const uint4 *row16 = reinterpret_cast<const uint4 *>(buf + (size_t)r * rowcap);
+      // Thread tl owns words tl + 256 k (k < 4) of the tile.  A trial's row
+      // offset `off` (bytes, CTA-uniform) selects words w = off >> 2 onward,
+      // shifted right by (off & 3) bytes.  Delays grow by 0 or 1 sample from
+      // one trial to the next, so consecutive trials mostly share w: the
+      // loaded words are kept and only re-shifted.
+      const uint32_t *row = reinterpret_cast<const uint32_t *>(buf + (size_t)r * rowcap) + tl;
       const int *offs = info[b].off[r];
-      int prev = -1;
+      int poff = -1, pw = -1;
+      uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
       uint32_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
 #pragma unroll
       for (int d = 0; d < DB; ++d) {
         const int off = offs[d];  // shared-memory broadcast
-        if (off != prev) {  // uniform across the CTA
-          prev = off;
-          const int q = tl + (off >> 4);
-          const int o = off & 15;
-          uint4 lo = row16[q], hi = row16[q + 1];
-          uint32_t w0 = lo.x, w1 = lo.y, w2 = lo.z, w3 = lo.w, w4 = hi.x, w5 = hi.y, w6 = hi.z,
-                   w7 = hi.w;
-          if (o & 8) {
-            w0 = w2; w1 = w3; w2 = w4; w3 = w5; w4 = w6; w5 = w7;
+        if (off != poff) {  // uniform across the CTA
+          poff = off;
+          const int w = off >> 2;
+          if (w != pw) {
+            pw = w;
+            const uint32_t *p = row + w;
+            a0 = p[0];
+            b0 = p[1];
+            a1 = p[256];
+            b1 = p[257];
+            a2 = p[512];
+            b2 = p[513];
+            a3 = p[768];
+            b3 = p[769];
           }
-          if (o & 4) {
-            w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5;
-          }
-          const unsigned sh = (unsigned)(o & 3) * 8u;
-          x0 = __funnelshift_r(w0, w1, sh);
-          x1 = __funnelshift_r(w1, w2, sh);
-          x2 = __funnelshift_r(w2, w3, sh);
-          x3 = __funnelshift_r(w3, w4, sh);
+          const unsigned sh = (unsigned)(off & 3) * 8u;
+          x0 = __funnelshift_r(a0, b0, sh);
+          x1 = __funnelshift_r(a1, b1, sh);
+          x2 = __funnelshift_r(a2, b2, sh);
+          x3 = __funnelshift_r(a3, b3, sh);
         }
         if constexpr (BYTE_LANES) {
           acc8[d][0] += x0;
@@ -273,41 +282,43 @@ __global__ void __launch_bounds__(DD_NT, 2)
     return;
   }
 
-  const uint64_t tb = t0 + (uint64_t)tl * DD_TPT;
+  // Word k of this thread holds samples t0 + 4 (tl + 256 k) + {0, 1, 2, 3}:
+  // acc[d][2k] their first two (16-bit lanes), acc[d][2k + 1] the last two.
 #pragma unroll
   for (int d = 0; d < DB; ++d) {
     const uint64_t tr = d0 + d;
-    float v[16];
     unsigned long long local = 0;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      uint32_t lo = acc[d][i] & 0xffffu, hi = acc[d][i] >> 16;
-      bool in0 = tb + 2 * i < n, in1 = tb + 2 * i + 1 < n;
-      v[2 * i] = (float)lo;
-      v[2 * i + 1] = (float)hi;
-      local += (in0 ? lo : 0u) + (in1 ? hi : 0u);
-    }
-    if (tr < ntrials) {
-      // Channel groups after the first add their (integer) partial sums to
-      // the earlier groups' in f32: exact while every sum stays below 2^24.
-      float *dst = out + tr * ldo + tb;
-      if (tb + 16 <= n) {
-        float4 *d4 = reinterpret_cast<float4 *>(dst);
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t tb = t0 + 4 * ((uint64_t)tl + 256 * k);
+      const uint32_t p = acc[d][2 * k], q = acc[d][2 * k + 1];
+      const float v[4] = {(float)(p & 0xffffu), (float)(p >> 16), (float)(q & 0xffffu),
+                          (float)(q >> 16)};
+      if (tb + 4 <= n) {
+        local += (p & 0xffffu) + (p >> 16) + (q & 0xffffu) + (q >> 16);
+      } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          float4 w = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        for (int i = 0; i < 4; ++i)
+          if (tb + i < n) local += (unsigned)v[i];
+      }
+      if (tr < ntrials) {
+        // Channel groups after the first add their (integer) partial sums to
+        // the earlier groups' in f32: exact while every sum stays below 2^24.
+        float *dst = out + tr * ldo + tb;
+        if (tb + 4 <= n) {
+          float4 w = make_float4(v[0], v[1], v[2], v[3]);
           if (accumulate) {
-            const float4 o = d4[i];
+            const float4 o = *reinterpret_cast<const float4 *>(dst);
             w.x += o.x;
             w.y += o.y;
             w.z += o.z;
             w.w += o.w;
           }
-          d4[i] = w;
+          *reinterpret_cast<float4 *>(dst) = w;
+        } else {
+          for (int i = 0; i < 4; ++i)
+            if (tb + i < n) dst[i] = accumulate ? dst[i] + v[i] : v[i];
         }
-      } else {
-        for (int i = 0; i < 16; ++i)
-          if (tb + i < n) dst[i] = accumulate ? dst[i] + v[i] : v[i];
       }
     }
 #pragma unroll
