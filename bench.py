@@ -270,6 +270,14 @@ def run_ours(args):
         s.run()
         s.sync()
     st = s.stage_times()
+    # The same with the stages serialised: each stage's kernels alone.
+    s.set_profiling(2)
+    s.stage_times(reset=True)
+    for _ in range(2):
+        rt.cudaMemsetAsync(flush, C.c_int(0), C.c_size_t(FLUSH), C.c_void_p(stream))
+        s.run()
+        s.sync()
+    st_iso = s.stage_times()
     s.set_profiling(False)
     N = 2 * (1 << (discovery - 1).bit_length())
     # The dominant kernels are the rFFT stage's (k_fft_pass1 + k_fft_pass2, one
@@ -283,10 +291,13 @@ def run_ours(args):
             continue
         ms_search = tot_ms / 2
         nbytes = stage_bytes(k, obs, trials, discovery, N, masked_fraction=mfrac)
+        iso = st_iso[k][0] / 2
         stages[k] = {"ms_per_search": round(ms_search, 4), "event_pairs_per_search": nl // 2,
                      "ms_per_event_pair": round(tot_ms / nl, 5),
                      "algorithmic_gb": round(nbytes / 1e9, 4),
-                     "gbs": round(nbytes / (ms_search / 1e3) / 1e9, 1)}
+                     "gbs": round(nbytes / (ms_search / 1e3) / 1e9, 1),
+                     "ms_per_search_serialised": round(iso, 4),
+                     "gbs_serialised": round(nbytes / (iso / 1e3) / 1e9, 1) if iso else None}
     # Dedispersion against its ALU bound: sample-adds (nch per DM-trial*sample)
     # packed 4 per 32-bit add for <= 4-bit samples (byte lanes), 2 otherwise
     # (16-bit lanes), against 128 32-bit integer adds per clock per SM at the
@@ -298,8 +309,10 @@ def run_ours(args):
         lanes = 4 if obs.nbits <= 4 else 2
         word_adds = obs.nchans * len(trials) * discovery / lanes
         dd_s = stages["dedisperse"]["ms_per_search"] / 1e3
+        dd_iso = stages["dedisperse"]["ms_per_search_serialised"] / 1e3
         peak_adds = nsm.value * 128 * mhz * 1e6
         stages["dedisperse"]["issue_frac"] = round(word_adds / dd_s / peak_adds, 4)
+        stages["dedisperse"]["issue_frac_serialised"] = round(word_adds / dd_iso / peak_adds, 4)
         stages["dedisperse"]["issue_basis"] = (
             f"{obs.nchans} x {len(trials)} x {discovery} sample-adds / {lanes} per 32-bit add "
             f"vs {nsm.value} SMs x 128 int32 adds/clk x {mhz:.0f} MHz")

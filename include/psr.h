@@ -479,9 +479,13 @@ int psr_session_mask(psr_session *s, uint64_t *channels, uint64_t *nchannels_bad
                      double *masked_fraction);
 /* Diagnostics with no counterpart in the reference (which only times whole
  * runs, cli/src/main.rs:415): when enabled, run() records CUDA events around
- * every stage on the session stream.  stage_times() fills ms[5] and
- * launches[5] for (unpack, rfi, dedisperse, fft, spectrum), summed over the
- * runs since the last reset. */
+ * every stage on the session stream.  enable 1: the stages overlap as in an
+ * unprofiled run (the spectrum stage of a chunk beside the next chunk's
+ * dedispersion and FFT); 2: serialised, each chunk's dedispersion waits for
+ * the previous chunk's spectrum stage, so each stage's time is its own
+ * kernels' alone.  stage_times() fills ms[5] and launches[5] for (unpack,
+ * rfi, dedisperse, fft, spectrum), summed over the runs since the last
+ * reset. */
 int psr_session_set_profiling(psr_session *s, int enable);
 int psr_session_stage_times(psr_session *s, double *ms, uint64_t *launches, int reset);
 /* confirmation::analyze over the last run's candidates (the psr search

@@ -1273,7 +1273,11 @@ int psr_session_set_profiling(psr_session *s, int enable) {
     set_error("session_set_profiling: null handle");
     return PSR_EINVAL;
   }
-  s->eng.profile = enable != 0;
+  if (enable < 0 || enable > 2) {
+    set_error("session_set_profiling: 0, 1 or 2");
+    return PSR_EINVAL;
+  }
+  s->eng.profile = enable;
   return PSR_OK;
 }
 

@@ -88,7 +88,9 @@ struct StageInfo {
 };
 
 // Issue the TMA copies of rows [c0, c0+cc) for trials [d0, d0+DB) of tile t0.
-// Run by warp 0: lane i stages row c0+i.
+// Run by warp 0: lane i stages row c0+i.  The delay of trial d0 + d and
+// channel c is delays[min(d0 + d, ntrials - 1) * dstride + c] (global memory,
+// or the CTA's block preloaded in shared memory with d0 = 0, ntrials = DB).
 template <int DB>
 __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns,
                             uint64_t nch, uint64_t dstride, const uint32_t *__restrict__ delays,
@@ -134,7 +136,7 @@ __device__ void issue_stage(const uint8_t *__restrict__ s, uint64_t ld, uint64_t
 // summed in the four 8-bit lanes of a 32-bit word with a plain IADD (no lane
 // overflows, so no carry crosses a byte); the byte lanes are widened into the
 // 16-bit lanes once per group.  Without BYTE_LANES every channel is widened.
-template <bool BYTE_LANES, int DB>
+template <bool BYTE_LANES, int DB, bool PRELOAD>
 __global__ void __launch_bounds__(DD_NT, 2)
     k_dedisp_u8(const uint8_t *__restrict__ s, uint64_t ld, uint64_t ns, uint64_t nch,
                 uint64_t dstride, const uint32_t *__restrict__ delays, uint64_t ntrials,
@@ -152,6 +154,28 @@ __global__ void __launch_bounds__(DD_NT, 2)
   const int tl = threadIdx.x;
   const int nchunks = (int)((nch + cc - 1) / cc);
 
+  // preload: the CTA's [DB][nch] block of delays is copied once into shared
+  // memory after the row buffers, so that issuing a stage (between chunks,
+  // while the other warps wait at the barrier) reads no global memory.
+  auto issue = [&](int k, int b) {
+    if constexpr (PRELOAD)
+      issue_stage<DB>(s, ld, ns, nch, nch,
+                      reinterpret_cast<const uint32_t *>(smem + 2 * bstride), DB, 0, t0,
+                      (uint64_t)k * cc, cc, smem + b * bstride, rowcap, &info[b], &bars[b],
+                      arm_only);
+    else
+      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)k * cc, cc,
+                      smem + b * bstride, rowcap, &info[b], &bars[b], arm_only);
+  };
+  if constexpr (PRELOAD) {
+    uint32_t *dly = reinterpret_cast<uint32_t *>(smem + 2 * bstride);
+    const unsigned nc = (unsigned)nch;  // <= 4096 when the block is preloaded
+    for (unsigned i = tl; i < DB * nc; i += DD_NT) {
+      const unsigned d = i / nc, c = i - d * nc;
+      const uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
+      dly[i] = delays[tr * dstride + c];
+    }
+  }
   if (tl == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
@@ -159,11 +183,8 @@ __global__ void __launch_bounds__(DD_NT, 2)
   }
   __syncthreads();
   if (tl < 32) {
-    issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, 0, cc, smem, rowcap,
-                    &info[0], &bars[0], arm_only);
-    if (nchunks > 1)
-      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)cc, cc,
-                      smem + bstride, rowcap, &info[1], &bars[1], arm_only);
+    issue(0, 0);
+    if (nchunks > 1) issue(1, 1);
   }
 
   uint32_t acc[DB][8];
@@ -210,21 +231,27 @@ __global__ void __launch_bounds__(DD_NT, 2)
       // offset `off` (bytes, CTA-uniform) selects words w = off >> 2 onward,
       // shifted right by (off & 3) bytes.  Delays grow by 0 or 1 sample from
       // one trial to the next, so consecutive trials mostly share w: the
-      // loaded words are kept and only re-shifted.
+      // loaded words are kept and only re-shifted.  Lane d < DB reads trial
+      // d's offset; the ballots of "offset changed" and "word changed"
+      // against trial d - 1 are warp-uniform bit masks and the offsets are
+      // broadcast by shuffles, so every branch below is uniform by
+      // construction.
       const uint32_t *row = reinterpret_cast<const uint32_t *>(buf + (size_t)r * rowcap) + tl;
-      const int *offs = info[b].off[r];
-      int poff = -1, pw = -1;
+      const int lane = tl & 31;
+      const int myoff = info[b].off[r][lane < DB ? lane : DB - 1];
+      const int prevoff = __shfl_up_sync(0xffffffffu, myoff, 1);
+      const unsigned chg =
+          __ballot_sync(0xffffffffu, lane < DB && (lane == 0 || myoff != prevoff));
+      const unsigned wchg =
+          __ballot_sync(0xffffffffu, lane < DB && (lane == 0 || (myoff >> 2) != (prevoff >> 2)));
       uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
       uint32_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
 #pragma unroll
       for (int d = 0; d < DB; ++d) {
-        const int off = offs[d];  // shared-memory broadcast
-        if (off != poff) {  // uniform across the CTA
-          poff = off;
-          const int w = off >> 2;
-          if (w != pw) {
-            pw = w;
-            const uint32_t *p = row + w;
+        if (chg & (1u << d)) {
+          const int off = __shfl_sync(0xffffffffu, myoff, d);
+          if (wchg & (1u << d)) {
+            const uint32_t *p = row + (off >> 2);
             a0 = p[0];
             b0 = p[1];
             a1 = p[256];
@@ -264,8 +291,7 @@ __global__ void __launch_bounds__(DD_NT, 2)
     __syncthreads();  // every thread is done reading buffer b
     if (tl < 32 && k + 2 < nchunks) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue_stage<DB>(s, ld, ns, nch, dstride, delays, ntrials, d0, t0, (uint64_t)(k + 2) * cc,
-                      cc, smem + b * bstride, rowcap, &info[b], &bars[b], arm_only);
+      issue(k + 2, b);
     }
   }
   widen();
@@ -962,31 +988,38 @@ int launch_dedisperse_ex(const DeviceObs &o, const uint32_t *d_delays, uint64_t 
     PSR_CUDA(cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     size_t budget = std::min((size_t)smax, (size_t)smsm / 2) - 4096;
     const uint64_t glen = std::min<uint64_t>(gch, o.nch);
+    // The CTA's delay block ([trials per CTA][channels of the group], u32) is
+    // preloaded into shared memory when it takes at most 16 KB.
+    const int group = (int)(255.0 / maxv);
+    const size_t dly_bytes = (size_t)(group >= 2 ? DD_DB8 : DD_DB) * glen * 4;
+    const int preload = dly_bytes <= 16384 && dly_bytes + 2 * (size_t)rowcap <= budget;
+    if (preload) budget -= dly_bytes;
     int cc = (int)std::min<uint64_t>({(uint64_t)DD_MAXCC, glen, budget / (2 * (size_t)rowcap)});
     if (cc >= 1) {
-      size_t smem = 2 * (size_t)cc * rowcap;
-      const int group = (int)(255.0 / maxv);
+      size_t smem = 2 * (size_t)cc * rowcap + (preload ? dly_bytes : 0);
       for (uint64_t c0 = 0; c0 < o.nch; c0 += glen) {
         const uint64_t ng = std::min(glen, o.nch - c0);
         const uint8_t *sg = o.samples.as<uint8_t>() + c0 * o.ld;
         const uint32_t *dg = d_delays + c0;
         const int acc = c0 > 0 ? 1 : 0;
         const int ccg = (int)std::min<uint64_t>((uint64_t)cc, ng);
-        if (group >= 2) {
-          dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB8 - 1) / DD_DB8));
-          PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<true, DD_DB8>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-          k_dedisp_u8<true, DD_DB8><<<grid, DD_NT, smem, st>>>(
-              sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo, d_part, ntiles, ccg, rowcap,
-              group, acc, d_err, spin, arm_only);
-        } else {
-          dim3 grid((unsigned)ntiles, (unsigned)((ntrials + DD_DB - 1) / DD_DB));
-          PSR_CUDA(cudaFuncSetAttribute(k_dedisp_u8<false, DD_DB>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-          k_dedisp_u8<false, DD_DB><<<grid, DD_NT, smem, st>>>(
-              sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo, d_part, ntiles, ccg, rowcap,
-              1, acc, d_err, spin, arm_only);
-        }
+        auto run = [&](auto kern, int db, int grp) -> int {
+          dim3 grid((unsigned)ntiles, (unsigned)((ntrials + db - 1) / db));
+          PSR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+          kern<<<grid, DD_NT, smem, st>>>(sg, o.ld, o.ns, ng, o.nch, dg, ntrials, n, d_out, ldo,
+                                          d_part, ntiles, ccg, rowcap, grp, acc, d_err, spin,
+                                          arm_only);
+          return PSR_OK;
+        };
+        int rc;
+        if (group >= 2)
+          rc = preload ? run(k_dedisp_u8<true, DD_DB8, true>, DD_DB8, group)
+                       : run(k_dedisp_u8<true, DD_DB8, false>, DD_DB8, group);
+        else
+          rc = preload ? run(k_dedisp_u8<false, DD_DB, true>, DD_DB, 1)
+                       : run(k_dedisp_u8<false, DD_DB, false>, DD_DB, 1);
+        if (rc != PSR_OK) return rc;
         PSR_CUDA(cudaGetLastError());
       }
       if (want_means) {

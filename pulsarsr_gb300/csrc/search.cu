@@ -118,6 +118,7 @@ int SearchEngine::enqueue_chunk(const DeviceObs &o, uint64_t ci, cudaStream_t st
                            cudaMemcpyDeviceToDevice, aux));
   PSR_CUDA(cudaEventRecord(ev_sel[b], aux));
   sel_pending[b] = true;
+  if (profile == 2) PSR_CUDA(cudaStreamWaitEvent(st, ev_sel[b], 0));
   return PSR_OK;
 }
 

@@ -27,9 +27,12 @@ struct SearchEngine {
   SpecConfig spec;
   SpecWork sw;
   // Optional per-stage timing: events recorded around every stage launch on
-  // the engine's stream; stage_ms accumulates their elapsed times.
+  // the engine's stream; stage_ms accumulates their elapsed times.  profile
+  // 1: stages overlap as in an untimed run; 2: serialised, each chunk's
+  // dedispersion waits for the previous chunk's spectrum work, so every
+  // stage's time is its kernels' own (no SMs shared with the other stream).
   enum { ST_DEDISP = 0, ST_FFT = 1, ST_SPEC = 2, ST_COUNT = 3 };
-  bool profile = false;
+  int profile = 0;
   std::vector<cudaEvent_t> ev_begin[ST_COUNT], ev_end[ST_COUNT];
   double stage_ms[ST_COUNT] = {0, 0, 0};
   uint64_t stage_launches[ST_COUNT] = {0, 0, 0};

@@ -76,8 +76,10 @@ class SearchSession:
 
     STAGES = ("unpack", "rfi", "dedisperse", "fft", "spectrum")
 
-    def set_profiling(self, enable: bool) -> None:
-        check(lib().psr_session_set_profiling(self._s, C.c_int(1 if enable else 0)))
+    def set_profiling(self, enable) -> None:
+        """False/0: off; True/1: stage events, stages overlapping as usual;
+        2: stage events with the stages serialised (each stage's own time)."""
+        check(lib().psr_session_set_profiling(self._s, C.c_int(int(enable))))
 
     def stage_times(self, reset: bool = False) -> dict:
         ms = np.zeros(5, dtype=np.float64)

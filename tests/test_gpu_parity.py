@@ -207,12 +207,17 @@ def test_dedisperse_matches_oracle(gpu, oracle, nbits):
         assert out[i].tobytes() == ref.tobytes(), i
 
 
-def test_dedisperse_many_channels_8bit_groups(gpu, oracle):
+@pytest.mark.parametrize("nbits,nch", [(8, 600), (4, 700)])
+def test_dedisperse_many_channels(gpu, oracle, nbits, nch):
     """600 channels of 8-bit data: the packed kernel runs in channel groups of
-    257 whose sums are added in f32 (exact below 2^24)."""
+    257 whose sums are added in f32 (exact below 2^24).  700 channels of 4-bit
+    data: one group whose per-CTA delay block (8 trials x 700 channels) is too
+    large to preload into shared memory, so stages read the delays from
+    global memory."""
     from pulsarsr_gb300 import dedisperse, fbank, synth
-    o = synth.Observation(nchans=600, nbits=8, nsamples=20000, tsamp=64e-6, fch1=1600.,
-                          foff=-400.0 / 600, seed=12, noise_mean=120., noise_sigma=40.,
+    mean, sigma = NOISE.get(nbits, (120., 40.))
+    o = synth.Observation(nchans=nch, nbits=nbits, nsamples=20000, tsamp=64e-6, fch1=1600.,
+                          foff=-400.0 / nch, seed=12, noise_mean=mean, noise_sigma=sigma,
                           pulsars=[synth.Pulsar(0.0123, 150.0, 0.04, 0.5)])
     raw = o.to_bytes()
     fb = fbank.decode(raw)
@@ -608,20 +613,28 @@ def test_session_pipeline_matches_oracle(gpu, oracle):
     cfg = search.Config(min_hz=15.0, max_hz=2000.0, threshold=8.0)
     block = max(int(0.1 / obs.tsamp), 32)
     s = session.SearchSession(hdr, obs.nsamples, trials, disc, cfg, block, 8.0)
-    for _ in range(2):  # a second run on the same buffers gives the same answer
+    _, d = oracle.decode(raw)
+    md, om = oracle.rfi_mask(d, block, 8.0)
+    oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials, disc,
+                                      threads=THREADS, min_hz=15.0, max_hz=2000.0,
+                                      threshold=8.0, max_candidates=32)
+    # Runs on the same buffers give the same answer, also with stage events
+    # (1) and with the stages serialised for timing (2).
+    for prof in (0, 1, 2):
+        s.set_profiling(prof)
+        s.stage_times(reset=True)
         s.load(raw[hdr.data_offset:])
         s.run()
         s.sync()
+        st = s.stage_times()
+        assert all(st[k][1] > 0 for k in ("dedisperse", "fft", "spectrum")) == (prof > 0)
         counts, cands = s.candidates()
         mask = s.mask()
-        _, d = oracle.decode(raw)
-        md, om = oracle.rfi_mask(d, block, 8.0)
         assert (mask["channels"], mask["blocks"]) == (om["channels"], om["blocks"])
-        oc, ocands = oracle.search_trials(md, obs.frequencies(), obs.tsamp, trials, disc,
-                                          threads=THREADS, min_hz=15.0, max_hz=2000.0,
-                                          threshold=8.0, max_candidates=32)
         assert counts.tolist() == oc.tolist()
         assert cands.tobytes() == ocands.tobytes()
+    with pytest.raises(Exception, match="0, 1 or 2"):
+        s.set_profiling(3)
 
 
 # ------------------------------------------------------------------- fold
