@@ -1,7 +1,12 @@
 """Batched search of observations of uneven shape through one CUDA graph
-launch: every observation's candidates equal those of its own search."""
+launch: every observation's candidates equal those of its own search and
+the oracle's."""
+import os
+
 import numpy as np
 import pytest
+
+THREADS = os.cpu_count() or 1
 
 SHAPES = [  # (nchans, nsamples, tsamp, fch1, foff, dm_max, period, dm)
     (64, 1 << 16, 64e-6, 1450.0, -1.5625, 120.0, 0.032, 62.0),
@@ -30,7 +35,7 @@ def plan(i, freqs, tsamp):
 
 
 @pytest.mark.gpu
-def test_batch_graph_equals_individual_searches(gpu):
+def test_batch_graph_equals_individual_searches(gpu, oracle):
     from pulsarsr_gb300 import batch, fbank, rfi, search
     cfg = search.Config(min_hz=1.0, max_hz=2000.0, threshold=8.0, max_candidates=32)
     obs, raws, want = [], [], []
@@ -46,6 +51,14 @@ def test_batch_graph_equals_individual_searches(gpu):
         fb = fbank.decode(raw)
         rfi.mask(fb, block, 8.0)
         want.append(search.search_trials(fb, trials, disc, cfg))
+        # the individual search against the oracle (RFI mask, then every trial)
+        _, d = oracle.decode(raw)
+        md, _ = oracle.rfi_mask(d, block, 8.0)
+        oc, ocands = oracle.search_trials(md, h.frequencies(), h.tsamp, trials, disc,
+                                          threads=THREADS, min_hz=1.0, max_hz=2000.0,
+                                          threshold=8.0, max_candidates=32)
+        assert np.array_equal(want[i][0], oc), i
+        assert want[i][1].tobytes() == ocands.tobytes(), i
     b = batch.Batch(obs, hbm_budget_bytes=1 << 28)  # small budget: several DM blocks
     for i, p in enumerate(raws):
         b.load(i, p)
