@@ -246,6 +246,11 @@ __global__ void __launch_bounds__(DD_NT, 2)
           __ballot_sync(0xffffffffu, lane < DB && (lane == 0 || (myoff >> 2) != (prevoff >> 2)));
       uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0, b0 = 0, b1 = 0, b2 = 0, b3 = 0;
       uint32_t x0 = 0, x1 = 0, x2 = 0, x3 = 0;
+      // 16-bit lanes: the shifted words split into sample pairs once per
+      // offset change, not once per trial
+      uint32_t y[BYTE_LANES ? 1 : 8];
+#pragma unroll
+      for (int i = 0; i < (BYTE_LANES ? 1 : 8); ++i) y[i] = 0;
 #pragma unroll
       for (int d = 0; d < DB; ++d) {
         if (chg & (1u << d)) {
@@ -266,6 +271,16 @@ __global__ void __launch_bounds__(DD_NT, 2)
           x1 = __funnelshift_r(a1, b1, sh);
           x2 = __funnelshift_r(a2, b2, sh);
           x3 = __funnelshift_r(a3, b3, sh);
+          if constexpr (!BYTE_LANES) {
+            y[0] = __byte_perm(x0, 0, 0x4140);
+            y[1] = __byte_perm(x0, 0, 0x4342);
+            y[2] = __byte_perm(x1, 0, 0x4140);
+            y[3] = __byte_perm(x1, 0, 0x4342);
+            y[4] = __byte_perm(x2, 0, 0x4140);
+            y[5] = __byte_perm(x2, 0, 0x4342);
+            y[6] = __byte_perm(x3, 0, 0x4140);
+            y[7] = __byte_perm(x3, 0, 0x4342);
+          }
         }
         if constexpr (BYTE_LANES) {
           acc8[d][0] += x0;
@@ -273,14 +288,8 @@ __global__ void __launch_bounds__(DD_NT, 2)
           acc8[d][2] += x2;
           acc8[d][3] += x3;
         } else {
-          acc[d][0] += __byte_perm(x0, 0, 0x4140);
-          acc[d][1] += __byte_perm(x0, 0, 0x4342);
-          acc[d][2] += __byte_perm(x1, 0, 0x4140);
-          acc[d][3] += __byte_perm(x1, 0, 0x4342);
-          acc[d][4] += __byte_perm(x2, 0, 0x4140);
-          acc[d][5] += __byte_perm(x2, 0, 0x4342);
-          acc[d][6] += __byte_perm(x3, 0, 0x4140);
-          acc[d][7] += __byte_perm(x3, 0, 0x4342);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) acc[d][i] += y[i];
         }
       }
       if (BYTE_LANES && ++gcount == group) {
@@ -848,8 +857,10 @@ std::atomic<int> g_subbands{-1};
 int dedisp_subbands_default(const DeviceObs &o) {
   const int g = g_subbands.load();
   if (g >= 0) return g;
-  // Measured on a GB300: subbands of 8 save about 5% on 8-bit samples at
-  // 4096 channels but cost about 8% at 64-1024 channels; on <= 4-bit samples
+  // Measured on a GB300 with the word-cache channel-by-channel kernel: the
+  // whole 8000-trial survey search (4096 x 8-bit channels, 2^23 samples)
+  // takes 13.39 s with subbands of 8 and 14.13 s channel by channel; at
+  // 64-1024 8-bit channels subbands cost about 8%, and on <= 4-bit samples
   // the byte-lane kernel is faster.  Batches tune it per shape class.
   return o.kind == SAMPLE_U8 && o.h.nbits == 8 && o.nch >= 2048 ? 8 : 0;
 }
