@@ -182,6 +182,17 @@ def measured_traffic(stage):
     return d["dram_bytes_per_launch"] / d["trials_per_launch"]
 
 
+def measured_instructions(stage):
+    """ncu warp instructions per trial for a stage's kernels (profiles/traffic.json)."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p)).get(stage)
+    if not d or "warp_instructions_per_launch" not in d:
+        return None
+    return d["warp_instructions_per_launch"] / d["trials_per_launch"]
+
+
 def max_over_ranks(x: float, dist) -> float:
     """The slowest rank's value (all ranks get it); x itself without a group."""
     if not dist:
@@ -336,8 +347,27 @@ def run_ours(args):
     ms_per_launch = fft_ms / fft_pairs
     alg_per_launch = stage_bytes("fft", obs, trials, discovery, N) / launches_per_search
     achieved = alg_per_launch / (ms_per_launch / 1e3) / 1e9
-    per_trial = measured_traffic("fft")
+    # ncu figures per trial were captured on the GBT-shaped case (the rFFT of
+    # 2^20 points); other shapes report none.
+    gbt = args.config == "c2"
+    per_trial = measured_traffic("fft") if gbt else None
     traffic = per_trial * trials_per_launch if per_trial else None
+    # The rFFT against its issue bound: warp instructions per trial (ncu, the
+    # same kernels on the 64-trial case) over the serialised stage time and
+    # 4 warp instructions per clock per SM at the sampled SM clock.
+    ipt = measured_instructions("fft") if gbt else None
+    fft_iso = stages.get("fft", {}).get("ms_per_search_serialised")
+    issue = None
+    if ipt and fft_iso:
+        nsm_f = C.c_int(0)
+        rt.cudaDeviceGetAttribute(C.byref(nsm_f), C.c_int(16), C.c_int(local))
+        mhz_f = clk.get("sm_mhz") or 2070.0
+        issue = {"warp_instructions_per_trial": round(ipt),
+                 "frac": round(ipt * len(trials) / (fft_iso / 1e3)
+                               / (nsm_f.value * 4 * mhz_f * 1e6), 4),
+                 "basis": "warp instructions per trial (profiles/traffic.json) x trials / "
+                          "serialised FFT stage time, vs 4 warp instructions per clock per "
+                          f"SM x {nsm_f.value} SMs x {mhz_f:.0f} MHz"}
     cpu = cpu_baseline(obs, raw, trials, discovery, args) if not args.no_cpu else None
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
@@ -357,7 +387,7 @@ def run_ours(args):
                      "traffic": int(traffic) if traffic else None,
                      "traffic_source": "profiles/traffic.json (ncu, cold L2), per trial x "
                                        "trials_per_launch",
-                     "peak_source": src},
+                     "peak_source": src, "issue": issue},
         "stages": stages,
         "clocks": clk,
         "candidates": int(counts.sum()),

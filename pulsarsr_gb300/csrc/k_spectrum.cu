@@ -139,9 +139,20 @@ __device__ double score_at(const HarmArgs &a, const float *raw, const float *sc,
   return inv_sqrt_div(__dsub_rn(sum, (double)h), hi);
 }
 
+// Appends a raw candidate.  The lanes of a warp that emit together (all for
+// the CTA's one trial) take consecutive slots: a ballot of the converged
+// lanes, one atomic by the lowest, the base broadcast by a shuffle and each
+// lane's rank among them.  The order of the raw list does not matter:
+// k_select orders it by (score, h, k).
 __device__ void emit(const HarmArgs &a, uint64_t trial, const float *raw, uint64_t k, int hi,
                      double score) {
-  const unsigned slot = atomicAdd(&a.raw_count[trial], 1u);
+  const unsigned mask = __activemask();
+  const int lane = (int)(threadIdx.x & 31);
+  const int leader = __ffs(mask) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(&a.raw_count[trial], (unsigned)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  const unsigned slot = base + (unsigned)__popc(mask & ((1u << lane) - 1u));
   if (slot >= a.raw_cap) {
     atomicOr(a.overflow, 1u);
     return;
