@@ -915,6 +915,11 @@ def main():
     ap.add_argument("--trials", type=int, default=0,
                     help="search only the first N trial DMs (small profiling case)")
     args = ap.parse_args()
+    if args.config == "c3" and args.impl == "ours":
+        # 64 concurrent graph branches: 32 hardware work queues instead of the
+        # default 8 (read when the CUDA context is created, so set before any
+        # CUDA call) measured 5.64 against 5.72 s per batch.
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     if args.impl == "reference":
         run_reference(args)
     else:
