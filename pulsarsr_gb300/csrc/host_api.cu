@@ -334,6 +334,7 @@ struct psr_session {
   uint64_t discovery = 0;
   SpecConfig spec;
   DevBuf errbuf;
+  HostBuf h_err;  // sync()'s copy of errbuf
   bool have_run = false;
   // unpack / rfi timing (the engine times its own stages)
   std::vector<cudaEvent_t> ev[2][2];
@@ -1256,9 +1257,10 @@ int psr_session_sync(psr_session *s) {
     return PSR_EINVAL;
   }
   cudaStream_t st = s->stream.s;
-  unsigned long long e = 0;
-  PSR_CUDA(cudaMemcpyAsync(&e, s->errbuf.p, 8, cudaMemcpyDeviceToHost, st));
+  PSR_TRY(s->h_err.ensure(8));
+  PSR_CUDA(cudaMemcpyAsync(s->h_err.p, s->errbuf.p, 8, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
+  const unsigned long long e = *s->h_err.as<unsigned long long>();
   if (e != ~0ull) {
     set_error("invalid or unsupported filterbank: nonfinite sample at " +
               std::to_string(e / s->o.nch) + "/" + std::to_string(e % s->o.nch));

@@ -59,6 +59,40 @@ __host__ __device__ inline bool f64_sums_exact(double mag, int q) {
 }
 
 // Owning device allocation (sized once, reused).
+// Page-locked host memory, grown on demand and kept across calls (device
+// copies into it run at full link speed, with no staging and no page faults).
+struct HostBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  HostBuf() = default;
+  HostBuf(const HostBuf &) = delete;
+  HostBuf &operator=(const HostBuf &) = delete;
+  ~HostBuf() { release(); }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int ensure(size_t n) {
+    if (n <= bytes && p) return PSR_OK;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      set_error(std::string("CUDA error in cudaHostAlloc(") + std::to_string(n) +
+                " bytes): " + cudaGetErrorString(e));
+      return PSR_ECUDA;
+    }
+    bytes = n;
+    return PSR_OK;
+  }
+  template <class T>
+  T *as() const {
+    return static_cast<T *>(p);
+  }
+};
+
 struct DevBuf {
   void *p = nullptr;
   size_t bytes = 0;

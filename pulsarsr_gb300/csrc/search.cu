@@ -171,11 +171,14 @@ int SearchEngine::enqueue(const DeviceObs &o, cudaStream_t st) {
 }
 
 int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
-  std::vector<unsigned> ov(nchunks);
-  unsigned e = 0;
-  PSR_CUDA(cudaMemcpyAsync(ov.data(), chunk_overflow.p, nchunks * 4, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, st));
+  // per-chunk overflow words, then the dedispersion error word
+  PSR_TRY(h_status.ensure((nchunks + 1) * 4));
+  unsigned *hs = h_status.as<unsigned>();
+  PSR_CUDA(cudaMemcpyAsync(hs, chunk_overflow.p, nchunks * 4, cudaMemcpyDeviceToHost, st));
+  PSR_CUDA(cudaMemcpyAsync(hs + nchunks, err.p, 4, cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
+  std::vector<unsigned> ov(hs, hs + nchunks);
+  const unsigned e = hs[nchunks];
   if (e) {
     set_error("dedispersion: a bounded wait for a staged tile gave up");
     return PSR_ETIMEOUT;
@@ -207,19 +210,24 @@ int SearchEngine::finish(const DeviceObs &o, cudaStream_t st) {
 int SearchEngine::collect(cudaStream_t st, uint64_t *counts, psr_candidate *out, uint64_t cap,
                           uint64_t *n_total) {
   const uint64_t maxc = std::max<uint64_t>(spec.max_candidates, 1);
-  std::vector<unsigned> kc(ntrials);
-  std::vector<psr_candidate> all(ntrials * maxc);
-  PSR_CUDA(cudaMemcpyAsync(kc.data(), kept_count.p, ntrials * 4, cudaMemcpyDeviceToHost, st));
-  PSR_CUDA(cudaMemcpyAsync(all.data(), kept.p, all.size() * sizeof(psr_candidate),
+  PSR_TRY(h_kept_count.ensure(ntrials * 4));
+  PSR_TRY(h_kept.ensure(ntrials * maxc * sizeof(psr_candidate)));
+  PSR_CUDA(cudaMemcpyAsync(h_kept_count.p, kept_count.p, ntrials * 4, cudaMemcpyDeviceToHost,
+                           st));
+  PSR_CUDA(cudaMemcpyAsync(h_kept.p, kept.p, ntrials * maxc * sizeof(psr_candidate),
                            cudaMemcpyDeviceToHost, st));
   PSR_CUDA(cudaStreamSynchronize(st));
+  const unsigned *kc = h_kept_count.as<unsigned>();
+  const psr_candidate *all = h_kept.as<psr_candidate>();
   uint64_t k = 0;
   for (uint64_t i = 0; i < ntrials; ++i) {
     if (counts) counts[i] = kc[i];
-    for (unsigned j = 0; j < kc[i]; ++j) {
-      if (out && k < cap) out[k] = all[i * maxc + j];
-      ++k;
+    // trial i's list, in order, as far as it fits
+    if (out && k < cap) {
+      const uint64_t m = std::min<uint64_t>(kc[i], cap - k);
+      std::memcpy(out + k, all + i * maxc, m * sizeof(psr_candidate));
     }
+    k += kc[i];
   }
   *n_total = k;
   if (out && k > cap) {

@@ -41,6 +41,8 @@ struct SearchEngine {
   ~SearchEngine();
   DevBuf delays, trial_dm, series, parts, sums, means, work, power, psum, kept, kept_count, err,
       chunk_overflow;
+  HostBuf h_kept, h_kept_count;  // collect()'s staging of the kept lists
+  HostBuf h_status;              // finish(): overflow and error words
   // The gates, harmonic items and selection of a chunk run on `aux`, so that
   // they overlap the FFTs of the following inner chunks and of the next
   // chunk on the caller's stream.  ev_fft[i % 2]: FFT of inner chunk i done.

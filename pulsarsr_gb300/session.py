@@ -62,7 +62,7 @@ class SearchSession:
         check(lib().psr_session_candidates(self._s, counts.ctypes.data_as(C.POINTER(C.c_uint64)),
                                            out.ctypes.data_as(C.c_void_p), C.c_uint64(cap),
                                            C.byref(n)))
-        return counts, out[:n.value].copy()
+        return counts, out[:n.value]
 
     def mask(self) -> dict:
         ch = np.zeros(self.nchans, dtype=np.uint64)
