@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(DD_NT, 2)
   };
   if constexpr (PRELOAD) {
     uint32_t *dly = reinterpret_cast<uint32_t *>(smem + 2 * bstride);
-    const unsigned nc = (unsigned)nch;  // <= 4096 when the block is preloaded
+    const unsigned nc = (unsigned)nch;  // DB * nch <= 4096 (16 KB) when preloaded
     for (unsigned i = tl; i < DB * nc; i += DD_NT) {
       const unsigned d = i / nc, c = i - d * nc;
       const uint64_t tr = d0 + d < ntrials ? d0 + d : ntrials - 1;
